@@ -1,0 +1,214 @@
+/*
+ * sodagpu.h — C ABI of the GB300 SODA Gibbs sampler (libsodagpu.so).
+ *
+ * The reference program (SODABayes, Fortran 2018 + OpenMP) has no plugin or FFI
+ * layer: its modules talk through the `globals` module (globals.f90:1-53) and the
+ * SODA sampler is the argument-less `subroutine soda_bayes` (models.f90:9), run
+ * from `run_program_sodaBayes` (SODABayes.f90:112-165) after `setup_soda`
+ * (SODABayes.f90:139).  Each entry point below replaces one step of that call
+ * chain; the comment on each names the reference code it stands in for.
+ *
+ * Conventions
+ *   - Plain C types only; every array is allocated and owned by the caller.
+ *   - Matrices are column-major (Fortran order).  Index arguments that the
+ *     reference keeps 1-based (permvec, SNP groups, mixture classes) stay
+ *     1-based at this boundary.
+ *   - Every function returns 0 on success and a negative SODAGPU_E* code on
+ *     failure; nothing calls exit/abort/stop.  sodagpu_errstr() names the code,
+ *     sodagpu_last_error() gives the message of the last failure on the calling
+ *     thread.
+ *   - One context per host thread.  A context owns one CUDA stream on the
+ *     device that was current when it was created.
+ */
+#ifndef SODAGPU_H
+#define SODAGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SODAGPU_ABI_VERSION 1
+
+#define SODAGPU_MAXDIST 20 /* globals.f90:8  maxdist: mixture classes */
+#define SODAGPU_MAXGRP 100 /* globals.f90:35 maxgrp:  SNP groups       */
+
+/* globals.f90:22  BayesA=1 ... BayesRc=6 */
+enum sodagpu_method {
+    SODAGPU_BAYES_A = 1,
+    SODAGPU_BAYES_B = 2,
+    SODAGPU_BAYES_C = 3,
+    SODAGPU_BAYES_CPI = 4,
+    SODAGPU_BAYES_R = 5,
+    SODAGPU_BAYES_RC = 6
+};
+
+/* Arithmetic of the per-iteration sweep.  The Z build is FP64 in every mode.
+ *   FP64: genotypes as centred/scaled FP64 columns, U in FP64 — the parity mode.
+ *   FP32: genotypes as centred/scaled FP32 columns, U in FP32 — the plain path.
+ *   FP8 : genotypes as exact 8-bit 0/1/2 codes with the centring applied as an
+ *         FP32 rank-1 correction, U as BF16 hi+lo pairs.                      */
+enum sodagpu_precision { SODAGPU_FP64 = 0, SODAGPU_FP32 = 1, SODAGPU_FP8 = 2 };
+
+/* Genotype input layouts for sodagpu_load_genotypes(). */
+enum sodagpu_geno_layout {
+    /* int8 codes 0/1/2, column-major nind x nloci (one SNP per column);
+     * missing calls already mapped to 1 as load_geno does (utilities.f90:446-451). */
+    SODAGPU_GENO_CODES = 0,
+    /* PLINK .bed SNP-major payload without the 3-byte magic header:
+     * nloci records of ceil(nind/4) bytes, decoded like utilities.f90:438-454. */
+    SODAGPU_GENO_BED = 1,
+    /* OR-ed flag: the pointer is device memory on the context's device. */
+    SODAGPU_GENO_DEVICE_PTR = 0x100
+};
+
+/* Error codes (negative). */
+enum sodagpu_status {
+    SODAGPU_OK = 0,
+    SODAGPU_E_ARG = -1,        /* invalid argument or configuration          */
+    SODAGPU_E_STATE = -2,      /* call out of order (e.g. run before build_z) */
+    SODAGPU_E_NOMEM = -3,      /* device or host allocation failed           */
+    SODAGPU_E_CUDA = -4,       /* CUDA runtime / launch error                */
+    SODAGPU_E_NOTPSD = -5,     /* d*I - X'X not positive semidefinite (soda.f90:496-499) */
+    SODAGPU_E_TIMEOUT = -6,    /* a bounded device wait gave up              */
+    SODAGPU_E_NODEVICE = -7,   /* no CUDA device / unsupported architecture  */
+    SODAGPU_E_UNSUPPORTED = -8 /* option combination not implemented         */
+};
+
+/* Job configuration: the values the reference reads from its option table
+ * (useroptions.f90:22-55) after parse() (useroptions.f90:554-572), plus the
+ * GPU-only knobs at the end.  Floating options are passed as the reference holds
+ * them: cast_float() reads them as default REAL (utilities.f90:168-171), so a
+ * drop-in host rounds them through float before widening to double.          */
+typedef struct sodagpu_config {
+    int32_t nind;       /* individuals (get_size, utilities.f90:256-267)        */
+    int32_t nloci;      /* SNPs        (get_size, utilities.f90:268-275)        */
+    int32_t method;     /* enum sodagpu_method (parse_method)                   */
+    int32_t nmix;       /* mixture classes (parse_nmix, useroptions.f90:375-400) */
+    int32_t ngroup;     /* SNP groups, 1 unless BayesRc (get_size 276-301)      */
+    int32_t blocksize;  /* SODA subset size  (setup_soda, soda.f90:407-417)     */
+    int32_t nblocks;    /* number of subsets                                    */
+    int32_t blockt;     /* subsets of full size; the rest hold blocksize-1 SNPs */
+    int32_t numit;      /* -numit  */
+    int32_t burnin;     /* -burnin */
+    int32_t thin;       /* -thin   */
+    int32_t precision;  /* enum sodagpu_precision                                */
+    int32_t chains;     /* independent chains sharing X and Z (>=1)             */
+    int32_t recal_every;/* residual recalibration period, 1000 in models.f90:571 */
+    int64_t seed;       /* -seed (set_random_seed, utilities.f90:504-517)       */
+    double pizero;      /* -pi: fraction of zero-effect SNPs (BayesB/C)         */
+    double scale_va, scale_ve, df_va, df_ve; /* priors (parse_priors)            */
+    double mix[SODAGPU_MAXDIST];   /* -mix   (class variances as share of Va)   */
+    double alpha[SODAGPU_MAXDIST]; /* -alpha (Dirichlet prior)                  */
+    double vara0;       /* value of the module variable `vara` on entry: the
+                           df_va<=0 branch adds to it (models.f90:99-102)       */
+    int32_t reserved[8];
+} sodagpu_config;
+
+/* One thinned iteration of the .hyp trace (models.f90:549-569). */
+typedef struct sodagpu_trace_row {
+    int32_t chain;
+    int32_t rep;        /* iteration, 1-based                                  */
+    int32_t included;   /* ModelSize                                           */
+    int32_t pad;
+    double mu, vare, vara;
+    int32_t snpindist[SODAGPU_MAXDIST]; /* counts for group 1 (ngroup==1 rows)   */
+    double varindist[SODAGPU_MAXDIST];  /* sum g^2 per class, group 1           */
+} sodagpu_trace_row;
+
+typedef void (*sodagpu_trace_cb)(void *user, const sodagpu_trace_row *row);
+
+typedef struct sodagpu_ctx sodagpu_ctx;
+
+/* ---- setup ------------------------------------------------------------- */
+
+/* Block sizing of setup_soda (soda.f90:407-421).  blocksize_opt/nblocks_opt are
+ * the -blocksize/-nblocks options (0 = unset), nthreads the resolved thread
+ * count.  Returns 1 when SODA has to be switched off (blocksize<=1, soda.f90:418),
+ * 0 otherwise. */
+int sodagpu_block_layout(int32_t nloci, int32_t nthreads, int32_t blocksize_opt,
+                         int32_t nblocks_opt, int32_t *blocksize, int32_t *nblocks,
+                         int32_t *blockt);
+
+/* Allocates the device state for one job (allocate_data, utilities.f90:558-586;
+ * the SODA arrays of setup_soda, soda.f90:422-428). */
+int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out);
+
+/* Genotypes (load_geno, utilities.f90:402-460) and their centring and scaling
+ * (xscale, utilities.f90:519-534).  Allele frequencies are computed on the
+ * device; sodagpu_get_freq returns them for the .frq writer. */
+int sodagpu_load_genotypes(sodagpu_ctx *ctx, const void *geno, int32_t layout);
+int sodagpu_get_freq(sodagpu_ctx *ctx, double *freq /* nloci */);
+
+/* Phenotypes (load_pheno, utilities.f90:329-400): nind doubles. */
+int sodagpu_load_pheno(sodagpu_ctx *ctx, const double *y);
+
+/* BayesRc SNP groups (load_snp_grp, utilities.f90:304-327): nloci 1-based ids. */
+int sodagpu_set_groups(sodagpu_ctx *ctx, const int32_t *group);
+
+/* Augmenting matrix (get_aug_matrix, soda.f90:445-518): per subset the exact
+ * genotype Gram (xxproduct, soda.f90:520-556), d = lambda_max + 0.001
+ * (power_method, soda.f90:378-401, 484-486) and the upper Cholesky factor of
+ * d*I - X'X (choleskyPD, soda.f90:8-47) with the pivoted fallback
+ * (choleskyPSD, soda.f90:49-124).  permvec is the 1-based SNP order of
+ * setup_soda (soda.f90:429-435); NULL means identity.  *nskipped receives the
+ * number of SNPs dropped by the pivoted fallback (may be NULL). */
+int sodagpu_build_z(sodagpu_ctx *ctx, const int32_t *permvec, int32_t *nskipped);
+
+/* Test hook: add `delta` to every d_b before the factorisation, which makes
+ * d*I - X'X indefinite for negative delta and exercises the pivoted path. */
+int sodagpu_set_d_offset(sodagpu_ctx *ctx, double delta);
+
+/* Chain initialisation (models.f90:56-128) for all chains. */
+int sodagpu_init_chains(sodagpu_ctx *ctx);
+
+/* Runs `iters` Gibbs iterations of every chain (models.f90:129-574), continuing
+ * the iteration count across calls.  When cb is non-NULL it is called after the
+ * iterations finish, once per chain and thinned iteration, in order. */
+int sodagpu_run(sodagpu_ctx *ctx, int32_t iters, sodagpu_trace_cb cb, void *user);
+
+/* Posterior means (models.f90:575-594) of one chain, any pointer may be NULL:
+ *   gstore[nloci], indiststore[nloci*nmix] (column-major), vara_sstore[nloci],
+ *   scalars[4] = {mu_store, vare_store, vara_store, included_store},
+ *   snpstore/pstore/varstore [ngroup*nmix] (column-major). */
+int sodagpu_get_results(sodagpu_ctx *ctx, int32_t chain, double *gstore,
+                        double *indiststore, double *vara_sstore, double *scalars,
+                        double *snpstore, double *pstore, double *varstore);
+
+/* Current sampler state of one chain (any pointer may be NULL):
+ *   g[nloci], cls[nloci] (1-based class = snptracker(:,2)), vara_s[nloci],
+ *   yadj[nind], yaadj[blocksize], scalars[4] = {mu, vare, vara, included}. */
+int sodagpu_get_state(sodagpu_ctx *ctx, int32_t chain, double *g, int32_t *cls,
+                      double *vara_s, double *yadj, double *yaadj, double *scalars);
+
+/* The augmenting matrix as the reference stores it: XA(blocksize, nloci)
+ * column-major (globals.f90:52) and xxd(nblocks) (any pointer may be NULL),
+ * plus skip flags by position (1 = skipped). */
+int sodagpu_get_z(sodagpu_ctx *ctx, double *xa, double *xxd, int32_t *skip);
+
+/* Genomic values pred = mu + X*effects (compute_dgv, utilities.f90:616-622)
+ * with the context's own genotypes and centring. */
+int sodagpu_compute_dgv(sodagpu_ctx *ctx, double mu, const double *effects,
+                        double *pred /* nind */);
+
+/* Prediction with external frequencies (setup_prediction + xscale's
+ * prediction branch, utilities.f90:540-553, 616-622): genotypes as in
+ * sodagpu_load_genotypes, freq[nloci] from a .frq file. Needs no context. */
+int sodagpu_predict(int32_t nind, int32_t nloci, const void *geno, int32_t layout,
+                    const double *freq, double mu, const double *effects,
+                    double *pred);
+
+/* Seconds spent in the last sodagpu_build_z and sodagpu_run calls. */
+int sodagpu_timings(sodagpu_ctx *ctx, double *build_z_s, double *run_s);
+
+void sodagpu_destroy(sodagpu_ctx *ctx);
+const char *sodagpu_errstr(int code);
+const char *sodagpu_last_error(void);
+int sodagpu_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SODAGPU_H */

@@ -1,0 +1,321 @@
+"""sodabayes_gb300 — GB300-native SODA Gibbs sampler behind SODABayes' entry points.
+
+The compute path is libsodagpu.so (CUDA, sm_103a; C ABI in include/sodagpu.h).
+This module is the Python host mirror of the reference's option handling
+(useroptions.f90) and of its job flow (SODABayes.f90:112-165) on top of that
+ABI.  There is no CPU fallback: without the shared library, or without an
+sm_103a GPU, every call raises SodaGpuError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import (BAYES_A, BAYES_B, BAYES_C, BAYES_CPI, BAYES_R, BAYES_RC, FP8, FP32, FP64, GENO_BED,
+                   GENO_CODES, GENO_DEVICE_PTR, METHODS, PRECISIONS, Config, TraceRow, fround)
+
+__all__ = ["SodaGpuError", "JobOptions", "make_config", "block_layout", "SodaJob", "predict", "library",
+           "METHODS", "PRECISIONS", "TraceRow"]
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libsodagpu.so")
+
+
+class SodaGpuError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str = ""):
+        self.code = code
+        super().__init__(f"{where}: {msg or 'error'} (code {code})")
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def library() -> C.CDLL:
+    """Loads libsodagpu.so (built by sodabayes_gb300.build); raises if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SodaGpuError(-7, "library", f"{LIB_PATH} is missing; run `python -m sodabayes_gb300.build`")
+        _lib = _abi.bind(C.CDLL(LIB_PATH), _abi.PROTOTYPES)
+    return _lib
+
+
+def _check(rc: int, where: str) -> None:
+    if rc != 0:
+        lib = library()
+        msg = lib.sodagpu_last_error().decode(errors="replace")
+        raise SodaGpuError(rc, where, msg or lib.sodagpu_errstr(rc).decode())
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def block_layout(nloci: int, nthreads: int = 1, blocksize: int = 0, nblocks: int = 0):
+    """setup_soda's block sizing (soda.f90:407-421): (blocksize, nblocks, blockt, soda_off)."""
+    bs, nb, bt = C.c_int32(), C.c_int32(), C.c_int32()
+    off = library().sodagpu_block_layout(nloci, nthreads, blocksize, nblocks, C.byref(bs), C.byref(nb), C.byref(bt))
+    if off < 0:
+        _check(off, "sodagpu_block_layout")
+    return bs.value, nb.value, bt.value, bool(off == 1)
+
+
+def block_layout_py(nloci: int, nthreads: int = 1, blocksize: int = 0, nblocks: int = 0):
+    """Pure restatement of soda.f90:407-421 (no library needed)."""
+    import math
+    if blocksize > 0:
+        bs = blocksize
+        nb = math.ceil(nloci / bs)
+        bt = nb
+    elif nblocks > 0:
+        nb = nblocks
+        bs = math.ceil(nloci / nb)
+        bt = nloci - (bs - 1) * nb
+    else:
+        bs = nthreads
+        nb = math.ceil(nloci / max(bs, 1))
+        bt = nb
+    return bs, nb, bt, bs <= 1
+
+
+@dataclass
+class JobOptions:
+    """The option table of useroptions.f90:23-55 that the SODA path reads, with
+    the reference's defaults, plus the GPU knobs (precision, chains)."""
+    method: str = "BayesCpi"
+    pi: float = 0.99
+    scale_va: float = 0.01
+    scale_ve: float = 0.01
+    df_va: float = 0.01
+    df_ve: float = 0.01
+    alpha: Sequence[float] = (1.0,)
+    numit: int = 50000
+    burnin: int = 5000
+    thin: int = 1
+    nmix: int = 2
+    mix: Sequence[float] = (0.0, 1.0)
+    seed: int = 0
+    nthreads: int = 1
+    blocksize: int = 0
+    nblocks: int = 0
+    ngroup: int = 1
+    precision: str = "fp64"
+    chains: int = 1
+    recal_every: int = 1000
+    vara0: float = 0.0
+
+
+def make_config(nind: int, nloci: int, opts: JobOptions) -> Config:
+    """Applies parse_method/parse_nmix/parse_pi/parse_priors/parse_soda
+    (useroptions.f90:375-537) to `opts` and fills the C config struct."""
+    names = {k.lower(): v for k, v in METHODS.items()}
+    m = names.get(opts.method.lower())
+    if m is None:
+        raise ValueError("supported methods: BayesA, BayesB, BayesC, BayesCpi, BayesR, and BayesRc")
+    cfg = Config()
+    cfg.nind, cfg.nloci, cfg.method = nind, nloci, m
+    # parse_nmix (useroptions.f90:375-400)
+    if opts.nmix > _abi.MAXDIST:
+        raise ValueError(f"nmix is too big. maximum allowed: {_abi.MAXDIST}")
+    nmix = 1 if m == BAYES_A else (2 if m in (BAYES_B, BAYES_C, BAYES_CPI) else opts.nmix)
+    cfg.nmix = nmix
+    cfg.ngroup = opts.ngroup if m == BAYES_RC else 1
+    # parse_pi (useroptions.f90:429-440): only BayesB/BayesC read -pi
+    pz = fround(opts.pi)
+    if m in (BAYES_B, BAYES_C) and not (0.0 < pz < 1.0):
+        raise ValueError("pi must be a value between 0 and 1")
+    cfg.pizero = pz
+    cfg.scale_va, cfg.scale_ve = fround(opts.scale_va), fround(opts.scale_ve)
+    cfg.df_va, cfg.df_ve = fround(opts.df_va), fround(opts.df_ve)
+    # parse_priors: -mix and -alpha (useroptions.f90:501-535)
+    for j in range(_abi.MAXDIST):
+        cfg.mix[j] = 0.0
+        cfg.alpha[j] = 0.0
+    if m in (BAYES_C, BAYES_CPI):
+        cfg.mix[0], cfg.mix[1] = 0.0, 1.0
+    elif m in (BAYES_R, BAYES_RC):
+        if len(opts.mix) != nmix:
+            raise ValueError(f"Number of mixture classes {nmix} but {len(opts.mix)} effect sizes specified (mix)")
+        for j, v in enumerate(opts.mix):
+            cfg.mix[j] = fround(v)
+    if m in (BAYES_CPI, BAYES_R, BAYES_RC):
+        al = list(opts.alpha)
+        if len(al) == 1:
+            al = al * nmix
+        elif len(al) != nmix:
+            raise ValueError(f"Number of mixture classes {nmix} but {len(al)} prior values for Dirichlet specified")
+        for j, v in enumerate(al):
+            cfg.alpha[j] = fround(v)
+    cfg.numit, cfg.burnin, cfg.thin, cfg.seed = opts.numit, opts.burnin, opts.thin, opts.seed
+    bs, nb, bt, off = block_layout_py(nloci, opts.nthreads, opts.blocksize, opts.nblocks)
+    if off:
+        raise ValueError("blocksize <= 1: the reference switches SODA off (soda.f90:418-421)")
+    cfg.blocksize, cfg.nblocks, cfg.blockt = bs, nb, bt
+    cfg.precision = PRECISIONS[opts.precision] if isinstance(opts.precision, str) else int(opts.precision)
+    cfg.chains = opts.chains
+    cfg.recal_every = opts.recal_every
+    cfg.vara0 = opts.vara0
+    return cfg
+
+
+class SodaJob:
+    """One SODA job on the GPU: the sequence setup_soda -> soda_bayes of
+    SODABayes.f90:139-142 through the C ABI."""
+
+    def __init__(self, cfg: Config):
+        self.cfg = cfg
+        self._lib = library()
+        self._ctx = C.c_void_p()
+        _check(self._lib.sodagpu_create(C.byref(cfg), C.byref(self._ctx)), "sodagpu_create")
+        self.n, self.p, self.chains = cfg.nind, cfg.nloci, cfg.chains
+
+    def close(self) -> None:
+        if self._ctx:
+            self._lib.sodagpu_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- setup -----------------------------------------------------------------
+    def load_genotypes(self, codes=None, bed: Optional[np.ndarray] = None, device_ptr: Optional[int] = None,
+                       layout: int = GENO_CODES) -> None:
+        """codes: int8 (nind, nloci) 0/1/2 (column-major is copied as-is);
+        bed: uint8 PLINK payload without the magic header;
+        device_ptr: a device address holding `layout` data."""
+        if device_ptr is not None:
+            _check(self._lib.sodagpu_load_genotypes(self._ctx, C.c_void_p(device_ptr), layout | GENO_DEVICE_PTR),
+                   "sodagpu_load_genotypes")
+            return
+        if bed is not None:
+            b = np.ascontiguousarray(bed, dtype=np.uint8)
+            _check(self._lib.sodagpu_load_genotypes(self._ctx, b.ctypes.data_as(C.c_void_p), GENO_BED),
+                   "sodagpu_load_genotypes")
+            return
+        g = np.asfortranarray(codes, dtype=np.int8)
+        if g.shape != (self.n, self.p):
+            raise ValueError(f"codes must be ({self.n}, {self.p}), got {g.shape}")
+        _check(self._lib.sodagpu_load_genotypes(self._ctx, g.ctypes.data_as(C.c_void_p), GENO_CODES),
+               "sodagpu_load_genotypes")
+
+    def freq(self) -> np.ndarray:
+        out = np.empty(self.p)
+        _check(self._lib.sodagpu_get_freq(self._ctx, _dp(out)), "sodagpu_get_freq")
+        return out
+
+    def load_pheno(self, y) -> None:
+        yy = np.ascontiguousarray(y, dtype=np.float64)
+        _check(self._lib.sodagpu_load_pheno(self._ctx, _dp(yy)), "sodagpu_load_pheno")
+
+    def set_groups(self, groups) -> None:
+        gg = np.ascontiguousarray(groups, dtype=np.int32)
+        _check(self._lib.sodagpu_set_groups(self._ctx, _ip(gg)), "sodagpu_set_groups")
+
+    def set_d_offset(self, delta: float) -> None:
+        _check(self._lib.sodagpu_set_d_offset(self._ctx, float(delta)), "sodagpu_set_d_offset")
+
+    def build_z(self, permvec=None) -> int:
+        nsk = C.c_int32()
+        pv = None if permvec is None else np.ascontiguousarray(permvec, dtype=np.int32)
+        _check(self._lib.sodagpu_build_z(self._ctx, None if pv is None else _ip(pv), C.byref(nsk)),
+               "sodagpu_build_z")
+        return nsk.value
+
+    def init_chains(self) -> None:
+        _check(self._lib.sodagpu_init_chains(self._ctx), "sodagpu_init_chains")
+
+    # -- sampling --------------------------------------------------------------
+    def run(self, iters: int, trace: Optional[Callable[[TraceRow], None]] = None) -> None:
+        if trace is None:
+            cb = _abi.TRACE_CB()
+        else:
+            cb = _abi.TRACE_CB(lambda user, row: trace(row.contents))
+        _check(self._lib.sodagpu_run(self._ctx, int(iters), cb, None), "sodagpu_run")
+
+    def state(self, chain: int = 0) -> dict:
+        g = np.empty(self.p)
+        cls = np.empty(self.p, dtype=np.int32)
+        vs = np.empty(self.p)
+        r = np.empty(self.n)
+        ra = np.empty(self.cfg.blocksize)
+        sc = np.empty(4)
+        _check(self._lib.sodagpu_get_state(self._ctx, chain, _dp(g), _ip(cls), _dp(vs), _dp(r), _dp(ra), _dp(sc)),
+               "sodagpu_get_state")
+        return {"g": g, "cls": cls, "vara_s": vs, "yadj": r, "yaadj": ra, "mu": sc[0], "vare": sc[1],
+                "vara": sc[2], "included": int(sc[3])}
+
+    def results(self, chain: int = 0) -> dict:
+        p, nm, ng = self.p, self.cfg.nmix, self.cfg.ngroup
+        gs = np.empty(p)
+        ind = np.empty((p, nm), order="F")
+        vss = np.empty(p)
+        sc = np.empty(4)
+        snp = np.empty((ng, nm), order="F")
+        pst = np.empty((ng, nm), order="F")
+        var = np.empty((ng, nm), order="F")
+        _check(self._lib.sodagpu_get_results(self._ctx, chain, _dp(gs), ind.ctypes.data_as(C.POINTER(C.c_double)),
+                                             _dp(vss), _dp(sc), snp.ctypes.data_as(C.POINTER(C.c_double)),
+                                             pst.ctypes.data_as(C.POINTER(C.c_double)),
+                                             var.ctypes.data_as(C.POINTER(C.c_double))), "sodagpu_get_results")
+        return {"gstore": gs, "indiststore": ind, "vara_sstore": vss, "mu_store": sc[0], "vare_store": sc[1],
+                "vara_store": sc[2], "included_store": sc[3], "snpstore": snp, "pstore": pst, "varstore": var}
+
+    def z(self):
+        xa = np.empty((self.cfg.blocksize, self.p), order="F")
+        xxd = np.empty(self.cfg.nblocks)
+        skip = np.empty(self.p, dtype=np.int32)
+        _check(self._lib.sodagpu_get_z(self._ctx, xa.ctypes.data_as(C.POINTER(C.c_double)), _dp(xxd), _ip(skip)),
+               "sodagpu_get_z")
+        return xa, xxd, skip
+
+    def compute_dgv(self, mu: float, effects) -> np.ndarray:
+        e = np.ascontiguousarray(effects, dtype=np.float64)
+        out = np.empty(self.n)
+        _check(self._lib.sodagpu_compute_dgv(self._ctx, float(mu), _dp(e), _dp(out)), "sodagpu_compute_dgv")
+        return out
+
+    def timings(self):
+        b, r = C.c_double(), C.c_double()
+        _check(self._lib.sodagpu_timings(self._ctx, C.byref(b), C.byref(r)), "sodagpu_timings")
+        return b.value, r.value
+
+
+def predict(codes=None, freq=None, mu: float = 0.0, effects=None, bed: Optional[np.ndarray] = None,
+            nind: Optional[int] = None) -> np.ndarray:
+    """Prediction mode (utilities.f90:540-553, 616-622): mu + X*effects with
+    the centring of an external .frq file."""
+    lib = library()
+    fr = np.ascontiguousarray(freq, dtype=np.float64)
+    e = np.ascontiguousarray(effects, dtype=np.float64)
+    p = fr.shape[0]
+    if bed is not None:
+        n = int(nind)
+        buf = np.ascontiguousarray(bed, dtype=np.uint8)
+        layout = GENO_BED
+    else:
+        g = np.asfortranarray(codes, dtype=np.int8)
+        n = g.shape[0]
+        buf = g
+        layout = GENO_CODES
+    out = np.empty(n)
+    _check(lib.sodagpu_predict(n, p, buf.ctypes.data_as(C.c_void_p), layout, _dp(fr), float(mu), _dp(e), _dp(out)),
+           "sodagpu_predict")
+    return out

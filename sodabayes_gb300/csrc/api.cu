@@ -1,0 +1,972 @@
+// api.cu — the C ABI of libsodagpu.so (declared in include/sodagpu.h).
+//
+// Host-side orchestration only: every array operation runs in the kernels of
+// zbuild.cu and sweep.cu.  The host computes block bounds, prefix sums of the
+// factor column lengths, the top eigenvalue of the small Lanczos tridiagonal
+// matrices, and formats results.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/sodagpu.h"
+#include "state.cuh"
+#include "sweep.cuh"
+#include "zbuild.cuh"
+
+using namespace soda;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t _e = (expr);                                                           \
+        if (_e != cudaSuccess)                                                             \
+            return fail(SODAGPU_E_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                        __FILE__, __LINE__);                                               \
+    } while (0)
+
+inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Largest eigenvalue of the symmetric tridiagonal matrix (a[0..m), b[0..m-1))
+// by Sturm-sequence bisection.
+double tridiag_max_eig(const double *a, const double *b, int m)
+{
+    double lo = a[0], hi = a[0];
+    for (int i = 0; i < m; ++i) {
+        const double r = (i > 0 ? fabs(b[i - 1]) : 0.0) + (i + 1 < m ? fabs(b[i]) : 0.0);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+    }
+    auto count_below = [&](double x) {
+        int cnt = 0;
+        double q = a[0] - x;
+        if (q < 0) ++cnt;
+        for (int i = 1; i < m; ++i) {
+            const double qq = q != 0.0 ? q : 1e-300;
+            q = a[i] - x - b[i - 1] * b[i - 1] / qq;
+            if (q < 0) ++cnt;
+        }
+        return cnt;
+    };
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (count_below(mid) == m) hi = mid;
+        else lo = mid;
+    }
+    return hi;
+}
+
+}  // namespace
+
+struct sodagpu_ctx {
+    sodagpu_config cfg;
+    int dev = 0, sm_count = 0;
+    cudaStream_t st = nullptr;
+    int n = 0, p = 0, bs = 0, nb = 0, bt = 0, C = 0, ldx = 0, ldr = 0, nr_ctas = 0;
+    int nskipped = 0, naind = 0;
+    double d_offset = 0.0;
+    bool have_geno = false, have_pheno = false, have_z = false, have_chain = false;
+    std::vector<void *> allocs;
+    std::vector<int32_t> blk_sizes, h_blk_ls;
+    // device
+    int8_t *Gsnp = nullptr, *G = nullptr;
+    float *X32 = nullptr;
+    double *xv = nullptr, *freq = nullptr, *y = nullptr;
+    int64_t *uoff = nullptr;
+    int32_t *ulen = nullptr;
+    double *U64 = nullptr;
+    float *U32 = nullptr;
+    __nv_bfloat16 *Uhi = nullptr, *Ulo = nullptr;
+    double *xxd = nullptr, *xpx = nullptr;
+    int32_t *perm = nullptr, *pos_of = nullptr, *iskipped = nullptr, *grp = nullptr, *blk_ls = nullptr;
+    uint8_t *skip = nullptr;
+    double *r = nullptr, *ra = nullptr, *g = nullptr, *vara_s = nullptr, *gstore = nullptr,
+           *vara_sstore = nullptr;
+    float *r32 = nullptr;
+    int32_t *cls = nullptr;
+    uint32_t *indist = nullptr;
+    ChainScal *scal = nullptr;
+    RunCtl *ctl = nullptr;
+    double *delta = nullptr, *rpart = nullptr, *rsum = nullptr, *statpart = nullptr, *recal_part = nullptr;
+    int32_t *cntpart = nullptr;
+    uint8_t *nzflag = nullptr;
+    sodagpu_trace_row *trace = nullptr;
+    int trace_cap = 0;
+    cudaGraphExec_t graph = nullptr;
+    double t_build = 0.0, t_run = 0.0;
+    Dev D;
+
+    template <class T>
+    int alloc(T **ptr, size_t count, bool zero = true)
+    {
+        void *p_ = nullptr;
+        const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+        cudaError_t e = cudaMalloc(&p_, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SODAGPU_E_NOMEM, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        }
+        if (zero) {
+            e = cudaMemsetAsync(p_, 0, bytes, st);
+            if (e != cudaSuccess) return fail(SODAGPU_E_CUDA, "cudaMemset failed: %s", cudaGetErrorString(e));
+        }
+        allocs.push_back(p_);
+        *ptr = (T *)p_;
+        return 0;
+    }
+    void release(void *p_)
+    {
+        if (!p_) return;
+        auto it = std::find(allocs.begin(), allocs.end(), p_);
+        if (it != allocs.end()) allocs.erase(it);
+        cudaFree(p_);
+    }
+};
+
+#define TRY(expr)                 \
+    do {                          \
+        int _rc = (expr);         \
+        if (_rc != 0) return _rc; \
+    } while (0)
+
+extern "C" {
+
+int sodagpu_abi_version(void) { return SODAGPU_ABI_VERSION; }
+
+const char *sodagpu_errstr(int code)
+{
+    switch (code) {
+    case SODAGPU_OK: return "ok";
+    case SODAGPU_E_ARG: return "invalid argument";
+    case SODAGPU_E_STATE: return "call out of order";
+    case SODAGPU_E_NOMEM: return "out of memory";
+    case SODAGPU_E_CUDA: return "CUDA error";
+    case SODAGPU_E_NOTPSD: return "d*I - X'X is not positive semidefinite";
+    case SODAGPU_E_TIMEOUT: return "device wait timed out";
+    case SODAGPU_E_NODEVICE: return "no usable CUDA device";
+    case SODAGPU_E_UNSUPPORTED: return "unsupported option combination";
+    default: return "unknown error";
+    }
+}
+
+const char *sodagpu_last_error(void) { return g_last_error.c_str(); }
+
+int sodagpu_block_layout(int32_t nloci, int32_t nthreads, int32_t blocksize_opt, int32_t nblocks_opt,
+                         int32_t *blocksize, int32_t *nblocks, int32_t *blockt)
+{
+    if (nloci < 1 || !blocksize || !nblocks || !blockt) return fail(SODAGPU_E_ARG, "bad block layout arguments");
+    int32_t bsz, nbk, bt;
+    if (blocksize_opt > 0) {            // soda.f90:407-409
+        bsz = blocksize_opt;
+        nbk = (int32_t)ceil((double)nloci / bsz);
+        bt = nbk;
+    } else if (nblocks_opt > 0) {       // soda.f90:410-412
+        nbk = nblocks_opt;
+        bsz = (int32_t)ceil((double)nloci / nbk);
+        bt = nloci - (bsz - 1) * nbk;
+    } else {                            // soda.f90:413-416
+        bsz = nthreads;
+        nbk = (int32_t)ceil((double)nloci / (bsz > 0 ? bsz : 1));
+        bt = nbk;
+    }
+    *blocksize = bsz;
+    *nblocks = nbk;
+    *blockt = bt;
+    return bsz <= 1 ? 1 : 0;           // soda.f90:418-421
+}
+
+int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out)
+{
+    if (!cfg || !out) return fail(SODAGPU_E_ARG, "null argument");
+    *out = nullptr;
+    if (cfg->nind < 2 || cfg->nloci < 1) return fail(SODAGPU_E_ARG, "nind must be >= 2 and nloci >= 1");
+    if (cfg->method < 1 || cfg->method > 6) return fail(SODAGPU_E_ARG, "method %d out of range", cfg->method);
+    if (cfg->nmix < 1 || cfg->nmix > SODAGPU_MAXDIST) return fail(SODAGPU_E_ARG, "nmix out of range");
+    if (cfg->ngroup < 1 || cfg->ngroup > SODAGPU_MAXGRP) return fail(SODAGPU_E_ARG, "ngroup out of range");
+    if (cfg->method == SODAGPU_BAYES_A && cfg->nmix != 1) return fail(SODAGPU_E_ARG, "BayesA needs nmix=1");
+    if ((cfg->method >= SODAGPU_BAYES_B && cfg->method <= SODAGPU_BAYES_CPI) && cfg->nmix != 2)
+        return fail(SODAGPU_E_ARG, "BayesB/C/Cpi need nmix=2");
+    if (cfg->method != SODAGPU_BAYES_RC && cfg->ngroup != 1) return fail(SODAGPU_E_ARG, "ngroup>1 needs BayesRc");
+    if (cfg->blocksize < 2 || cfg->nblocks < 1 || cfg->blockt < 0 || cfg->blockt > cfg->nblocks)
+        return fail(SODAGPU_E_ARG, "invalid SODA block layout");
+    if (cfg->thin < 1 || cfg->numit < 0 || cfg->burnin < 0) return fail(SODAGPU_E_ARG, "bad numit/burnin/thin");
+    if (cfg->precision < 0 || cfg->precision > 2) return fail(SODAGPU_E_ARG, "precision out of range");
+    if (cfg->chains < 1 || !sweep_chain_count_supported(cfg->chains))
+        return fail(SODAGPU_E_UNSUPPORTED, "chains must be 1, 2, 4, 8 or 16");
+    for (int j = 1; j < cfg->nmix; ++j)
+        if (cfg->method >= SODAGPU_BAYES_C && !(cfg->mix[j] > 0.0))
+            return fail(SODAGPU_E_ARG, "mix[%d] must be > 0", j);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SODAGPU_E_NODEVICE, "no CUDA device visible");
+    }
+    sodagpu_ctx *c = new (std::nothrow) sodagpu_ctx();
+    if (!c) return fail(SODAGPU_E_NOMEM, "host allocation failed");
+    c->cfg = *cfg;
+    cudaGetDevice(&c->dev);
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, c->dev);
+    if (prop.major != 10 || prop.minor != 3) {
+        delete c;
+        return fail(SODAGPU_E_NODEVICE, "libsodagpu is built for sm_103a; device %d is sm_%d%d (%s)", c->dev,
+                    prop.major, prop.minor, prop.name);
+    }
+    c->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return fail(SODAGPU_E_CUDA, "stream creation failed");
+    }
+    c->n = cfg->nind;
+    c->p = cfg->nloci;
+    c->bs = cfg->blocksize;
+    c->nb = cfg->nblocks;
+    c->bt = cfg->blockt;
+    c->C = cfg->chains;
+    c->ldx = (int)round_up((size_t)c->n, 128);
+    c->ldr = c->ldx;
+    c->nr_ctas = (c->n + ROW_THREADS - 1) / ROW_THREADS;
+    // block bounds (models.f90:136-142), 0-based first positions
+    c->h_blk_ls.resize(c->nb + 1);
+    c->blk_sizes.resize(c->nb);
+    for (int b = 0; b < c->nb; ++b) {
+        const int blocki = b + 1;
+        int ls, le;
+        if (blocki <= c->bt) {
+            ls = (blocki - 1) * c->bs + 1;
+            le = std::min(ls + c->bs - 1, c->p);
+        } else {
+            ls = c->bs * c->bt + (blocki - c->bt - 1) * (c->bs - 1) + 1;
+            le = std::min(ls + c->bs - 2, c->p);
+        }
+        if (le < ls) {
+            sodagpu_destroy(c);
+            return fail(SODAGPU_E_ARG, "empty SODA block %d", blocki);
+        }
+        c->h_blk_ls[b] = ls - 1;
+        c->blk_sizes[b] = le - ls + 1;
+    }
+    c->h_blk_ls[c->nb] = c->h_blk_ls[c->nb - 1] + c->blk_sizes[c->nb - 1];
+    if (c->h_blk_ls[c->nb] != c->p) {
+        sodagpu_destroy(c);
+        return fail(SODAGPU_E_ARG, "blocks cover %d of %d SNPs", c->h_blk_ls[c->nb], c->p);
+    }
+    if (sweep_prepare(c->bs) != cudaSuccess) {
+        sodagpu_destroy(c);
+        return fail(SODAGPU_E_UNSUPPORTED, "blocksize %d too large", c->bs);
+    }
+    int rc = 0;
+    rc = rc ? rc : c->alloc(&c->Gsnp, (size_t)c->p * c->ldx);
+    rc = rc ? rc : c->alloc(&c->freq, c->p);
+    rc = rc ? rc : c->alloc(&c->y, c->n);
+    rc = rc ? rc : c->alloc(&c->grp, c->p);
+    rc = rc ? rc : c->alloc(&c->blk_ls, c->nb + 1);
+    rc = rc ? rc : c->alloc(&c->ctl, 1);
+    if (rc) {
+        sodagpu_destroy(c);
+        return rc;
+    }
+    std::vector<int32_t> ones(c->p, 1);
+    cudaMemcpyAsync(c->grp, ones.data(), sizeof(int32_t) * c->p, cudaMemcpyHostToDevice, c->st);
+    cudaMemcpyAsync(c->blk_ls, c->h_blk_ls.data(), sizeof(int32_t) * (c->nb + 1), cudaMemcpyHostToDevice, c->st);
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) {
+        sodagpu_destroy(c);
+        return fail(SODAGPU_E_CUDA, "initial copies failed");
+    }
+    *out = c;
+    return 0;
+}
+
+int sodagpu_load_genotypes(sodagpu_ctx *c, const void *geno, int32_t layout)
+{
+    if (!c || !geno) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->Gsnp) return fail(SODAGPU_E_STATE, "genotypes already consumed by sodagpu_build_z");
+    const bool on_dev = (layout & SODAGPU_GENO_DEVICE_PTR) != 0;
+    const int kind = layout & 0xff;
+    const cudaMemcpyKind mk = on_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (kind == SODAGPU_GENO_CODES) {
+        CUDA_TRY(cudaMemcpy2DAsync(c->Gsnp, c->ldx, geno, c->n, c->n, c->p, mk, c->st));
+    } else if (kind == SODAGPU_GENO_BED) {
+        const size_t rec = ((size_t)c->n + 3) / 4;
+        uint8_t *tmp = nullptr;
+        TRY(c->alloc(&tmp, rec * c->p, false));
+        CUDA_TRY(cudaMemcpyAsync(tmp, geno, rec * c->p, mk, c->st));
+        CUDA_TRY(zb_decode_bed(tmp, c->n, c->p, c->Gsnp, c->ldx, c->st));
+        CUDA_TRY(cudaStreamSynchronize(c->st));
+        c->release(tmp);
+    } else {
+        return fail(SODAGPU_E_ARG, "unknown genotype layout %d", layout);
+    }
+    int *bad = nullptr, h_bad = 0;
+    TRY(c->alloc(&bad, 1));
+    CUDA_TRY(zb_freq(c->Gsnp, c->n, c->p, c->ldx, c->freq, bad, c->st));
+    CUDA_TRY(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->release(bad);
+    if (h_bad) return fail(SODAGPU_E_ARG, "%d genotype codes outside 0..2", h_bad);
+    c->have_geno = true;
+    return 0;
+}
+
+int sodagpu_get_freq(sodagpu_ctx *c, double *freq)
+{
+    if (!c || !freq) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_geno) return fail(SODAGPU_E_STATE, "no genotypes loaded");
+    CUDA_TRY(cudaMemcpyAsync(freq, c->freq, sizeof(double) * c->p, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sodagpu_load_pheno(sodagpu_ctx *c, const double *y)
+{
+    if (!c || !y) return fail(SODAGPU_E_ARG, "null argument");
+    for (int i = 0; i < c->n; ++i)
+        if (!std::isfinite(y[i])) return fail(SODAGPU_E_ARG, "phenotype %d is not finite", i + 1);
+    CUDA_TRY(cudaMemcpyAsync(c->y, y, sizeof(double) * c->n, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->have_pheno = true;
+    return 0;
+}
+
+int sodagpu_set_groups(sodagpu_ctx *c, const int32_t *group)
+{
+    if (!c || !group) return fail(SODAGPU_E_ARG, "null argument");
+    for (int j = 0; j < c->p; ++j)
+        if (group[j] < 1 || group[j] > c->cfg.ngroup)
+            return fail(SODAGPU_E_ARG, "group of SNP %d is %d, outside 1..%d", j + 1, group[j], c->cfg.ngroup);
+    CUDA_TRY(cudaMemcpyAsync(c->grp, group, sizeof(int32_t) * c->p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sodagpu_set_d_offset(sodagpu_ctx *c, double delta)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    c->d_offset = delta;
+    return 0;
+}
+
+int sodagpu_build_z(sodagpu_ctx *c, const int32_t *permvec, int32_t *nskipped_out)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_geno || !c->Gsnp) return fail(SODAGPU_E_STATE, "load genotypes before sodagpu_build_z");
+    if (c->have_z) return fail(SODAGPU_E_STATE, "sodagpu_build_z already ran on this context");
+    const auto t0 = std::chrono::steady_clock::now();
+    const int p = c->p, n = c->n, bs = c->bs, nb = c->nb;
+    std::vector<int32_t> h_perm(p), h_pos(p, -1);
+    for (int k = 0; k < p; ++k) {
+        const int v = permvec ? permvec[k] - 1 : k;
+        if (v < 0 || v >= p || h_pos[v] != -1) return fail(SODAGPU_E_ARG, "permvec is not a permutation of 1..nloci");
+        h_perm[k] = v;
+        h_pos[v] = k;
+    }
+    TRY(c->alloc(&c->perm, p, false));
+    TRY(c->alloc(&c->pos_of, p, false));
+    TRY(c->alloc(&c->G, (size_t)p * c->ldx, false));
+    TRY(c->alloc(&c->xv, (size_t)p * 4, false));
+    TRY(c->alloc(&c->xxd, nb));
+    TRY(c->alloc(&c->ulen, p));
+    TRY(c->alloc(&c->uoff, p + 1));
+    TRY(c->alloc(&c->skip, p));
+    CUDA_TRY(cudaMemcpyAsync(c->perm, h_perm.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaMemcpyAsync(c->pos_of, h_pos.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(zb_gather(c->Gsnp, c->G, c->perm, p, c->ldx, c->st));
+    CUDA_TRY(zb_xv(c->freq, c->perm, p, c->xv, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->release(c->Gsnp);
+    c->Gsnp = nullptr;
+    if (c->cfg.precision == SODAGPU_FP32) {
+        TRY(c->alloc(&c->X32, (size_t)p * c->ldx, false));
+        CUDA_TRY(zb_x32(c->G, c->xv, c->X32, n, p, c->ldx, c->st));
+    }
+    // FP64 work matrices of every subset
+    std::vector<int64_t> wofs(nb);
+    int64_t wtot = 0;
+    int maxN = 0;
+    for (int b = 0; b < nb; ++b) {
+        wofs[b] = wtot;
+        wtot += (int64_t)c->blk_sizes[b] * c->blk_sizes[b];
+        maxN = std::max(maxN, c->blk_sizes[b]);
+    }
+    double *W = nullptr;
+    int64_t *d_wofs = nullptr;
+    TRY(c->alloc(&W, (size_t)wtot, false));
+    TRY(c->alloc(&d_wofs, nb, false));
+    CUDA_TRY(cudaMemcpyAsync(d_wofs, wofs.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice, c->st));
+    const int BATCH = std::min(nb, 64);
+    const int mmax = std::min(maxN, 400);
+    CUDA_TRY(zb_lz_prepare(maxN, mmax));
+    double *V = nullptr, *wvec = nullptr, *alpha = nullptr, *beta = nullptr;
+    int64_t *d_vofs = nullptr;
+    int32_t *d_batch = nullptr, *d_status = nullptr;
+    uint8_t *d_done = nullptr;
+    TRY(c->alloc(&V, (size_t)BATCH * mmax * maxN));
+    TRY(c->alloc(&wvec, (size_t)BATCH * maxN));
+    TRY(c->alloc(&alpha, (size_t)BATCH * mmax));
+    TRY(c->alloc(&beta, (size_t)BATCH * mmax));
+    TRY(c->alloc(&d_vofs, BATCH, false));
+    TRY(c->alloc(&d_batch, BATCH, false));
+    TRY(c->alloc(&d_status, nb));
+    TRY(c->alloc(&d_done, BATCH));
+    std::vector<int64_t> vofs(BATCH);
+    for (int i = 0; i < BATCH; ++i) vofs[i] = (int64_t)i * mmax * maxN;
+    CUDA_TRY(cudaMemcpyAsync(d_vofs, vofs.data(), sizeof(int64_t) * BATCH, cudaMemcpyHostToDevice, c->st));
+    std::vector<double> h_xxd(nb), ha((size_t)BATCH * mmax), hb((size_t)BATCH * mmax);
+    std::vector<int32_t> h_status(nb, 0);
+    std::vector<int32_t> batch_ids;
+    const float shift_f = 0.001f;   // soda.f90:485 adds a REAL literal
+    for (int b0 = 0; b0 < nb; b0 += BATCH) {
+        const int nbat = std::min(BATCH, nb - b0);
+        batch_ids.resize(nbat);
+        int bmax = 0;
+        for (int i = 0; i < nbat; ++i) {
+            batch_ids[i] = b0 + i;
+            bmax = std::max(bmax, c->blk_sizes[b0 + i]);
+        }
+        CUDA_TRY(cudaMemcpyAsync(d_batch, batch_ids.data(), sizeof(int32_t) * nbat, cudaMemcpyHostToDevice, c->st));
+        CUDA_TRY(zb_gram(c->G, c->ldx, c->blk_ls, d_batch, nbat, bmax, d_wofs, c->freq, c->perm, n, W, c->st));
+        // Lanczos for lambda_max of each subset
+        CUDA_TRY(cudaMemsetAsync(d_done, 0, BATCH, c->st));
+        CUDA_TRY(cudaMemsetAsync(alpha, 0, sizeof(double) * BATCH * mmax, c->st));
+        CUDA_TRY(cudaMemsetAsync(beta, 0, sizeof(double) * BATCH * mmax, c->st));
+        CUDA_TRY(zb_lz_init(c->blk_ls, d_batch, nbat, d_vofs, V, (uint64_t)llabs(c->cfg.seed), c->st));
+        std::vector<uint8_t> done(nbat, 0);
+        std::vector<double> theta(nbat, 0.0), theta_prev(nbat, -1.0);
+        std::vector<int> steps(nbat, 0);
+        const int bmm = std::min(bmax, mmax);
+        for (int j = 0; j < bmm; ++j) {
+            CUDA_TRY(zb_lz_step(W, d_wofs, c->blk_ls, d_batch, nbat, bmax, d_vofs, V, wvec, maxN, alpha, beta, mmax,
+                                j, d_done, c->st));
+            const bool check = ((j + 1) % 8 == 0) || j + 1 == bmm;
+            if (!check) continue;
+            CUDA_TRY(cudaMemcpyAsync(ha.data(), alpha, sizeof(double) * nbat * mmax, cudaMemcpyDeviceToHost, c->st));
+            CUDA_TRY(cudaMemcpyAsync(hb.data(), beta, sizeof(double) * nbat * mmax, cudaMemcpyDeviceToHost, c->st));
+            CUDA_TRY(cudaStreamSynchronize(c->st));
+            bool all = true;
+            for (int i = 0; i < nbat; ++i) {
+                if (done[i]) continue;
+                const int Nb = c->blk_sizes[b0 + i];
+                const int m = std::min(j + 1, Nb);
+                const double *a = &ha[(size_t)i * mmax];
+                const double *bb = &hb[(size_t)i * mmax];
+                theta[i] = tridiag_max_eig(a, bb, m);
+                steps[i] = m;
+                const double scale = std::max(fabs(theta[i]), 1e-300);
+                bool conv = false;
+                if (m >= Nb) conv = true;   // full Krylov space: exact
+                for (int t = 0; t < m && !conv; ++t)
+                    if (bb[t] <= 1e-13 * scale) conv = true;   // invariant subspace
+                if (!conv && theta_prev[i] >= 0.0 && fabs(theta[i] - theta_prev[i]) <= 1e-15 * scale) conv = true;
+                theta_prev[i] = theta[i];
+                if (conv) done[i] = 1;
+                else all = false;
+            }
+            CUDA_TRY(cudaMemcpyAsync(d_done, done.data(), nbat, cudaMemcpyHostToDevice, c->st));
+            if (all) break;
+        }
+        for (int i = 0; i < nbat; ++i)
+            h_xxd[b0 + i] = fabs(theta[i]) + (double)shift_f + c->d_offset;
+        CUDA_TRY(cudaMemcpyAsync(c->xxd + b0, &h_xxd[b0], sizeof(double) * nbat, cudaMemcpyHostToDevice, c->st));
+        CUDA_TRY(zb_form_m(W, d_wofs, c->blk_ls, d_batch, nbat, c->xxd, c->st));
+        CUDA_TRY(zb_cholesky(W, d_wofs, c->blk_ls, d_batch, nbat, bmax, d_status, c->st));
+        CUDA_TRY(zb_pd_lengths(c->blk_ls, d_batch, nbat, d_status, c->ulen, c->skip, c->st));
+        CUDA_TRY(cudaStreamSynchronize(c->st));
+    }
+    CUDA_TRY(cudaMemcpyAsync(h_status.data(), d_status, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    // pivoted fallback for the subsets whose factorisation failed (soda.f90:492-510)
+    std::vector<int32_t> h_iskipped;
+    int naless = p;
+    {
+        double *M = nullptr, *work = nullptr;
+        int32_t *piv = nullptr, *rank = nullptr, *pst = nullptr;
+        bool any_fail = false;
+        for (int b = 0; b < nb; ++b) any_fail |= h_status[b] != 0;
+        if (any_fail) {
+            TRY(c->alloc(&M, (size_t)maxN * maxN, false));
+            TRY(c->alloc(&work, (size_t)2 * maxN));
+            TRY(c->alloc(&piv, maxN));
+            TRY(c->alloc(&rank, 1));
+            TRY(c->alloc(&pst, 1));
+        }
+        std::vector<int32_t> hpiv(maxN);
+        int nsk = 0;
+        for (int b = 0; b < nb; ++b) {
+            const int N = c->blk_sizes[b];
+            if (h_status[b] != 0) {
+                int32_t one = b;
+                CUDA_TRY(cudaMemcpyAsync(d_batch, &one, sizeof(int32_t), cudaMemcpyHostToDevice, c->st));
+                CUDA_TRY(zb_gram(c->G, c->ldx, c->blk_ls, d_batch, 1, N, d_wofs, c->freq, c->perm, n, W, c->st));
+                CUDA_TRY(zb_form_m(W, d_wofs, c->blk_ls, d_batch, 1, c->xxd, c->st));
+                CUDA_TRY(cudaMemcpyAsync(M, W + wofs[b], sizeof(double) * N * N, cudaMemcpyDeviceToDevice, c->st));
+                CUDA_TRY(zb_psd_block(W + wofs[b], M, N, c->h_blk_ls[b], c->ulen, c->skip, piv, rank, pst, work, c->st));
+                int32_t h_rank = 0, h_pst = 0;
+                CUDA_TRY(cudaMemcpyAsync(&h_rank, rank, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
+                CUDA_TRY(cudaMemcpyAsync(&h_pst, pst, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
+                CUDA_TRY(cudaMemcpyAsync(hpiv.data(), piv, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, c->st));
+                CUDA_TRY(cudaStreamSynchronize(c->st));
+                if (h_pst != 0) return fail(SODAGPU_E_NOTPSD, "subset %d: d*I - X'X is not positive semidefinite", b + 1);
+                for (int j = h_rank; j < N; ++j) {
+                    const int jj = hpiv[j] - 1;
+                    h_iskipped.push_back(h_perm[c->h_blk_ls[b] + jj]);
+                    ++nsk;
+                }
+            } else {
+                naless = 0;
+            }
+            naless = std::min(naless, bs - N + nsk);
+        }
+        if (M) { c->release(M); c->release(work); c->release(piv); c->release(rank); c->release(pst); }
+    }
+    c->nskipped = (int)h_iskipped.size();
+    c->naind = bs - naless;
+    // ragged offsets and packing
+    std::vector<int32_t> h_len(p);
+    CUDA_TRY(cudaMemcpyAsync(h_len.data(), c->ulen, sizeof(int32_t) * p, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    std::vector<int64_t> h_off(p + 1);
+    int64_t tot = 0;
+    for (int k = 0; k < p; ++k) {
+        h_off[k] = tot;
+        tot += h_len[k];
+    }
+    h_off[p] = tot;
+    CUDA_TRY(cudaMemcpyAsync(c->uoff, h_off.data(), sizeof(int64_t) * (p + 1), cudaMemcpyHostToDevice, c->st));
+    TRY(c->alloc(&c->U64, (size_t)tot, false));
+    if (c->cfg.precision == SODAGPU_FP32) TRY(c->alloc(&c->U32, (size_t)tot, false));
+    if (c->cfg.precision == SODAGPU_FP8) {
+        TRY(c->alloc(&c->Uhi, (size_t)tot, false));
+        TRY(c->alloc(&c->Ulo, (size_t)tot, false));
+    }
+    for (int b0 = 0; b0 < nb; b0 += BATCH) {
+        const int nbat = std::min(BATCH, nb - b0);
+        batch_ids.resize(nbat);
+        for (int i = 0; i < nbat; ++i) batch_ids[i] = b0 + i;
+        CUDA_TRY(cudaMemcpyAsync(d_batch, batch_ids.data(), sizeof(int32_t) * nbat, cudaMemcpyHostToDevice, c->st));
+        CUDA_TRY(zb_pack(W, d_wofs, c->blk_ls, d_batch, nbat, c->uoff, c->ulen, c->U64, c->U32, c->Uhi, c->Ulo, c->st));
+        CUDA_TRY(cudaStreamSynchronize(c->st));
+    }
+    c->release(W);
+    c->release(V);
+    c->release(wvec);
+    c->release(alpha);
+    c->release(beta);
+    c->release(d_vofs);
+    c->release(d_batch);
+    c->release(d_status);
+    c->release(d_done);
+    c->release(d_wofs);
+    TRY(c->alloc(&c->iskipped, std::max(1, c->nskipped), false));
+    TRY(c->alloc(&c->xpx, p));
+    if (c->nskipped)
+        CUDA_TRY(cudaMemcpyAsync(c->iskipped, h_iskipped.data(), sizeof(int32_t) * c->nskipped, cudaMemcpyHostToDevice,
+                                 c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->have_z = true;
+    if (nskipped_out) *nskipped_out = c->nskipped;
+    c->t_build = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+__global__ void k_xpx(const int8_t *G, int ldx, const double *xv, const int32_t *pos_of, const int32_t *isk, int nsk,
+                      int n, double *xpx)
+{
+    __shared__ double sh[32];
+    for (int t = blockIdx.x; t < nsk; t += gridDim.x) {
+        const int snp = isk[t], k = pos_of[snp];
+        double s = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double x = xv[(size_t)k * 4 + G[(size_t)k * ldx + i]];
+            s += x * x;
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tsum = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tsum += sh[w];
+            xpx[snp] = tsum;
+        }
+        __syncthreads();
+    }
+}
+
+int build_dev(sodagpu_ctx *c)
+{
+    Dev &D = c->D;
+    memset(&D, 0, sizeof D);
+    D.n = c->n;
+    D.p = c->p;
+    D.bs = c->bs;
+    D.nb = c->nb;
+    D.bt = c->bt;
+    D.method = c->cfg.method;
+    D.nmix = c->cfg.nmix;
+    D.ngroup = c->cfg.ngroup;
+    D.chains = c->C;
+    D.precision = c->cfg.precision;
+    D.ldx = c->ldx;
+    D.ldr = c->ldr;
+    D.nskipped = c->nskipped;
+    D.naind = c->naind;
+    D.nr_ctas = c->nr_ctas;
+    D.recal = c->cfg.recal_every;
+    D.burnin = c->cfg.burnin;
+    D.thin = c->cfg.thin;
+    D.seed = (uint64_t)llabs(c->cfg.seed);
+    D.pizero = c->cfg.pizero;
+    D.scale_ve = c->cfg.scale_ve;
+    D.df_va = c->cfg.df_va;
+    D.df_ve = c->cfg.df_ve;
+    for (int j = 0; j < MAXDIST; ++j) {
+        D.mix[j] = c->cfg.mix[j];
+        D.alpha[j] = c->cfg.alpha[j];
+    }
+    D.G = c->G;
+    D.X32 = c->X32;
+    D.xv = c->xv;
+    D.y = c->y;
+    D.uoff = c->uoff;
+    D.ulen = c->ulen;
+    D.U64 = c->U64;
+    D.U32 = c->U32;
+    D.Uhi = c->Uhi;
+    D.Ulo = c->Ulo;
+    D.xxd = c->xxd;
+    D.xpx = c->xpx;
+    D.perm = c->perm;
+    D.pos_of = c->pos_of;
+    D.skip = c->skip;
+    D.iskipped = c->iskipped;
+    D.grp = c->grp;
+    D.blk_ls = c->blk_ls;
+    D.r = c->r;
+    D.r32 = c->r32;
+    D.ra = c->ra;
+    D.g = c->g;
+    D.cls = c->cls;
+    D.vara_s = c->vara_s;
+    D.gstore = c->gstore;
+    D.vara_sstore = c->vara_sstore;
+    D.indist = c->indist;
+    D.scal = c->scal;
+    D.ctl = c->ctl;
+    D.delta = c->delta;
+    D.nzflag = c->nzflag;
+    D.rpart = c->rpart;
+    D.rsum = c->rsum;
+    D.statpart = c->statpart;
+    D.cntpart = c->cntpart;
+    D.recal_part = c->recal_part;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sodagpu_init_chains(sodagpu_ctx *c)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_z || !c->have_pheno) return fail(SODAGPU_E_STATE, "build Z and load phenotypes first");
+    const int C = c->C, p = c->p, nm = c->cfg.nmix, ngm = c->cfg.ngroup * nm;
+    if (!c->r) {
+        TRY(c->alloc(&c->r, (size_t)C * c->ldr));
+        TRY(c->alloc(&c->r32, (size_t)C * c->ldr));
+        TRY(c->alloc(&c->ra, (size_t)C * c->bs));
+        TRY(c->alloc(&c->g, (size_t)C * p));
+        TRY(c->alloc(&c->cls, (size_t)C * p));
+        TRY(c->alloc(&c->vara_s, (size_t)C * p));
+        TRY(c->alloc(&c->gstore, (size_t)C * p));
+        TRY(c->alloc(&c->vara_sstore, (size_t)C * p));
+        TRY(c->alloc(&c->indist, (size_t)C * p * nm));
+        TRY(c->alloc(&c->scal, C));
+        TRY(c->alloc(&c->delta, (size_t)C * c->bs));
+        TRY(c->alloc(&c->nzflag, c->bs));
+        TRY(c->alloc(&c->rpart, (size_t)C * c->nr_ctas));
+        TRY(c->alloc(&c->rsum, (size_t)C * c->nr_ctas));
+        TRY(c->alloc(&c->statpart, (size_t)C * NSTAT * ngm));
+        TRY(c->alloc(&c->cntpart, (size_t)C * NSTAT * ngm));
+        TRY(c->alloc(&c->recal_part, (size_t)C * RECAL_SPLIT * c->ldr));
+    }
+    build_dev(c);
+    RunCtl h{};
+    CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
+    if (c->nskipped)
+        k_xpx<<<std::min(c->nskipped, 1024), 256, 0, c->st>>>(c->G, c->ldx, c->xv, c->pos_of, c->iskipped,
+                                                               c->nskipped, c->n, c->xpx);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(sweep_enqueue_init(c->D, c->cfg.vara0, c->cfg.scale_va, c->sm_count, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    // capture one iteration of every chain as a CUDA graph
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    cudaGraph_t gr;
+    CUDA_TRY(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = sweep_enqueue_iteration(c->D, c->blk_sizes.data(), c->sm_count, c->st);
+    cudaError_t e2 = cudaStreamEndCapture(c->st, &gr);
+    if (e != cudaSuccess) return fail(SODAGPU_E_CUDA, "capturing the iteration failed: %s", cudaGetErrorString(e));
+    if (e2 != cudaSuccess) return fail(SODAGPU_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
+    e = cudaGraphInstantiate(&c->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return fail(SODAGPU_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    c->have_chain = true;
+    return 0;
+}
+
+int sodagpu_run(sodagpu_ctx *c, int32_t iters, sodagpu_trace_cb cb, void *user)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_chain) return fail(SODAGPU_E_STATE, "call sodagpu_init_chains first");
+    if (iters < 0) return fail(SODAGPU_E_ARG, "iters < 0");
+    if (iters == 0) return 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    RunCtl h{};
+    CUDA_TRY(cudaMemcpyAsync(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    const int rep0 = h.rep;
+    const int thin = c->cfg.thin;
+    const int rows = (cb ? ((rep0 + iters) / thin - rep0 / thin) : 0) * c->C;
+    if (rows > c->trace_cap) {
+        if (c->trace) c->release(c->trace);
+        c->trace = nullptr;
+        TRY(c->alloc(&c->trace, rows, false));
+        c->trace_cap = rows;
+    }
+    h.trace_iter = 0;
+    h.trace_cap = cb ? rows : 0;
+    h.trace_count = 0;
+    h.trace = cb ? c->trace : nullptr;
+    CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
+    for (int t = 0; t < iters; ++t) CUDA_TRY(cudaGraphLaunch(c->graph, c->st));
+    CUDA_TRY(cudaMemcpyAsync(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->t_run = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (h.err) return fail(SODAGPU_E_TIMEOUT, "a bounded device loop gave up (code %d)", h.err);
+    if (cb && rows > 0) {
+        std::vector<sodagpu_trace_row> hr(rows);
+        CUDA_TRY(cudaMemcpy(hr.data(), c->trace, sizeof(sodagpu_trace_row) * rows, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < rows; ++i) cb(user, &hr[i]);
+    }
+    return 0;
+}
+
+int sodagpu_get_results(sodagpu_ctx *c, int32_t chain, double *gstore, double *indiststore, double *vara_sstore,
+                        double *scalars, double *snpstore, double *pstore, double *varstore)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_chain) return fail(SODAGPU_E_STATE, "no chain");
+    if (chain < 0 || chain >= c->C) return fail(SODAGPU_E_ARG, "chain out of range");
+    const int p = c->p, nm = c->cfg.nmix, ng = c->cfg.ngroup, ngm = ng * nm;
+    ChainScal *S = new ChainScal;
+    cudaError_t e = cudaMemcpyAsync(S, c->scal + chain, sizeof(ChainScal), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {
+        delete S;
+        return fail(SODAGPU_E_CUDA, "reading chain scalars: %s", cudaGetErrorString(e));
+    }
+    const double cnt = (double)S->counter;
+    const size_t off = (size_t)chain * p;
+    if (gstore) {
+        CUDA_TRY(cudaMemcpy(gstore, c->gstore + off, sizeof(double) * p, cudaMemcpyDeviceToHost));
+        for (int j = 0; j < p; ++j) gstore[j] = gstore[j] / cnt;
+    }
+    if (vara_sstore) {
+        CUDA_TRY(cudaMemcpy(vara_sstore, c->vara_sstore + off, sizeof(double) * p, cudaMemcpyDeviceToHost));
+        for (int j = 0; j < p; ++j) vara_sstore[j] = vara_sstore[j] / cnt;
+    }
+    if (indiststore) {
+        std::vector<uint32_t> h((size_t)p * nm);
+        CUDA_TRY(cudaMemcpy(h.data(), c->indist + off * nm, sizeof(uint32_t) * p * nm, cudaMemcpyDeviceToHost));
+        for (int j = 0; j < p; ++j)
+            for (int q = 0; q < nm; ++q) indiststore[(size_t)j + (size_t)q * p] = (double)h[(size_t)j * nm + q] / cnt;
+    }
+    if (scalars) {
+        scalars[0] = S->mu_store / cnt;
+        scalars[1] = S->vare_store / cnt;
+        scalars[2] = S->vara_store / cnt;
+        scalars[3] = S->included_store / cnt;
+    }
+    for (int t = 0; t < ngm; ++t) {
+        if (snpstore) snpstore[t] = S->snpstore[t] / cnt;
+        if (pstore) pstore[t] = S->pstore[t] / cnt;
+        if (varstore) varstore[t] = S->varstore[t] / cnt;
+    }
+    delete S;
+    return 0;
+}
+
+int sodagpu_get_state(sodagpu_ctx *c, int32_t chain, double *g, int32_t *cls, double *vara_s, double *yadj,
+                      double *yaadj, double *scalars)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_chain) return fail(SODAGPU_E_STATE, "no chain");
+    if (chain < 0 || chain >= c->C) return fail(SODAGPU_E_ARG, "chain out of range");
+    const int p = c->p;
+    const size_t off = (size_t)chain * p;
+    if (g) CUDA_TRY(cudaMemcpy(g, c->g + off, sizeof(double) * p, cudaMemcpyDeviceToHost));
+    if (cls) CUDA_TRY(cudaMemcpy(cls, c->cls + off, sizeof(int32_t) * p, cudaMemcpyDeviceToHost));
+    if (vara_s) CUDA_TRY(cudaMemcpy(vara_s, c->vara_s + off, sizeof(double) * p, cudaMemcpyDeviceToHost));
+    if (yadj) CUDA_TRY(cudaMemcpy(yadj, c->r + (size_t)chain * c->ldr, sizeof(double) * c->n, cudaMemcpyDeviceToHost));
+    if (yaadj) CUDA_TRY(cudaMemcpy(yaadj, c->ra + (size_t)chain * c->bs, sizeof(double) * c->bs, cudaMemcpyDeviceToHost));
+    if (scalars) {
+        ChainScal *S = new ChainScal;
+        RunCtl h{};
+        cudaError_t e = cudaMemcpy(S, c->scal + chain, sizeof(ChainScal), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            delete S;
+            return fail(SODAGPU_E_CUDA, "reading chain scalars: %s", cudaGetErrorString(e));
+        }
+        scalars[0] = S->mu[h.rep & 1];
+        scalars[1] = S->vare;
+        scalars[2] = S->vara;
+        scalars[3] = S->included;
+        delete S;
+    }
+    return 0;
+}
+
+int sodagpu_get_z(sodagpu_ctx *c, double *xa, double *xxd, int32_t *skip)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_z) return fail(SODAGPU_E_STATE, "no Z built");
+    if (xa) {
+        double *dxa = nullptr;
+        TRY(c->alloc(&dxa, (size_t)c->bs * c->p, false));
+        CUDA_TRY(zb_unpack_dense(c->U64, c->uoff, c->ulen, c->p, c->bs, dxa, c->st));
+        CUDA_TRY(cudaMemcpyAsync(xa, dxa, sizeof(double) * c->bs * c->p, cudaMemcpyDeviceToHost, c->st));
+        CUDA_TRY(cudaStreamSynchronize(c->st));
+        c->release(dxa);
+    }
+    if (xxd) CUDA_TRY(cudaMemcpy(xxd, c->xxd, sizeof(double) * c->nb, cudaMemcpyDeviceToHost));
+    if (skip) {
+        std::vector<uint8_t> h(c->p);
+        CUDA_TRY(cudaMemcpy(h.data(), c->skip, c->p, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < c->p; ++k) skip[k] = h[k];
+    }
+    return 0;
+}
+
+int sodagpu_compute_dgv(sodagpu_ctx *c, double mu, const double *effects, double *pred)
+{
+    if (!c || !effects || !pred) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_z) return fail(SODAGPU_E_STATE, "no genotypes in subset order (run sodagpu_build_z)");
+    const int nsplit = 32;
+    double *deff = nullptr, *part = nullptr, *dpred = nullptr;
+    TRY(c->alloc(&deff, c->p, false));
+    TRY(c->alloc(&part, (size_t)nsplit * c->ldx, false));
+    TRY(c->alloc(&dpred, c->n, false));
+    CUDA_TRY(cudaMemcpyAsync(deff, effects, sizeof(double) * c->p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(zb_dgv(c->G, c->ldx, c->xv, c->perm, deff, c->n, c->p, mu, part, nsplit, dpred, c->st));
+    CUDA_TRY(cudaMemcpyAsync(pred, dpred, sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->release(deff);
+    c->release(part);
+    c->release(dpred);
+    return 0;
+}
+
+int sodagpu_predict(int32_t nind, int32_t nloci, const void *geno, int32_t layout, const double *freq, double mu,
+                    const double *effects, double *pred)
+{
+    if (nind < 1 || nloci < 1 || !geno || !freq || !effects || !pred) return fail(SODAGPU_E_ARG, "bad argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SODAGPU_E_NODEVICE, "no CUDA device visible");
+    }
+    cudaStream_t st;
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const int n = nind, p = nloci;
+    const int ldx = (int)round_up((size_t)n, 128);
+    int8_t *G = nullptr;
+    double *dfreq = nullptr, *xv = nullptr, *deff = nullptr, *part = nullptr, *dpred = nullptr;
+    int32_t *perm = nullptr;
+    uint8_t *tmp = nullptr;
+    const int nsplit = 32;
+    std::vector<int32_t> ident(p);
+    for (int k = 0; k < p; ++k) ident[k] = k;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    chk(cudaMalloc(&G, (size_t)p * ldx));
+    chk(cudaMalloc(&dfreq, sizeof(double) * p));
+    chk(cudaMalloc(&xv, sizeof(double) * 4 * p));
+    chk(cudaMalloc(&deff, sizeof(double) * p));
+    chk(cudaMalloc(&part, sizeof(double) * nsplit * ldx));
+    chk(cudaMalloc(&dpred, sizeof(double) * n));
+    chk(cudaMalloc(&perm, sizeof(int32_t) * p));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(G, 0, (size_t)p * ldx, st));
+    const bool on_dev = (layout & SODAGPU_GENO_DEVICE_PTR) != 0;
+    const cudaMemcpyKind mk = on_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (e == cudaSuccess) {
+        if ((layout & 0xff) == SODAGPU_GENO_CODES) {
+            chk(cudaMemcpy2DAsync(G, ldx, geno, n, n, p, mk, st));
+        } else {
+            const size_t rec = ((size_t)n + 3) / 4;
+            chk(cudaMalloc(&tmp, rec * p));
+            if (e == cudaSuccess) chk(cudaMemcpyAsync(tmp, geno, rec * p, mk, st));
+            if (e == cudaSuccess) chk(zb_decode_bed(tmp, n, p, G, ldx, st));
+        }
+    }
+    if (e == cudaSuccess) chk(cudaMemcpyAsync(dfreq, freq, sizeof(double) * p, cudaMemcpyHostToDevice, st));
+    if (e == cudaSuccess) chk(cudaMemcpyAsync(deff, effects, sizeof(double) * p, cudaMemcpyHostToDevice, st));
+    if (e == cudaSuccess) chk(cudaMemcpyAsync(perm, ident.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, st));
+    if (e == cudaSuccess) chk(zb_xv(dfreq, perm, p, xv, st));
+    if (e == cudaSuccess) chk(zb_dgv(G, ldx, xv, nullptr, deff, n, p, mu, part, nsplit, dpred, st));
+    if (e == cudaSuccess) chk(cudaMemcpyAsync(pred, dpred, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    if (e == cudaSuccess) chk(cudaStreamSynchronize(st));
+    cudaFree(G); cudaFree(dfreq); cudaFree(xv); cudaFree(deff); cudaFree(part); cudaFree(dpred); cudaFree(perm);
+    cudaFree(tmp);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return fail(SODAGPU_E_CUDA, "prediction failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+int sodagpu_timings(sodagpu_ctx *c, double *build_z_s, double *run_s)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (build_z_s) *build_z_s = c->t_build;
+    if (run_s) *run_s = c->t_run;
+    return 0;
+}
+
+void sodagpu_destroy(sodagpu_ctx *c)
+{
+    if (!c) return;
+    if (c->st) cudaStreamSynchronize(c->st);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (void *p_ : c->allocs) cudaFree(p_);
+    c->allocs.clear();
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+}  // extern "C"

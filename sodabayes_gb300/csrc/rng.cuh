@@ -1,0 +1,147 @@
+// rng.cuh — counter-based draws for the SODA sampler (device side).
+//
+// The reference gives every OpenMP thread its own xoroshiro128+ stream
+// (parallelrng.f90:54-149), so a SNP's draws depend on which thread ran it.
+// On the GPU each draw is instead keyed by (seed, chain, iteration, slot,
+// purpose): Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11) turns that
+// counter into 64-bit words, which are mapped to [0,1) exactly like
+// rng_int64_to_real64 (parallelrng.f90:242-249).  The distributions below
+// restate the reference's transforms:
+//   normal         Box-Muller, sine branch, REAL-precision pi (parallelrng.f90:264-277)
+//   gamma          Marsaglia & Tsang 2000, boost for shape<1  (parallelrng.f90:294-333)
+//   inv. chi^2     1/gamma(dof/2, 2/(dof*scale))               (parallelrng.f90:348-362)
+//   Dirichlet      normalised gammas                            (parallelrng.f90:445-455)
+#pragma once
+#include <stdint.h>
+
+namespace soda {
+
+// Purposes (third counter word); the CPU oracle uses the same numbering.
+enum Purpose : uint32_t {
+    P_SNP = 1, P_MU = 2, P_VARA = 3, P_VARE = 4, P_PI = 5, P_RA = 6,
+    P_SKIP = 7, P_PERM = 8, P_POWER = 9
+};
+
+// parallelrng.f90:20 declares pi as a default REAL literal: float(pi) widened.
+#define SODA_REF_PI 3.1415927410125732
+
+struct CRng {
+    uint32_t k0, k1, c0, c1, c2, c3;
+    uint32_t o2, o3;
+    int have;
+};
+
+__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t &c0, uint32_t &c1, uint32_t &c2,
+                                                       uint32_t &c3, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = mulhi32(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = mulhi32(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+}
+
+__host__ __device__ __forceinline__ void crng_init(CRng &s, uint64_t seed, int chain, int iter,
+                                                   int slot, int purpose)
+{
+    s.k0 = (uint32_t)seed;
+    s.k1 = (uint32_t)(seed >> 32);
+    s.c0 = (uint32_t)iter;
+    s.c1 = (uint32_t)slot;
+    s.c2 = (uint32_t)purpose;
+    s.c3 = (uint32_t)chain << 20;
+    s.have = 0;
+}
+
+__host__ __device__ __forceinline__ uint64_t crng_u64(CRng &s)
+{
+    if (s.have == 0) {
+        uint32_t a = s.c0, b = s.c1, c = s.c2, d = s.c3;
+        philox4x32_10(a, b, c, d, s.k0, s.k1);
+        s.c3++;
+        s.o2 = c;
+        s.o3 = d;
+        s.have = 1;
+        return ((uint64_t)b << 32) | a;
+    }
+    s.have = 0;
+    return ((uint64_t)s.o3 << 32) | s.o2;
+}
+
+__host__ __device__ __forceinline__ double crng_unit(CRng &s)
+{
+    const uint64_t bits = 0x3FF0000000000000ULL | (crng_u64(s) >> 12);
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)bits) - 1.0;
+#else
+    double d;
+    __builtin_memcpy(&d, &bits, sizeof d);
+    return d - 1.0;
+#endif
+}
+
+// rand_normal (parallelrng.f90:264-277)
+__device__ __forceinline__ double d_rnorm(double mean, double sd, CRng &s)
+{
+    if (sd <= 0.0) return mean;
+    const double u1 = crng_unit(s), u2 = crng_unit(s);
+    const double rr = sqrt(-2.0 * log(u1));
+    const double th = 2.0 * SODA_REF_PI * u2;
+    return mean + sd * rr * sin(th);
+}
+
+// rand_gamma (parallelrng.f90:294-333).  The rejection loop is bounded; on
+// the (practically impossible) exhaustion *err is set and the last candidate
+// returned.
+__device__ __forceinline__ double d_rgamma(double shape, double scale, CRng &s, int *err)
+{
+    const bool small = shape < 1.0;
+    const double sh = small ? shape + 1.0 : shape;
+    const double sc = small ? 1.0 : scale;
+    const double d = sh - 1.0 / 3.0;
+    const double c = 1.0 / sqrt(9.0 * d);
+    double res = d;
+    int tries = 0;
+    for (;;) {
+        double x = d_rnorm(0.0, 1.0, s);
+        double v = 1.0 + c * x;
+        while (v <= 0.0 && tries < 100000) {
+            x = d_rnorm(0.0, 1.0, s);
+            v = 1.0 + c * x;
+            ++tries;
+        }
+        v = v * v * v;
+        const double u = crng_unit(s);
+        const double xsq = x * x;
+        res = sc * d * v;
+        if ((u < 1.0 - 0.0331 * xsq * xsq) || (log(u) < 0.5 * xsq + d * (1.0 - v + log(v)))) break;
+        if (++tries >= 100000) { if (err) *err = 1; break; }
+    }
+    if (small) {
+        // shape < 1: g ~ gamma(shape+1, 1), then scale*g*w**(1/shape)
+        const double w = crng_unit(s);
+        return scale * res * pow(w, 1.0 / shape);
+    }
+    return res;
+}
+
+// rand_scaled_inverse_chi_square (parallelrng.f90:348-362)
+__device__ __forceinline__ double d_rscinvchi2(double dof, double scale, CRng &s, int *err)
+{
+    const double shape = 0.5 * dof, sc = 0.5 * dof * scale;
+    return 1.0 / d_rgamma(shape, 1.0 / sc, s, err);
+}
+
+}  // namespace soda

@@ -1,0 +1,107 @@
+// state.cuh — device-side layout of one SODA job.
+//
+// HBM layout (all arrays 256-byte aligned):
+//   G      int8   [nloci][ldx]   genotype codes 0/1/2, one column per subset
+//                                position k (SNP perm[k]), padded to ldx
+//   X32    float  [nloci][ldx]   centred/scaled columns (FP32 mode only)
+//   xv     double [nloci][4]     the three values (code - 2p)/sqrt(2p(1-p))
+//                                of each column and 1/sqrt(2p(1-p)); all 0
+//                                for monomorphic SNPs
+//   U*     packed ragged columns of the augmenting matrix: column k holds
+//          rows 0..ulen[k]-1 at uoff[k]; FP64 / FP32 / BF16 hi+lo by mode
+//   r      double [C][ldr]       residual yadj (master copy, FP64)
+//   r32    float  [C][ldr]       FP32 copy read by the FP32/FP8 dot products
+//   ra     double [C][bs]        augmented residual yAadj
+//   g, vara_s double [C][nloci], cls int32 [C][nloci] (by SNP id)
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include "../../include/sodagpu.h"
+
+namespace soda {
+
+constexpr int MAXDIST = SODAGPU_MAXDIST;
+constexpr int MAXGRP = SODAGPU_MAXGRP;
+constexpr int MAXGM = MAXDIST * MAXGRP;
+
+// Per-chain scalars and small tables (device memory, one per chain).
+struct ChainScal {
+    double mu[2];              // mu of the previous / current iteration (by rep parity)
+    double vara, vare, scale_va;
+    double gp[MAXDIST], vare_gp[MAXDIST];
+    double mu_store, vare_store, vara_store, included_store;
+    int32_t included, counter, keep, err;
+    double p[MAXGM];           // (ngroup, nmix) column-major
+    double log_p[MAXGM];
+    double varindist[MAXGM];
+    double snpstore[MAXGM], pstore[MAXGM], varstore[MAXGM];
+    int32_t snpindist[MAXGM];
+};
+
+// Control block written by the host before a run and by the kernels.
+struct RunCtl {
+    int32_t rep;               // iteration counter (1-based once running)
+    int32_t trace_iter;        // thinned iterations seen in this run
+    int32_t trace_cap;         // rows available in trace
+    int32_t trace_count;       // rows written
+    int32_t err;               // sticky device error flag
+    sodagpu_trace_row *trace;  // device trace buffer
+};
+
+// Everything the kernels read, passed by value.
+struct Dev {
+    // sizes
+    int n, p, bs, nb, bt, method, nmix, ngroup, chains, precision;
+    int ldx;                   // column stride of G / X32 (elements)
+    int ldr;                   // chain stride of r / r32
+    int nskipped, naind;
+    int nr_ctas;               // row CTAs of the residual kernels
+    int recal;
+    int burnin, thin;
+    uint64_t seed;
+    double pizero, scale_ve, df_va, df_ve;
+    double mix[MAXDIST], alpha[MAXDIST];
+    // data (shared by chains)
+    const int8_t *G;
+    const float *X32;
+    const double *xv;          // [p][4]: x for codes 0,1,2 and 1/sd (0 if monomorphic)
+    const double *y;
+    const int64_t *uoff;
+    const int32_t *ulen;
+    const double *U64;
+    const float *U32;
+    const __nv_bfloat16 *Uhi, *Ulo;
+    const double *xxd;         // d per subset
+    const double *xpx;         // x'x by SNP (skipped SNPs)
+    const int32_t *perm;       // position -> SNP (0-based)
+    const int32_t *pos_of;     // SNP -> position
+    const uint8_t *skip;       // by position
+    const int32_t *iskipped;   // skipped SNP ids
+    const int32_t *grp;        // by SNP, 1-based
+    const int32_t *blk_ls;     // [nb+1] first position of each subset
+    // chain state
+    double *r;
+    float *r32;
+    double *ra;
+    double *g;
+    int32_t *cls;
+    double *vara_s;
+    double *gstore, *vara_sstore;
+    uint32_t *indist;          // [C][p][nmix] kept-sample class counts
+    ChainScal *scal;
+    RunCtl *ctl;
+    // scratch
+    double *delta;             // [C][bs]
+    uint8_t *nzflag;           // [bs]
+    double *rpart;             // [C][nr_ctas] row-CTA partial sums (mu, rsum, r^2)
+    double *rsum;              // [C][nr_ctas] partial sums of r for the FP8 centring
+    double *statpart;          // [C][NSTAT][ngroup*nmix] sum g^2
+    int32_t *cntpart;          // [C][NSTAT][ngroup*nmix] counts
+    double *recal_part;        // [C][RECAL_SPLIT][ldr]
+};
+
+constexpr int NSTAT = 64;          // CTAs of the per-iteration SNP statistics
+constexpr int ROW_THREADS = 256;   // rows per row-CTA
+constexpr int RECAL_SPLIT = 32;    // column splits of the residual recalibration
+
+}  // namespace soda

@@ -1,0 +1,966 @@
+// sweep.cu — per-iteration kernels of the SODA Gibbs sampler.
+//
+// One iteration (models.f90:129-574) is, per chain:
+//   mu draw                              k_mu_partial + k_mu_apply   (models.f90:130-132)
+//   for each subset b (sequential):
+//     rhs_j = x_j'r + u_j'ra (+d g_j) and the per-SNP draw
+//                                        k_rhs_draw                  (models.f90:146-162, 211-256, 350-413)
+//     r += X_b delta, ra += U_b delta    k_update                    (models.f90:164-174, 258-272, 415-430)
+//   single-site updates of skipped SNPs  k_skipped                   (models.f90:178-193, 276-320, 433-495)
+//   class counts, sum g^2, sum r^2       k_stats
+//   sigma2_g, sigma2_e, pi draws, trace  k_hyper                     (models.f90:194, 321-325, 496-522, 549-569)
+//   ra redraw, posterior accumulators    k_post                      (models.f90:523-548)
+//   residual recalibration               k_recal_partial/_apply      (models.f90:571-573)
+// All chains of the context advance together inside each launch.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "rng.cuh"
+#include "state.cuh"
+#include "sweep.cuh"
+
+namespace soda {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sumf(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Deterministic block sum; every thread gets the total.  blockDim.x % 32 == 0.
+__device__ double block_sum(double v, double *sh /* >= 33 doubles */)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double t = lane < nw ? sh[lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) sh[32] = t;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+__device__ __forceinline__ int cur_rep(const Dev &D) { return *((volatile int32_t *)&D.ctl->rep); }
+
+__device__ __forceinline__ void flag_err(const Dev &D, int code)
+{
+    atomicExch(&D.ctl->err, code);
+}
+
+// ---------------------------------------------------------------------------
+// Per-SNP conditional draw inside a subset.  Returns delta = g_old - g_new.
+// Restates models.f90:146-161 (BayesA), 211-255 (BayesB), 350-412 (C/Cpi/R/Rc).
+// ---------------------------------------------------------------------------
+__device__ double draw_snp(const Dev &D, const ChainScal *S, int c, int rep, int snploc,
+                           double rhs, double zz, double zz_vare, CRng &R, int *err)
+{
+    const size_t o = (size_t)c * D.p + snploc;
+    const double vare = S->vare;
+    double gk = D.g[o];
+    const double gold = gk;
+    const int m = D.method;
+    if (m == SODAGPU_BAYES_A) {
+        rhs = rhs + zz * gk;
+        const double vs = D.vara_s[o];
+        const double v1 = zz + vare / vs;
+        gk = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+        D.g[o] = gk;
+        const double scale = (gk * gk + S->scale_va * D.df_va) / (D.df_va + 1.0);
+        D.vara_s[o] = d_rscinvchi2(D.df_va + 1.0, scale, R, err);
+        return gold - gk;
+    }
+    const int cl = D.cls[o];
+    if (cl > 1) rhs = rhs + zz * gk;
+    const int ng = D.ngroup;
+    if (m == SODAGPU_BAYES_B) {
+        const double vs = D.vara_s[o];
+        const double s1 = S->log_p[0];
+        const double logdetV = log(vs * zz_vare + 1.0);
+        const double uhat = rhs / (zz + vare / vs);
+        const double s2 = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[ng];
+        const double clike = s1 - s2;
+        double sk;
+        if (clike > 700) sk = 0.0;
+        else if (clike < -700) sk = 1.0;
+        else sk = 1.0 / (1.0 + exp(clike));
+        const double u = crng_unit(R);
+        const int flag = u < sk ? 2 : 1;
+        double gnew;
+        if (flag == 1) {
+            gk = d_rnorm(0.0, sqrt(vs), R);
+            gnew = 0.0;
+        } else {
+            const double v1 = zz + vare / vs;
+            gk = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+            gnew = gk;
+        }
+        D.g[o] = gnew;
+        D.cls[o] = flag;
+        const double scale = (gk * gk + S->scale_va * D.df_va) / (D.df_va + 1.0);
+        D.vara_s[o] = d_rscinvchi2(D.df_va + 1.0, scale, R, err);
+        return gold - gnew;
+    }
+    // BayesC / Cpi / R / Rc
+    const int nm = D.nmix;
+    const int sg = D.grp[snploc] - 1;
+    double s[MAXDIST];
+    s[0] = S->log_p[sg];
+    for (int kk = 1; kk < nm; ++kk) {
+        const double logdetV = log(S->gp[kk] * zz_vare + 1.0);
+        const double uhat = rhs / (zz + S->vare_gp[kk]);
+        s[kk] = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[sg + kk * ng];
+    }
+    const double u = crng_unit(R);
+    double ssculm = 0.0;
+    int flag = 1;
+    for (int kk = 0; kk < nm; ++kk) {
+        const double skk = s[kk];
+        double sk = 0.0;
+        bool overflow = false;
+        for (int j = 0; j < nm; ++j) {
+            if (j == kk) continue;
+            const double clike = s[j] - skk;
+            if (clike < -700) continue;
+            if (clike > 700) { overflow = true; break; }
+            sk = sk + exp(clike);
+        }
+        const double st = overflow ? 0.0 : 1.0 / (1.0 + sk);
+        ssculm = ssculm + st;
+        if (u < ssculm) { flag = kk + 1; break; }
+    }
+    double gnew = 0.0;
+    if (flag != 1) {
+        const double v1 = zz + vare / S->gp[flag - 1];
+        gnew = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+    }
+    D.cls[o] = flag;
+    D.g[o] = gnew;
+    return gold - gnew;
+}
+
+// ---------------------------------------------------------------------------
+// iteration start and the mu draw
+// ---------------------------------------------------------------------------
+__global__ void k_iter_begin(Dev D)
+{
+    RunCtl *ctl = D.ctl;
+    const int rep = ctl->rep + 1;
+    ctl->rep = rep;
+    if (rep % D.thin == 0) ctl->trace_iter += 1;
+}
+
+__global__ void __launch_bounds__(ROW_THREADS) k_mu_partial(Dev D)
+{
+    __shared__ double sh[33];
+    const int c = blockIdx.y, rep = cur_rep(D);
+    const double mu_old = D.scal[c].mu[(rep - 1) & 1];
+    const int i = blockIdx.x * ROW_THREADS + threadIdx.x;
+    const double v = i < D.n ? D.r[(size_t)c * D.ldr + i] + mu_old : 0.0;
+    const double t = block_sum(v, sh);
+    if (threadIdx.x == 0) D.rpart[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
+{
+    __shared__ double sh[33];
+    __shared__ double s_mu;
+    const int c = blockIdx.y, rep = cur_rep(D);
+    ChainScal *S = &D.scal[c];
+    const double mu_old = S->mu[(rep - 1) & 1];
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int t = 0; t < D.nr_ctas; ++t) tot += D.rpart[(size_t)c * D.nr_ctas + t];
+        CRng R;
+        crng_init(R, D.seed, c, rep, 0, P_MU);
+        const double nn = (double)D.n;
+        const double mu = d_rnorm(tot / nn, sqrt(S->vare / nn), R);
+        s_mu = mu;
+        if (blockIdx.x == 0) S->mu[rep & 1] = mu;
+    }
+    __syncthreads();
+    const double mu = s_mu;
+    const int i = blockIdx.x * ROW_THREADS + threadIdx.x;
+    double v = 0.0;
+    if (i < D.n) {
+        const size_t o = (size_t)c * D.ldr + i;
+        v = (D.r[o] + mu_old) - mu;
+        D.r[o] = v;
+        D.r32[o] = (float)v;
+    }
+    if (D.precision == SODAGPU_FP8) {
+        const double t = block_sum(v, sh);
+        if (threadIdx.x == 0) D.rsum[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// rhs and draw: one warp per subset position, all chains.
+// ---------------------------------------------------------------------------
+template <int MODE, int CT>
+__global__ void __launch_bounds__(256) k_rhs_draw(Dev D, int b, int wpc)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ls = D.blk_ls[b];
+    const int N = D.blk_ls[b + 1] - ls;
+    const int jk = blockIdx.x * wpc + warp;
+    if (warp >= wpc || jk >= N) return;
+    const int k = ls + jk;
+    const int rep = cur_rep(D);
+    if (D.skip[k]) {
+        if (lane < CT) D.delta[(size_t)lane * D.bs + jk] = 0.0;
+        if (lane == 0) D.nzflag[jk] = 0;
+        return;
+    }
+    typedef typename std::conditional<MODE == SODAGPU_FP64, double, float>::type acc_t;
+    acc_t acc[CT];
+#pragma unroll
+    for (int c = 0; c < CT; ++c) acc[c] = 0;
+
+    if (MODE == SODAGPU_FP64) {
+        const int8_t *col = D.G + (size_t)k * D.ldx;
+        const double x0 = D.xv[(size_t)k * 4 + 0], x1 = D.xv[(size_t)k * 4 + 1],
+                     x2 = D.xv[(size_t)k * 4 + 2];
+        for (int i = lane; i < D.n; i += 32) {
+            const int code = col[i];
+            const double x = code == 0 ? x0 : (code == 1 ? x1 : x2);
+#pragma unroll
+            for (int c = 0; c < CT; ++c) acc[c] += (acc_t)(x * D.r[(size_t)c * D.ldr + i]);
+        }
+    } else if (MODE == SODAGPU_FP32) {
+        const float4 *col = reinterpret_cast<const float4 *>(D.X32 + (size_t)k * D.ldx);
+        const int n4 = D.ldx >> 2;
+#pragma unroll 4
+        for (int i4 = lane; i4 < n4; i4 += 32) {
+            const float4 xx = __ldg(col + i4);
+#pragma unroll
+            for (int c = 0; c < CT; ++c) {
+                const float4 rr = __ldg(reinterpret_cast<const float4 *>(D.r32 + (size_t)c * D.ldr) + i4);
+                acc[c] = fmaf(xx.x, rr.x, acc[c]);
+                acc[c] = fmaf(xx.y, rr.y, acc[c]);
+                acc[c] = fmaf(xx.z, rr.z, acc[c]);
+                acc[c] = fmaf(xx.w, rr.w, acc[c]);
+            }
+        }
+    } else {  // FP8: exact codes, rank-1 centring after the dot product
+        const uint4 *col = reinterpret_cast<const uint4 *>(D.G + (size_t)k * D.ldx);
+        const int n16 = D.ldx >> 4;
+#pragma unroll 2
+        for (int i16 = lane; i16 < n16; i16 += 32) {
+            const uint4 w = __ldg(col + i16);
+            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float g0 = (float)(ww[q] & 0xff), g1 = (float)((ww[q] >> 8) & 0xff),
+                            g2 = (float)((ww[q] >> 16) & 0xff), g3 = (float)(ww[q] >> 24);
+#pragma unroll
+                for (int c = 0; c < CT; ++c) {
+                    const float4 rr = __ldg(reinterpret_cast<const float4 *>(D.r32 + (size_t)c * D.ldr) +
+                                            i16 * 4 + q);
+                    acc[c] = fmaf(g0, rr.x, acc[c]);
+                    acc[c] = fmaf(g1, rr.y, acc[c]);
+                    acc[c] = fmaf(g2, rr.z, acc[c]);
+                    acc[c] = fmaf(g3, rr.w, acc[c]);
+                }
+            }
+        }
+    }
+    // u_k' ra over the stored rows of column k
+    acc_t accu[CT];
+#pragma unroll
+    for (int c = 0; c < CT; ++c) accu[c] = 0;
+    {
+        const int64_t off = D.uoff[k];
+        const int len = D.ulen[k];
+        for (int i = lane; i < len; i += 32) {
+            acc_t u;
+            if (MODE == SODAGPU_FP64) u = (acc_t)D.U64[off + i];
+            else if (MODE == SODAGPU_FP32) u = (acc_t)D.U32[off + i];
+            else u = (acc_t)(__bfloat162float(D.Uhi[off + i]) + __bfloat162float(D.Ulo[off + i]));
+#pragma unroll
+            for (int c = 0; c < CT; ++c) accu[c] += u * (acc_t)D.ra[(size_t)c * D.bs + i];
+        }
+    }
+    double xr_mine = 0.0, ur_mine = 0.0;
+#pragma unroll
+    for (int c = 0; c < CT; ++c) {
+        double a, u;
+        if (MODE == SODAGPU_FP64) {
+            a = warp_sum((double)acc[c]);
+            u = warp_sum((double)accu[c]);
+        } else {
+            a = (double)warp_sumf((float)acc[c]);
+            u = (double)warp_sumf((float)accu[c]);
+        }
+        if (lane == c) { xr_mine = a; ur_mine = u; }
+    }
+    double delta = 0.0;
+    if (lane < CT) {
+        const int c = lane;
+        double xr = xr_mine;
+        if (MODE == SODAGPU_FP8) {
+            // x_k'r = (G_k'r - 2p sum(r)) / sd = G_k'r * (1/sd) + x0 * sum(r)
+            double rs = 0.0;
+            for (int t = 0; t < D.nr_ctas; ++t) rs += D.rsum[(size_t)c * D.nr_ctas + t];
+            xr = xr * D.xv[(size_t)k * 4 + 3] + D.xv[(size_t)k * 4 + 0] * rs;
+        }
+        const ChainScal *S = &D.scal[c];
+        const double zz = D.xxd[b];
+        const double zz_vare = zz / S->vare;
+        CRng R;
+        crng_init(R, D.seed, c, rep, D.perm[k], P_SNP);
+        int err = 0;
+        delta = draw_snp(D, S, c, rep, D.perm[k], xr + ur_mine, zz, zz_vare, R, &err);
+        if (err) flag_err(D, 1);
+        D.delta[(size_t)c * D.bs + jk] = delta;
+    }
+    const unsigned nz = __ballot_sync(0xffffffffu, lane < CT && delta != 0.0);
+    if (lane == 0) D.nzflag[jk] = nz != 0u;
+}
+
+// ---------------------------------------------------------------------------
+// residual update r += X_b delta (rows) and ra += U_b delta (augmented rows),
+// columns in subset order for every element (models.f90:164-174).
+// ---------------------------------------------------------------------------
+constexpr int UPD_CHUNK = 32;
+
+static inline size_t update_smem_bytes(int bs) { return sizeof(int) * ((size_t)bs + 32); }
+
+template <int MODE, int CT>
+__global__ void __launch_bounds__(ROW_THREADS) k_update(Dev D, int b)
+{
+    extern __shared__ int s_list[];  // bs + 32 ints
+    __shared__ int s_wcnt[ROW_THREADS / 32 + 1];
+    __shared__ int s_n;
+    __shared__ double s_xv[UPD_CHUNK][3];
+    __shared__ double s_dl[UPD_CHUNK][CT];
+    __shared__ int64_t s_off[UPD_CHUNK];
+    __shared__ int s_len[UPD_CHUNK];
+    __shared__ double sh[33];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int ls = D.blk_ls[b];
+    const int N = D.blk_ls[b + 1] - ls;
+    // compact the positions with a non-zero delta in any chain, in order
+    if (tid == 0) s_n = 0;
+    __syncthreads();
+    for (int base = 0; base < N; base += ROW_THREADS) {
+        const int jk = base + tid;
+        const bool f = jk < N && D.nzflag[jk];
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_wcnt[w] = __popc(m);
+        __syncthreads();
+        if (tid == 0) {
+            int acc = s_n;
+            for (int q = 0; q < ROW_THREADS / 32; ++q) {
+                const int t = s_wcnt[q];
+                s_wcnt[q] = acc;
+                acc += t;
+            }
+            s_wcnt[ROW_THREADS / 32] = acc;
+        }
+        __syncthreads();
+        if (f) s_list[s_wcnt[w] + __popc(m & ((1u << lane) - 1u))] = jk;
+        __syncthreads();
+        if (tid == 0) s_n = s_wcnt[ROW_THREADS / 32];
+        __syncthreads();
+    }
+    const int nlist = s_n;
+    if (nlist == 0) return;
+    const bool rows = blockIdx.x < D.nr_ctas;
+    const int i = (rows ? blockIdx.x : blockIdx.x - D.nr_ctas) * ROW_THREADS + tid;
+    const bool active = rows ? i < D.n : i < D.bs;
+    double acc[CT];
+#pragma unroll
+    for (int c = 0; c < CT; ++c)
+        acc[c] = active ? (rows ? D.r[(size_t)c * D.ldr + i] : D.ra[(size_t)c * D.bs + i]) : 0.0;
+    for (int base = 0; base < nlist; base += UPD_CHUNK) {
+        const int cnt = min(UPD_CHUNK, nlist - base);
+        __syncthreads();
+        for (int t = tid; t < cnt * CT; t += ROW_THREADS) {
+            const int q = t / CT, c = t % CT;
+            s_dl[q][c] = D.delta[(size_t)c * D.bs + s_list[base + q]];
+        }
+        if (tid < cnt) {
+            const int k = ls + s_list[base + tid];
+            s_xv[tid][0] = D.xv[(size_t)k * 4 + 0];
+            s_xv[tid][1] = D.xv[(size_t)k * 4 + 1];
+            s_xv[tid][2] = D.xv[(size_t)k * 4 + 2];
+            s_off[tid] = D.uoff[k];
+            s_len[tid] = D.ulen[k];
+        }
+        __syncthreads();
+        if (!active) continue;
+        for (int q = 0; q < cnt; ++q) {
+            const int k = ls + s_list[base + q];
+            double x;
+            if (rows) {
+                if (MODE == SODAGPU_FP32) {
+                    x = (double)D.X32[(size_t)k * D.ldx + i];
+                } else {
+                    const int code = D.G[(size_t)k * D.ldx + i];
+                    x = s_xv[q][code];
+                }
+            } else {
+                if (i >= s_len[q]) continue;
+                const int64_t o = s_off[q] + i;
+                if (MODE == SODAGPU_FP64) x = D.U64[o];
+                else if (MODE == SODAGPU_FP32) x = (double)D.U32[o];
+                else x = (double)__bfloat162float(D.Uhi[o]) + (double)__bfloat162float(D.Ulo[o]);
+            }
+#pragma unroll
+            for (int c = 0; c < CT; ++c) acc[c] = acc[c] + x * s_dl[q][c];
+        }
+    }
+    if (active) {
+#pragma unroll
+        for (int c = 0; c < CT; ++c) {
+            if (rows) {
+                D.r[(size_t)c * D.ldr + i] = acc[c];
+                D.r32[(size_t)c * D.ldr + i] = (float)acc[c];
+            } else {
+                D.ra[(size_t)c * D.bs + i] = acc[c];
+            }
+        }
+    }
+    if (MODE == SODAGPU_FP8 && rows) {
+#pragma unroll
+        for (int c = 0; c < CT; ++c) {
+            const double t = block_sum(active ? acc[c] : 0.0, sh);
+            if (tid == 0) D.rsum[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// skipped SNPs (pivoted fallback only), one CTA per chain, SNPs in order.
+// The reference reads module copies of log_p / vare_gp here that its parallel
+// regions never assign; the current values are used.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_skipped(Dev D)
+{
+    __shared__ double sh[33];
+    __shared__ double s_d;
+    const int c = blockIdx.x, rep = cur_rep(D);
+    ChainScal *S = &D.scal[c];
+    double *r = D.r + (size_t)c * D.ldr;
+    for (int t = 0; t < D.nskipped; ++t) {
+        const int snploc = D.iskipped[t];
+        const int k = D.pos_of[snploc];
+        const int8_t *col = D.G + (size_t)k * D.ldx;
+        const double *xv = D.xv + (size_t)k * 4;
+        double part = 0.0;
+        for (int i = threadIdx.x; i < D.n; i += blockDim.x) part += r[i] * xv[col[i]];
+        const double dot = block_sum(part, sh);
+        if (threadIdx.x == 0) {
+            const size_t o = (size_t)c * D.p + snploc;
+            const double vare = S->vare, zz = D.xpx[snploc], zz_vare = zz / vare;
+            double gk = D.g[o], gt = 0.0, rhs = dot, upd = 0.0;
+            CRng R;
+            crng_init(R, D.seed, c, rep, snploc, P_SKIP);
+            int err = 0;
+            const int m = D.method, ng = D.ngroup, nm = D.nmix;
+            if (m == SODAGPU_BAYES_A) {
+                rhs = rhs + zz * gk;
+                const double v1 = zz + vare / D.vara_s[o];
+                gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+                upd = gk - gt;
+                D.g[o] = gt;
+                const double scale = (gt * gt + S->scale_va * D.df_va) / (D.df_va + 1.0);
+                D.vara_s[o] = d_rscinvchi2(D.df_va + 1.0, scale, R, &err);
+            } else if (m == SODAGPU_BAYES_B) {
+                if (D.cls[o] > 1) rhs = rhs + zz * gk;
+                const double vs = D.vara_s[o];
+                const double s1 = S->log_p[0];
+                const double logdetV = log(vs * zz_vare + 1.0);
+                const double uhat = rhs / (zz + vare / vs);
+                const double s2 = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[ng];
+                const double clike = s1 - s2;
+                double sk;
+                if (clike > 700) sk = 0.0;
+                else if (clike < -700) sk = 1.0;
+                else sk = 1.0 / (1.0 + exp(clike));
+                const double u = crng_unit(R);
+                const int flag = u < sk ? 2 : 1;
+                if (flag == 1) {
+                    gt = d_rnorm(0.0, sqrt(vs), R);
+                    upd = D.cls[o] > 1 ? gk : 0.0;
+                    D.g[o] = 0.0;
+                } else {
+                    const double v1 = zz + vare / vs;
+                    gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+                    upd = gk - gt;
+                    D.g[o] = gt;
+                }
+                D.cls[o] = flag;
+                const double scale = (gt * gt + S->scale_va * D.df_va) / (D.df_va + 1.0);
+                D.vara_s[o] = d_rscinvchi2(D.df_va + 1.0, scale, R, &err);
+            } else {
+                if (D.cls[o] > 1) rhs = rhs + zz * gk;
+                const int sg = D.grp[snploc] - 1;
+                double s[MAXDIST];
+                s[0] = S->log_p[sg];
+                for (int kk = 1; kk < nm; ++kk) {
+                    const double logdetV = log(S->gp[kk] * zz_vare + 1.0);
+                    const double uhat = rhs / (zz + S->vare_gp[kk]);
+                    s[kk] = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[sg + kk * ng];
+                }
+                const double u = crng_unit(R);
+                double ssculm = 0.0;
+                int flag = 1;
+                for (int kk = 0; kk < nm; ++kk) {
+                    const double skk = s[kk];
+                    double sk = 0.0;
+                    bool overflow = false;
+                    for (int j = 0; j < nm; ++j) {
+                        if (j == kk) continue;
+                        const double clike = s[j] - skk;
+                        if (clike < -700) continue;
+                        if (clike > 700) { overflow = true; break; }
+                        sk = sk + exp(clike);
+                    }
+                    ssculm = ssculm + (overflow ? 0.0 : 1.0 / (1.0 + sk));
+                    if (u < ssculm) { flag = kk + 1; break; }
+                }
+                if (flag == 1) {
+                    gt = 0.0;
+                    upd = D.cls[o] > 1 ? gk : 0.0;
+                } else {
+                    const double v1 = zz + vare / S->gp[flag - 1];
+                    gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+                    upd = gk - gt;
+                }
+                D.g[o] = gt;
+                D.cls[o] = flag;
+            }
+            if (err) flag_err(D, 1);
+            s_d = upd;
+        }
+        __syncthreads();
+        const double upd = s_d;
+        if (upd != 0.0)
+            for (int i = threadIdx.x; i < D.n; i += blockDim.x) r[i] = r[i] + xv[col[i]] * upd;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-iteration statistics: class counts and sum g^2 per (group, class),
+// sum r^2 (models.f90:194, 321-325, 496-503, 515)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_stats(Dev D)
+{
+    __shared__ double sh[33];
+    const int c = blockIdx.y;
+    if (blockIdx.x < NSTAT) {
+        const int ngm = D.ngroup * D.nmix;
+        const size_t base = (size_t)c * D.p;
+        for (int e = 0; e < ngm; ++e) {
+            const int eg = e % D.ngroup, em = e / D.ngroup;
+            double v = 0.0;
+            int cnt = 0;
+            for (int j = blockIdx.x * 256 + threadIdx.x; j < D.p; j += NSTAT * 256) {
+                const int cl = D.cls[base + j];
+                if (D.grp[j] - 1 == eg && cl - 1 == em) {
+                    const double gj = D.g[base + j];
+                    v += gj * gj;
+                    ++cnt;
+                }
+            }
+            const double tv = block_sum(v, sh);
+            const double tc = block_sum((double)cnt, sh);
+            if (threadIdx.x == 0) {
+                const size_t o = ((size_t)c * NSTAT + blockIdx.x) * ngm + e;
+                D.statpart[o] = tv;
+                D.cntpart[o] = (int32_t)tc;
+            }
+        }
+    } else {
+        const int rb = blockIdx.x - NSTAT;
+        const int i = rb * 256 + threadIdx.x;
+        const double v = i < D.n ? D.r[(size_t)c * D.ldr + i] : 0.0;
+        const double t = block_sum(v * v, sh);
+        if (threadIdx.x == 0) D.rpart[(size_t)c * D.nr_ctas + rb] = t;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_hyper(Dev D)
+{
+    __shared__ double s_vara;
+    const int c = blockIdx.x, rep = cur_rep(D);
+    ChainScal *S = &D.scal[c];
+    const int ng = D.ngroup, nm = D.nmix, ngm = ng * nm, m = D.method;
+    for (int e = threadIdx.x; e < ngm; e += blockDim.x) {
+        double v = 0.0;
+        int cnt = 0;
+        for (int t = 0; t < NSTAT; ++t) {
+            const size_t o = ((size_t)c * NSTAT + t) * ngm + e;
+            v += D.statpart[o];
+            cnt += D.cntpart[o];
+        }
+        S->varindist[e] = v;
+        S->snpindist[e] = cnt;
+    }
+    __syncthreads();
+    int err = 0;
+    if (threadIdx.x == 0) {
+        if (m == SODAGPU_BAYES_B) {
+            S->included = S->snpindist[ng];
+            S->varindist[0] = 0.0;
+        } else if (m != SODAGPU_BAYES_A) {
+            int excl = 0;
+            for (int i = 0; i < ng; ++i) excl += S->snpindist[i];
+            S->included = D.p - excl;
+            double scale = 0.0;
+            for (int i = 0; i < ng; ++i)
+                for (int j = 1; j < nm; ++j) scale = scale + S->varindist[i + j * ng] / D.mix[j];
+            scale = (scale + S->scale_va * D.df_va) / (D.df_va + (double)S->included);
+            CRng R;
+            crng_init(R, D.seed, c, rep, 0, P_VARA);
+            S->vara = d_rscinvchi2((double)S->included + D.df_va, scale, R, &err);
+            for (int j = 0; j < nm; ++j) S->gp[j] = D.mix[j] * S->vara;
+        }
+        double rr = 0.0;
+        for (int t = 0; t < D.nr_ctas; ++t) rr += D.rpart[(size_t)c * D.nr_ctas + t];
+        const double nn = (double)D.n;
+        const double scale = (rr + D.scale_ve * D.df_ve) / (nn + D.df_ve);
+        CRng R;
+        crng_init(R, D.seed, c, rep, 0, P_VARE);
+        S->vare = d_rscinvchi2(nn + D.df_ve, scale, R, &err);
+        s_vara = S->vara;
+    }
+    __syncthreads();
+    // pi ~ Dirichlet(counts + alpha), one thread per group (models.f90:517-522)
+    if (m == SODAGPU_BAYES_CPI || m == SODAGPU_BAYES_R || m == SODAGPU_BAYES_RC) {
+        for (int i = threadIdx.x; i < ng; i += blockDim.x) {
+            CRng R;
+            crng_init(R, D.seed, c, rep, i, P_PI);
+            double x[MAXDIST], sx = 0.0;
+            for (int j = 0; j < nm; ++j)
+                x[j] = d_rgamma((double)S->snpindist[i + j * ng] + D.alpha[j], 1.0, R, &err);
+            for (int j = 0; j < nm; ++j) sx = sx + x[j];
+            for (int j = 0; j < nm; ++j) S->p[i + j * ng] = x[j] / sx;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const bool keep = rep > D.burnin && rep % D.thin == 0;
+        S->keep = keep;
+        const double mu = S->mu[rep & 1];
+        if (keep) {
+            S->counter += 1;
+            S->mu_store = S->mu_store + mu;
+            for (int e = 0; e < ngm; ++e) S->varstore[e] = S->varstore[e] + S->varindist[e];
+            S->vare_store = S->vare_store + S->vare;
+            if (m != SODAGPU_BAYES_A) {
+                S->included_store = S->included_store + S->included;
+                for (int e = 0; e < ngm; ++e) S->snpstore[e] = S->snpstore[e] + S->snpindist[e];
+                if (m != SODAGPU_BAYES_B && m != SODAGPU_BAYES_C)
+                    for (int e = 0; e < ngm; ++e) S->pstore[e] = S->pstore[e] + S->p[e];
+            }
+            if (m != SODAGPU_BAYES_A && m != SODAGPU_BAYES_B) S->vara_store = S->vara_store + s_vara;
+        }
+        if (rep % D.thin == 0) {
+            RunCtl *ctl = D.ctl;
+            const int row = (ctl->trace_iter - 1) * D.chains + c;
+            if (ctl->trace && row >= 0 && row < ctl->trace_cap) {
+                sodagpu_trace_row *tr = ctl->trace + row;
+                tr->chain = c;
+                tr->rep = rep;
+                tr->included = S->included;
+                tr->pad = 0;
+                tr->mu = mu;
+                tr->vare = S->vare;
+                tr->vara = S->vara;
+                for (int j = 0; j < MAXDIST; ++j) {
+                    tr->snpindist[j] = j < nm ? S->snpindist[j * ng] : 0;
+                    tr->varindist[j] = j < nm ? S->varindist[j * ng] : 0.0;
+                }
+            }
+        }
+        // log_p and vare/gp for the next iteration (models.f90:198-199, 330-338)
+        if (m != SODAGPU_BAYES_A) {
+            for (int e = 0; e < ngm; ++e) S->log_p[e] = log(S->p[e]);
+            for (int j = 1; j < nm; ++j) S->vare_gp[j] = S->vare / S->gp[j];
+        }
+        if (err) flag_err(D, 1);
+    }
+}
+
+// ra redraw (models.f90:523-525) and the per-SNP accumulators (528, 535-538, 544)
+__global__ void __launch_bounds__(256) k_post(Dev D)
+{
+    const int c = blockIdx.y, rep = cur_rep(D);
+    const ChainScal *S = &D.scal[c];
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const double sd = sqrt(S->vare);
+    for (int i = t0; i < D.naind; i += stride) {
+        CRng R;
+        crng_init(R, D.seed, c, rep, i, P_RA);
+        D.ra[(size_t)c * D.bs + i] = d_rnorm(0.0, sd, R);
+    }
+    if (!S->keep) return;
+    const int m = D.method;
+    for (int j = t0; j < D.p; j += stride) {
+        const size_t o = (size_t)c * D.p + j;
+        D.gstore[o] = D.gstore[o] + D.g[o];
+        if (m != SODAGPU_BAYES_A) D.indist[o * D.nmix + (D.cls[o] - 1)] += 1u;
+        if (m == SODAGPU_BAYES_A || m == SODAGPU_BAYES_B)
+            D.vara_sstore[o] = D.vara_sstore[o] + D.vara_s[o];
+    }
+}
+
+// compute_residuals (utilities.f90:609-614), every `recal` iterations
+__global__ void __launch_bounds__(256) k_recal_partial(Dev D, int force)
+{
+    const int rep = cur_rep(D);
+    if (!force && (D.recal <= 0 || rep % D.recal != 0)) return;
+    const int c = blockIdx.z, split = blockIdx.y;
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= D.n) return;
+    const int per = (D.p + RECAL_SPLIT - 1) / RECAL_SPLIT;
+    const int k0 = split * per, k1 = min(D.p, k0 + per);
+    double acc = 0.0;
+    const double *g = D.g + (size_t)c * D.p;
+    for (int k = k0; k < k1; ++k) {
+        const double gj = g[D.perm[k]];
+        if (gj == 0.0) continue;
+        acc = acc + D.xv[(size_t)k * 4 + D.G[(size_t)k * D.ldx + i]] * gj;
+    }
+    D.recal_part[((size_t)c * RECAL_SPLIT + split) * D.ldr + i] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_recal_apply(Dev D, int force, int mu_slot)
+{
+    const int rep = cur_rep(D);
+    if (!force && (D.recal <= 0 || rep % D.recal != 0)) return;
+    const int c = blockIdx.y;
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= D.n) return;
+    double d = 0.0;
+    for (int s = 0; s < RECAL_SPLIT; ++s) d = d + D.recal_part[((size_t)c * RECAL_SPLIT + s) * D.ldr + i];
+    const int slot = mu_slot >= 0 ? mu_slot : (rep & 1);
+    const double v = D.y[i] - d - D.scal[c].mu[slot];
+    D.r[(size_t)c * D.ldr + i] = v;
+    D.r32[(size_t)c * D.ldr + i] = (float)v;
+}
+
+// ---------------------------------------------------------------------------
+// chain initialisation (models.f90:56-128)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_init_chain(Dev D, double vara0, double scale_va0)
+{
+    __shared__ double sh[33];
+    const int c = blockIdx.x, m = D.method, ng = D.ngroup, nm = D.nmix;
+    ChainScal *S = &D.scal[c];
+    const double nn = (double)D.n;
+    double sy = 0.0;
+    for (int i = threadIdx.x; i < D.n; i += blockDim.x) sy += D.y[i];
+    sy = block_sum(sy, sh);
+    const double mu = sy / nn;
+    double rr = 0.0, vy = 0.0;
+    for (int i = threadIdx.x; i < D.n; i += blockDim.x) {
+        const double v = (D.y[i] - 0.0) - mu;
+        D.r[(size_t)c * D.ldr + i] = v;
+        D.r32[(size_t)c * D.ldr + i] = (float)v;
+        rr += v * v;
+        vy += (D.y[i] - mu) * (D.y[i] - mu);
+    }
+    rr = block_sum(rr, sh);
+    vy = block_sum(vy, sh);
+    if (threadIdx.x == 0) {
+        S->mu[0] = mu;
+        S->mu[1] = mu;
+        S->scale_va = scale_va0;
+        S->vara = vara0;
+        S->counter = 0;
+        S->keep = 0;
+        S->err = 0;
+        S->included = 0;
+        S->mu_store = S->vare_store = S->vara_store = S->included_store = 0.0;
+        for (int e = 0; e < MAXGM; ++e) {
+            S->snpstore[e] = S->pstore[e] = S->varstore[e] = 0.0;
+            S->varindist[e] = 0.0;
+            S->snpindist[e] = 0;
+            S->p[e] = 0.0;
+            S->log_p[e] = 0.0;
+        }
+        if (m != SODAGPU_BAYES_A) {
+            if (m == SODAGPU_BAYES_B || m == SODAGPU_BAYES_C) {
+                for (int i = 0; i < ng; ++i) {
+                    S->p[i] = D.pizero;
+                    S->p[i + ng] = 1.0 - D.pizero;
+                }
+            } else {
+                for (int i = 0; i < ng; ++i) {
+                    S->p[i] = 0.5;
+                    double s = 0.0;
+                    for (int j = 1; j < nm; ++j) S->p[i + j * ng] = 1.0 / D.mix[j];
+                    for (int j = 1; j < nm; ++j) s = s + S->p[i + j * ng];
+                    for (int j = 1; j < nm; ++j) S->p[i + j * ng] = 0.5 * S->p[i + j * ng] / s;
+                }
+            }
+        }
+        if (D.df_va <= 0.0) {
+            const double vary = vy / (nn - 1.0);
+            if (m == SODAGPU_BAYES_A) {
+                S->vara = S->scale_va * vary / D.p;
+            } else if (m == SODAGPU_BAYES_B) {
+                S->vara = S->scale_va * vary / D.p / S->p[ng];
+            } else {
+                for (int i = 0; i < ng; ++i) {
+                    double dp = 0.0;
+                    for (int j = 0; j < nm; ++j) dp = dp + S->p[i + j * ng] * D.mix[j];
+                    S->vara = S->vara + dp;
+                }
+                S->vara = S->scale_va * vary / D.p / S->vara;
+            }
+            S->scale_va = 0.0;
+        } else {
+            S->vara = S->scale_va * D.df_va / (D.df_va + 2.0);
+        }
+        for (int j = 0; j < nm; ++j) S->gp[j] = D.mix[j] * S->vara;
+        const double scale = (rr + D.scale_ve * D.df_ve) / (nn + D.df_ve);
+        CRng R;
+        crng_init(R, D.seed, c, 0, 0, P_VARE);
+        int err = 0;
+        S->vare = d_rscinvchi2(nn + D.df_ve, scale, R, &err);
+        if (err) flag_err(D, 1);
+        if (m != SODAGPU_BAYES_A) {
+            for (int e = 0; e < ng * nm; ++e) S->log_p[e] = log(S->p[e]);
+            for (int j = 1; j < nm; ++j) S->vare_gp[j] = S->vare / S->gp[j];
+        }
+    }
+    __syncthreads();
+    const double sd = sqrt(S->vare);
+    for (int i = threadIdx.x; i < D.bs; i += blockDim.x) {
+        double v = 0.0;
+        if (i < D.naind) {
+            CRng R;
+            crng_init(R, D.seed, c, 0, i, P_RA);
+            v = d_rnorm(0.0, sd, R);
+        }
+        D.ra[(size_t)c * D.bs + i] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_init_snp(Dev D)
+{
+    const int c = blockIdx.y;
+    const double vara = D.scal[c].vara;
+    const int m = D.method;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < D.p; j += gridDim.x * blockDim.x) {
+        const size_t o = (size_t)c * D.p + j;
+        D.g[o] = 0.0;
+        D.cls[o] = m == SODAGPU_BAYES_A ? 1 : 2;
+        D.vara_s[o] = (m == SODAGPU_BAYES_A || m == SODAGPU_BAYES_B) ? vara : 0.0;
+        D.gstore[o] = 0.0;
+        D.vara_sstore[o] = 0.0;
+        for (int q = 0; q < D.nmix; ++q) D.indist[o * D.nmix + q] = 0u;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launch helpers
+// ---------------------------------------------------------------------------
+template <int MODE, int CT>
+static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int wpc, cudaStream_t st)
+{
+    const int grid1 = (nblk_snps + wpc - 1) / wpc;
+    k_rhs_draw<MODE, CT><<<grid1, 32 * wpc, 0, st>>>(D, b, wpc);
+    const int grid2 = D.nr_ctas + (D.bs + ROW_THREADS - 1) / ROW_THREADS;
+    k_update<MODE, CT><<<grid2, ROW_THREADS, update_smem_bytes(D.bs), st>>>(D, b);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int wpc, cudaStream_t st)
+{
+    switch (D.chains) {
+    case 1: return launch_block<MODE, 1>(D, b, nsnp, wpc, st);
+    case 2: return launch_block<MODE, 2>(D, b, nsnp, wpc, st);
+    case 4: return launch_block<MODE, 4>(D, b, nsnp, wpc, st);
+    case 8: return launch_block<MODE, 8>(D, b, nsnp, wpc, st);
+    case 16: return launch_block<MODE, 16>(D, b, nsnp, wpc, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+int sweep_chain_count_supported(int c) { return c == 1 || c == 2 || c == 4 || c == 8 || c == 16; }
+
+template <int MODE>
+static cudaError_t set_update_smem_mode(size_t bytes)
+{
+    cudaError_t e = cudaSuccess;
+    e = cudaFuncSetAttribute(k_update<MODE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return e;
+}
+
+// Raises the dynamic shared-memory limit of the update kernels for large subsets.
+cudaError_t sweep_prepare(int bs)
+{
+    const size_t bytes = update_smem_bytes(bs);
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    if (bytes > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = set_update_smem_mode<SODAGPU_FP64>(bytes);
+    if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP32>(bytes);
+    if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP8>(bytes);
+    return e;
+}
+
+cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, cudaStream_t st)
+{
+    const int C = D.chains;
+    k_iter_begin<<<1, 1, 0, st>>>(D);
+    k_mu_partial<<<dim3(D.nr_ctas, C), ROW_THREADS, 0, st>>>(D);
+    k_mu_apply<<<dim3(D.nr_ctas, C), ROW_THREADS, 0, st>>>(D);
+    for (int b = 0; b < D.nb; ++b) {
+        const int nsnp = blk_sizes[b];
+        // about two CTAs per SM, at most 8 warps per CTA
+        int wpc = (nsnp + 2 * sm_count - 1) / (2 * sm_count);
+        wpc = wpc < 1 ? 1 : (wpc > 8 ? 8 : wpc);
+        cudaError_t e;
+        if (D.precision == SODAGPU_FP64) e = launch_block_mode<SODAGPU_FP64>(D, b, nsnp, wpc, st);
+        else if (D.precision == SODAGPU_FP32) e = launch_block_mode<SODAGPU_FP32>(D, b, nsnp, wpc, st);
+        else e = launch_block_mode<SODAGPU_FP8>(D, b, nsnp, wpc, st);
+        if (e != cudaSuccess) return e;
+    }
+    if (D.nskipped > 0) k_skipped<<<C, 1024, 0, st>>>(D);
+    k_stats<<<dim3(NSTAT + D.nr_ctas, C), 256, 0, st>>>(D);
+    k_hyper<<<C, 128, 0, st>>>(D);
+    const int pgrid = (D.p + 255) / 256 < 4 * sm_count ? (D.p + 255) / 256 : 4 * sm_count;
+    k_post<<<dim3(pgrid > 0 ? pgrid : 1, C), 256, 0, st>>>(D);
+    k_recal_partial<<<dim3((D.n + 255) / 256, RECAL_SPLIT, C), 256, 0, st>>>(D, 0);
+    k_recal_apply<<<dim3((D.n + 255) / 256, C), 256, 0, st>>>(D, 0, -1);
+    return cudaGetLastError();
+}
+
+cudaError_t sweep_enqueue_init(const Dev &D, double vara0, double scale_va0, int sm_count, cudaStream_t st)
+{
+    k_init_chain<<<D.chains, 256, 0, st>>>(D, vara0, scale_va0);
+    const int pgrid = (D.p + 255) / 256 < 4 * sm_count ? (D.p + 255) / 256 : 4 * sm_count;
+    k_init_snp<<<dim3(pgrid > 0 ? pgrid : 1, D.chains), 256, 0, st>>>(D);
+    return cudaGetLastError();
+}
+
+cudaError_t sweep_enqueue_recal(const Dev &D, double mu_slot_unused, cudaStream_t st)
+{
+    (void)mu_slot_unused;
+    k_recal_partial<<<dim3((D.n + 255) / 256, RECAL_SPLIT, D.chains), 256, 0, st>>>(D, 1);
+    k_recal_apply<<<dim3((D.n + 255) / 256, D.chains), 256, 0, st>>>(D, 1, -1);
+    return cudaGetLastError();
+}
+
+}  // namespace soda
