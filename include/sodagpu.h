@@ -200,8 +200,18 @@ int sodagpu_predict(int32_t nind, int32_t nloci, const void *geno, int32_t layou
                     const double *freq, double mu, const double *effects,
                     double *pred);
 
-/* Seconds spent in the last sodagpu_build_z and sodagpu_run calls. */
-int sodagpu_timings(sodagpu_ctx *ctx, double *build_z_s, double *run_s);
+/* Seconds spent in the last sodagpu_build_z and sodagpu_run calls (host
+ * clock), and the device time of the last run's iterations in milliseconds
+ * (CUDA events on the context's stream around the iteration launches). */
+int sodagpu_timings(sodagpu_ctx *ctx, double *build_z_s, double *run_s, double *run_device_ms);
+
+/* Measurement hook: runs `iters` iterations (advancing the chains exactly like
+ * sodagpu_run) with kernels launched one by one and a CUDA-event pair around
+ * each launch.  ms[c] receives the summed device time and launches[c] the
+ * launch count of kernel class c: 0 rhs + per-SNP draws, 1 residual update,
+ * 2 mu draw, 3 hyper-parameter draws and accumulators. */
+#define SODAGPU_NPROF 4
+int sodagpu_profile_kernels(sodagpu_ctx *ctx, int32_t iters, double *ms, int32_t *launches);
 
 void sodagpu_destroy(sodagpu_ctx *ctx);
 const char *sodagpu_errstr(int code);

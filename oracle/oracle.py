@@ -41,6 +41,7 @@ PROTOTYPES = {
     "oracle_init_chains": (C.c_int, [_P]),
     "oracle_run": (C.c_int, [_P, C.c_int32, TRACE_CB, _P]),
     "oracle_run_blocks": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "oracle_set_sparse_state": (C.c_int, [_P, C.c_double, C.c_int64]),
     "oracle_get_state": (C.c_int, [_P, C.c_int32, _DP, _IP, _DP, _DP, _DP, _DP]),
     "oracle_get_results": (C.c_int, [_P, C.c_int32, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
     "oracle_compute_dgv": (C.c_int, [_P, C.c_double, _DP, _DP]),
@@ -160,6 +161,9 @@ class Oracle:
 
     def run_blocks(self, first_block: int, nblocks_run: int, reps: int = 1):
         _chk(self._lib.oracle_run_blocks(self._o, first_block, nblocks_run, reps), "oracle_run_blocks")
+
+    def set_sparse_state(self, incl: float, seed: int = 1):
+        _chk(self._lib.oracle_set_sparse_state(self._o, float(incl), seed), "oracle_set_sparse_state")
 
     def state(self, chain: int = 0) -> dict:
         g = np.empty(self.p)

@@ -566,6 +566,7 @@ static int cholesky_pd_ld(int n, const double *A, double *U, int ldu)
         if (tmp <= 0.0 || isnan(tmp)) return i + 1;
         double uii = sqrt(tmp);
         U[IDX2(i, i, ldu)] = uii;
+#pragma omp parallel for schedule(static) if (n - i > 256)
         for (int j = i + 1; j < n; ++j) {
             double dj = 0.0;
             for (int k = 0; k < i; ++k) dj = dj + U[IDX2(k, j, ldu)] * U[IDX2(k, i, ldu)];
@@ -712,8 +713,18 @@ int oracle_build_z(oracle_ctx *o, const int32_t *permvec, int64_t power_maxit,
         ctr_init(&r.c, o->cfg.seed, 0, 0, b, P_POWER);
         for (int i = 0; i < nn; ++i) start[i] = rng_u(&r);
         double lam;
-        int64_t maxit = power_maxit > 0 ? power_maxit : (int64_t)1000 * nn;
-        oracle_power_method(nn, xx, start, maxit, &lam, NULL);
+        if (power_maxit < 0) {
+            /* timing samples only: Gershgorin upper bound instead of lambda_max */
+            lam = 0.0;
+            for (int j = 0; j < nn; ++j) {
+                double rs = 0.0;
+                for (int k = 0; k < nn; ++k) rs += fabs(xx[IDX2(k, j, nn)]);
+                if (rs > lam) lam = rs;
+            }
+        } else {
+            int64_t maxit = power_maxit > 0 ? power_maxit : (int64_t)1000 * nn;
+            oracle_power_method(nn, xx, start, maxit, &lam, NULL);
+        }
         double d = lam + D_SHIFT + d_offset;
         o->xxd[b] = d;
         for (size_t t = 0; t < (size_t)nn * nn; ++t) xx[t] = -xx[t];
@@ -1303,9 +1314,35 @@ int oracle_run_blocks(oracle_ctx *o, int32_t first_block, int32_t nblocks_run, i
     if (!o || !o->have_chain) return SODAGPU_E_STATE;
     if (first_block < 0 || nblocks_run < 1 || first_block + nblocks_run > o->nb) return SODAGPU_E_ARG;
     chain_t *c = &o->ch[0];
+    const int nm = o->nmix, ng = o->ngroup;
     for (int t = 0; t < reps; ++t) {
         c->rep++;
+        if (o->method != SODAGPU_BAYES_A) {
+            for (int i = 0; i < ng; ++i)
+                for (int j = 0; j < nm; ++j) c->log_p[IDX2(i, j, ng)] = log(c->p[IDX2(i, j, ng)]);
+            for (int j = 1; j < nm; ++j) c->vare_gp[j] = c->vare / c->gp[j];
+        }
         for (int b = first_block; b < first_block + nblocks_run; ++b) sweep_block(o, c, 0, b, c->rep);
+    }
+    return 0;
+}
+
+/* Timing helper: puts chain 0 in the sparse state of a settled BayesC-type
+ * chain — a random fraction `incl` of SNPs in class 2 (with g = 0, so the
+ * residuals stay consistent) and pi = (1-incl, incl). */
+int oracle_set_sparse_state(oracle_ctx *o, double incl, int64_t seed)
+{
+    if (!o || !o->have_chain) return SODAGPU_E_STATE;
+    if (o->method == SODAGPU_BAYES_A || o->method == SODAGPU_BAYES_B) return SODAGPU_E_ARG;
+    chain_t *c = &o->ch[0];
+    xo_state st;
+    xo_streams(seed, 1, &st);
+    for (int j = 0; j < o->p; ++j) c->cls[j] = u64_to_unit(xo_next(&st)) < incl ? 2 : 1;
+    for (int i = 0; i < o->ngroup; ++i) {
+        c->p[IDX2(i, 0, o->ngroup)] = 1.0 - incl;
+        for (int k = 1; k < o->nmix; ++k) c->p[IDX2(i, k, o->ngroup)] = incl / (o->nmix - 1);
+        for (int k = 0; k < o->nmix; ++k)
+            c->log_p[IDX2(i, k, o->ngroup)] = log(c->p[IDX2(i, k, o->ngroup)]);
     }
     return 0;
 }

@@ -50,6 +50,7 @@ int oracle_init_chains(oracle_ctx *o);
 int oracle_run(oracle_ctx *o, int32_t iters, sodagpu_trace_cb cb, void *user);
 int oracle_run_blocks(oracle_ctx *o, int32_t first_block, int32_t nblocks_run,
                       int32_t reps);
+int oracle_set_sparse_state(oracle_ctx *o, double incl, int64_t seed);
 int oracle_get_state(oracle_ctx *o, int32_t chain, double *g, int32_t *cls,
                      double *vara_s, double *yadj, double *yaadj, double *scalars);
 int oracle_get_results(oracle_ctx *o, int32_t chain, double *gstore,

@@ -197,10 +197,14 @@ class SodaJob:
 
     # -- setup -----------------------------------------------------------------
     def load_genotypes(self, codes=None, bed: Optional[np.ndarray] = None, device_ptr: Optional[int] = None,
-                       layout: int = GENO_CODES) -> None:
+                       host_ptr: Optional[int] = None, layout: int = GENO_CODES) -> None:
         """codes: int8 (nind, nloci) 0/1/2 (column-major is copied as-is);
         bed: uint8 PLINK payload without the magic header;
-        device_ptr: a device address holding `layout` data."""
+        device_ptr / host_ptr: an address holding `layout` data (e.g. pinned memory)."""
+        if host_ptr is not None:
+            _check(self._lib.sodagpu_load_genotypes(self._ctx, C.c_void_p(host_ptr), layout),
+                   "sodagpu_load_genotypes")
+            return
         if device_ptr is not None:
             _check(self._lib.sodagpu_load_genotypes(self._ctx, C.c_void_p(device_ptr), layout | GENO_DEVICE_PTR),
                    "sodagpu_load_genotypes")
@@ -293,9 +297,18 @@ class SodaJob:
         return out
 
     def timings(self):
-        b, r = C.c_double(), C.c_double()
-        _check(self._lib.sodagpu_timings(self._ctx, C.byref(b), C.byref(r)), "sodagpu_timings")
-        return b.value, r.value
+        """(build_z seconds, last run seconds, last run device milliseconds)"""
+        b, r, d = C.c_double(), C.c_double(), C.c_double()
+        _check(self._lib.sodagpu_timings(self._ctx, C.byref(b), C.byref(r), C.byref(d)), "sodagpu_timings")
+        return b.value, r.value, d.value
+
+    def profile_kernels(self, iters: int) -> dict:
+        """Per-kernel-class device time (ms) and launch counts over `iters` eager iterations."""
+        ms = np.zeros(4)
+        n = np.zeros(4, dtype=np.int32)
+        _check(self._lib.sodagpu_profile_kernels(self._ctx, int(iters), _dp(ms), _ip(n)), "sodagpu_profile_kernels")
+        names = ("rhs_draw", "update", "mu", "other")
+        return {names[k]: (float(ms[k]), int(n[k])) for k in range(4)}
 
 
 def predict(codes=None, freq=None, mu: float = 0.0, effects=None, bed: Optional[np.ndarray] = None,

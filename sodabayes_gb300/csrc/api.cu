@@ -84,7 +84,7 @@ struct sodagpu_ctx {
     int dev = 0, sm_count = 0;
     cudaStream_t st = nullptr;
     int n = 0, p = 0, bs = 0, nb = 0, bt = 0, C = 0, ldx = 0, ldr = 0, nr_ctas = 0;
-    int nskipped = 0, naind = 0;
+    int nskipped = 0, naind = 0, nsplit = 1;
     double d_offset = 0.0;
     bool have_geno = false, have_pheno = false, have_z = false, have_chain = false;
     std::vector<void *> allocs;
@@ -108,13 +108,14 @@ struct sodagpu_ctx {
     uint32_t *indist = nullptr;
     ChainScal *scal = nullptr;
     RunCtl *ctl = nullptr;
-    double *delta = nullptr, *rpart = nullptr, *rsum = nullptr, *statpart = nullptr, *recal_part = nullptr;
-    int32_t *cntpart = nullptr;
+    double *delta = nullptr, *rpart = nullptr, *rsum = nullptr, *statpart = nullptr, *recal_part = nullptr,
+           *upart = nullptr, *rpx = nullptr, *rpu = nullptr;
+    int32_t *cntpart = nullptr, *ucount = nullptr, *rticket = nullptr;
     uint8_t *nzflag = nullptr;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
     cudaGraphExec_t graph = nullptr;
-    double t_build = 0.0, t_run = 0.0;
+    double t_build = 0.0, t_run = 0.0, t_run_dev_ms = 0.0;
     Dev D;
 
     template <class T>
@@ -246,7 +247,7 @@ int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out)
     c->C = cfg->chains;
     c->ldx = (int)round_up((size_t)c->n, 128);
     c->ldr = c->ldx;
-    c->nr_ctas = (c->n + ROW_THREADS - 1) / ROW_THREADS;
+    c->nr_ctas = (c->n + ROW_TILE - 1) / ROW_TILE;
     // block bounds (models.f90:136-142), 0-based first positions
     c->h_blk_ls.resize(c->nb + 1);
     c->blk_sizes.resize(c->nb);
@@ -683,6 +684,12 @@ int build_dev(sodagpu_ctx *c)
     D.statpart = c->statpart;
     D.cntpart = c->cntpart;
     D.recal_part = c->recal_part;
+    D.upart = c->upart;
+    D.ucount = c->ucount;
+    D.nsplit = c->nsplit;
+    D.rpx = c->rpx;
+    D.rpu = c->rpu;
+    D.rticket = c->rticket;
     return 0;
 }
 
@@ -713,6 +720,13 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         TRY(c->alloc(&c->statpart, (size_t)C * NSTAT * ngm));
         TRY(c->alloc(&c->cntpart, (size_t)C * NSTAT * ngm));
         TRY(c->alloc(&c->recal_part, (size_t)C * RECAL_SPLIT * c->ldr));
+        const int ntile = c->nr_ctas + (c->bs + ROW_TILE - 1) / ROW_TILE;
+        c->nsplit = std::max(1, std::min(16, (2 * c->sm_count + ntile - 1) / ntile));
+        TRY(c->alloc(&c->upart, (size_t)ntile * c->nsplit * C * ROW_TILE));
+        TRY(c->alloc(&c->ucount, ntile));
+        TRY(c->alloc(&c->rpx, (size_t)RHS_KSPLIT_MAX * C * c->bs));
+        TRY(c->alloc(&c->rpu, (size_t)RHS_KSPLIT_MAX * C * c->bs));
+        TRY(c->alloc(&c->rticket, c->bs));
     }
     build_dev(c);
     RunCtl h{};
@@ -765,9 +779,19 @@ int sodagpu_run(sodagpu_ctx *c, int32_t iters, sodagpu_trace_cb cb, void *user)
     h.trace_count = 0;
     h.trace = cb ? c->trace : nullptr;
     CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaEventRecord(e0, c->st));
     for (int t = 0; t < iters; ++t) CUDA_TRY(cudaGraphLaunch(c->graph, c->st));
+    CUDA_TRY(cudaEventRecord(e1, c->st));
     CUDA_TRY(cudaMemcpyAsync(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost, c->st));
     CUDA_TRY(cudaStreamSynchronize(c->st));
+    float dev_ms = 0.f;
+    cudaEventElapsedTime(&dev_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->t_run_dev_ms = dev_ms;
     c->t_run = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (h.err) return fail(SODAGPU_E_TIMEOUT, "a bounded device loop gave up (code %d)", h.err);
     if (cb && rows > 0) {
@@ -950,12 +974,49 @@ int sodagpu_predict(int32_t nind, int32_t nloci, const void *geno, int32_t layou
     return 0;
 }
 
-int sodagpu_timings(sodagpu_ctx *c, double *build_z_s, double *run_s)
+int sodagpu_timings(sodagpu_ctx *c, double *build_z_s, double *run_s, double *run_device_ms)
 {
     if (!c) return fail(SODAGPU_E_ARG, "null argument");
     if (build_z_s) *build_z_s = c->t_build;
     if (run_s) *run_s = c->t_run;
+    if (run_device_ms) *run_device_ms = c->t_run_dev_ms;
     return 0;
+}
+
+int sodagpu_profile_kernels(sodagpu_ctx *c, int32_t iters, double *ms, int32_t *launches)
+{
+    if (!c || !ms || !launches) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_chain) return fail(SODAGPU_E_STATE, "call sodagpu_init_chains first");
+    for (int k = 0; k < PROF_NCLASS; ++k) { ms[k] = 0.0; launches[k] = 0; }
+    RunCtl h{};
+    CUDA_TRY(cudaMemcpyAsync(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    h.trace = nullptr;
+    h.trace_cap = 0;
+    h.trace_iter = 0;
+    CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
+    const int cap = 2 * c->nb + 8;
+    std::vector<cudaEvent_t> ev(2 * cap);
+    std::vector<int> cls(cap);
+    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
+    int rc = 0;
+    for (int t = 0; t < iters && rc == 0; ++t) {
+        ProfHook hook{ev.data(), cls.data(), 0, cap};
+        cudaError_t e = sweep_enqueue_iteration(c->D, c->blk_sizes.data(), c->sm_count, c->st, &hook);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        if (e != cudaSuccess) {
+            rc = fail(SODAGPU_E_CUDA, "profiled iteration failed: %s", cudaGetErrorString(e));
+            break;
+        }
+        for (int q = 0; q < hook.n; ++q) {
+            float x = 0.f;
+            cudaEventElapsedTime(&x, ev[2 * q], ev[2 * q + 1]);
+            ms[cls[q]] += x;
+            launches[cls[q]] += 1;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return rc;
 }
 
 void sodagpu_destroy(sodagpu_ctx *c)

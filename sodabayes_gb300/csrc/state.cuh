@@ -55,7 +55,7 @@ struct Dev {
     int ldx;                   // column stride of G / X32 (elements)
     int ldr;                   // chain stride of r / r32
     int nskipped, naind;
-    int nr_ctas;               // row CTAs of the residual kernels
+    int nr_ctas;               // row tiles (ROW_TILE rows) of the residual kernels
     int recal;
     int burnin, thin;
     uint64_t seed;
@@ -98,10 +98,19 @@ struct Dev {
     double *statpart;          // [C][NSTAT][ngroup*nmix] sum g^2
     int32_t *cntpart;          // [C][NSTAT][ngroup*nmix] counts
     double *recal_part;        // [C][RECAL_SPLIT][ldr]
+    double *upart;             // [tiles][nsplit][C][ROW_TILE] update partial sums
+    int32_t *ucount;           // [tiles] update tickets (self-resetting)
+    int nsplit;                // column splits of the update
+    double *rpx, *rpu;         // [RHS_KSPLIT_MAX][C][bs] rhs partial sums (genotype / augmented part)
+    int32_t *rticket;          // [bs] rhs tickets per M tile (self-resetting)
 };
 
+constexpr int RHS_KSPLIT_MAX = 16;
+
 constexpr int NSTAT = 64;          // CTAs of the per-iteration SNP statistics
-constexpr int ROW_THREADS = 256;   // rows per row-CTA
+constexpr int ROW_THREADS = 256;   // threads of the row kernels
+constexpr int ROWS_PER_THREAD = 4;
+constexpr int ROW_TILE = ROW_THREADS * ROWS_PER_THREAD;   // rows per row CTA
 constexpr int RECAL_SPLIT = 32;    // column splits of the residual recalibration
 
 }  // namespace soda

@@ -4,7 +4,7 @@
 //   mu draw                              k_mu_partial + k_mu_apply   (models.f90:130-132)
 //   for each subset b (sequential):
 //     rhs_j = x_j'r + u_j'ra (+d g_j) and the per-SNP draw
-//                                        k_rhs_draw                  (models.f90:146-162, 211-256, 350-413)
+//                                        k_rhs (rhs_kernel.cuh)      (models.f90:146-162, 211-256, 350-413)
 //     r += X_b delta, ra += U_b delta    k_update                    (models.f90:164-174, 258-272, 415-430)
 //   single-site updates of skipped SNPs  k_skipped                   (models.f90:178-193, 276-320, 433-495)
 //   class counts, sum g^2, sum r^2       k_stats
@@ -148,6 +148,12 @@ __device__ double draw_snp(const Dev &D, const ChainScal *S, int c, int rep, int
     return gold - gnew;
 }
 
+}  // namespace soda
+
+#include "rhs_kernel.cuh"
+
+namespace soda {
+
 // ---------------------------------------------------------------------------
 // iteration start and the mu draw
 // ---------------------------------------------------------------------------
@@ -164,8 +170,12 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_partial(Dev D)
     __shared__ double sh[33];
     const int c = blockIdx.y, rep = cur_rep(D);
     const double mu_old = D.scal[c].mu[(rep - 1) & 1];
-    const int i = blockIdx.x * ROW_THREADS + threadIdx.x;
-    const double v = i < D.n ? D.r[(size_t)c * D.ldr + i] + mu_old : 0.0;
+    double v = 0.0;
+#pragma unroll
+    for (int q = 0; q < ROWS_PER_THREAD; ++q) {
+        const int i = blockIdx.x * ROW_TILE + q * ROW_THREADS + threadIdx.x;
+        if (i < D.n) v += D.r[(size_t)c * D.ldr + i] + mu_old;
+    }
     const double t = block_sum(v, sh);
     if (threadIdx.x == 0) D.rpart[(size_t)c * D.nr_ctas + blockIdx.x] = t;
 }
@@ -189,167 +199,53 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
     }
     __syncthreads();
     const double mu = s_mu;
-    const int i = blockIdx.x * ROW_THREADS + threadIdx.x;
-    double v = 0.0;
-    if (i < D.n) {
-        const size_t o = (size_t)c * D.ldr + i;
-        v = (D.r[o] + mu_old) - mu;
-        D.r[o] = v;
-        D.r32[o] = (float)v;
+    double vs = 0.0;
+#pragma unroll
+    for (int q = 0; q < ROWS_PER_THREAD; ++q) {
+        const int i = blockIdx.x * ROW_TILE + q * ROW_THREADS + threadIdx.x;
+        if (i < D.n) {
+            const size_t o = (size_t)c * D.ldr + i;
+            const double v = (D.r[o] + mu_old) - mu;
+            D.r[o] = v;
+            D.r32[o] = (float)v;
+            vs += v;
+        }
     }
     if (D.precision == SODAGPU_FP8) {
-        const double t = block_sum(v, sh);
+        const double t = block_sum(vs, sh);
         if (threadIdx.x == 0) D.rsum[(size_t)c * D.nr_ctas + blockIdx.x] = t;
     }
 }
 
 // ---------------------------------------------------------------------------
-// rhs and draw: one warp per subset position, all chains.
+// residual update r += X_b delta (rows of r) and ra += U_b delta (rows of ra)
+// (models.f90:164-174).  Only positions with a non-zero delta in some chain
+// contribute.  Each row tile (1024 rows) is split over `nsplit` CTAs by
+// column chunks; every CTA writes its partial sums, and the last CTA of the
+// tile to finish (atomic ticket) adds them in split order — deterministic,
+// no waiting.  FP64 mode accumulates in FP64, the FP32/FP8 modes in FP32;
+// the master residual is FP64 in every mode.
 // ---------------------------------------------------------------------------
-template <int MODE, int CT>
-__global__ void __launch_bounds__(256) k_rhs_draw(Dev D, int b, int wpc)
-{
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ls = D.blk_ls[b];
-    const int N = D.blk_ls[b + 1] - ls;
-    const int jk = blockIdx.x * wpc + warp;
-    if (warp >= wpc || jk >= N) return;
-    const int k = ls + jk;
-    const int rep = cur_rep(D);
-    if (D.skip[k]) {
-        if (lane < CT) D.delta[(size_t)lane * D.bs + jk] = 0.0;
-        if (lane == 0) D.nzflag[jk] = 0;
-        return;
-    }
-    typedef typename std::conditional<MODE == SODAGPU_FP64, double, float>::type acc_t;
-    acc_t acc[CT];
-#pragma unroll
-    for (int c = 0; c < CT; ++c) acc[c] = 0;
-
-    if (MODE == SODAGPU_FP64) {
-        const int8_t *col = D.G + (size_t)k * D.ldx;
-        const double x0 = D.xv[(size_t)k * 4 + 0], x1 = D.xv[(size_t)k * 4 + 1],
-                     x2 = D.xv[(size_t)k * 4 + 2];
-        for (int i = lane; i < D.n; i += 32) {
-            const int code = col[i];
-            const double x = code == 0 ? x0 : (code == 1 ? x1 : x2);
-#pragma unroll
-            for (int c = 0; c < CT; ++c) acc[c] += (acc_t)(x * D.r[(size_t)c * D.ldr + i]);
-        }
-    } else if (MODE == SODAGPU_FP32) {
-        const float4 *col = reinterpret_cast<const float4 *>(D.X32 + (size_t)k * D.ldx);
-        const int n4 = D.ldx >> 2;
-#pragma unroll 4
-        for (int i4 = lane; i4 < n4; i4 += 32) {
-            const float4 xx = __ldg(col + i4);
-#pragma unroll
-            for (int c = 0; c < CT; ++c) {
-                const float4 rr = __ldg(reinterpret_cast<const float4 *>(D.r32 + (size_t)c * D.ldr) + i4);
-                acc[c] = fmaf(xx.x, rr.x, acc[c]);
-                acc[c] = fmaf(xx.y, rr.y, acc[c]);
-                acc[c] = fmaf(xx.z, rr.z, acc[c]);
-                acc[c] = fmaf(xx.w, rr.w, acc[c]);
-            }
-        }
-    } else {  // FP8: exact codes, rank-1 centring after the dot product
-        const uint4 *col = reinterpret_cast<const uint4 *>(D.G + (size_t)k * D.ldx);
-        const int n16 = D.ldx >> 4;
-#pragma unroll 2
-        for (int i16 = lane; i16 < n16; i16 += 32) {
-            const uint4 w = __ldg(col + i16);
-            const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float g0 = (float)(ww[q] & 0xff), g1 = (float)((ww[q] >> 8) & 0xff),
-                            g2 = (float)((ww[q] >> 16) & 0xff), g3 = (float)(ww[q] >> 24);
-#pragma unroll
-                for (int c = 0; c < CT; ++c) {
-                    const float4 rr = __ldg(reinterpret_cast<const float4 *>(D.r32 + (size_t)c * D.ldr) +
-                                            i16 * 4 + q);
-                    acc[c] = fmaf(g0, rr.x, acc[c]);
-                    acc[c] = fmaf(g1, rr.y, acc[c]);
-                    acc[c] = fmaf(g2, rr.z, acc[c]);
-                    acc[c] = fmaf(g3, rr.w, acc[c]);
-                }
-            }
-        }
-    }
-    // u_k' ra over the stored rows of column k
-    acc_t accu[CT];
-#pragma unroll
-    for (int c = 0; c < CT; ++c) accu[c] = 0;
-    {
-        const int64_t off = D.uoff[k];
-        const int len = D.ulen[k];
-        for (int i = lane; i < len; i += 32) {
-            acc_t u;
-            if (MODE == SODAGPU_FP64) u = (acc_t)D.U64[off + i];
-            else if (MODE == SODAGPU_FP32) u = (acc_t)D.U32[off + i];
-            else u = (acc_t)(__bfloat162float(D.Uhi[off + i]) + __bfloat162float(D.Ulo[off + i]));
-#pragma unroll
-            for (int c = 0; c < CT; ++c) accu[c] += u * (acc_t)D.ra[(size_t)c * D.bs + i];
-        }
-    }
-    double xr_mine = 0.0, ur_mine = 0.0;
-#pragma unroll
-    for (int c = 0; c < CT; ++c) {
-        double a, u;
-        if (MODE == SODAGPU_FP64) {
-            a = warp_sum((double)acc[c]);
-            u = warp_sum((double)accu[c]);
-        } else {
-            a = (double)warp_sumf((float)acc[c]);
-            u = (double)warp_sumf((float)accu[c]);
-        }
-        if (lane == c) { xr_mine = a; ur_mine = u; }
-    }
-    double delta = 0.0;
-    if (lane < CT) {
-        const int c = lane;
-        double xr = xr_mine;
-        if (MODE == SODAGPU_FP8) {
-            // x_k'r = (G_k'r - 2p sum(r)) / sd = G_k'r * (1/sd) + x0 * sum(r)
-            double rs = 0.0;
-            for (int t = 0; t < D.nr_ctas; ++t) rs += D.rsum[(size_t)c * D.nr_ctas + t];
-            xr = xr * D.xv[(size_t)k * 4 + 3] + D.xv[(size_t)k * 4 + 0] * rs;
-        }
-        const ChainScal *S = &D.scal[c];
-        const double zz = D.xxd[b];
-        const double zz_vare = zz / S->vare;
-        CRng R;
-        crng_init(R, D.seed, c, rep, D.perm[k], P_SNP);
-        int err = 0;
-        delta = draw_snp(D, S, c, rep, D.perm[k], xr + ur_mine, zz, zz_vare, R, &err);
-        if (err) flag_err(D, 1);
-        D.delta[(size_t)c * D.bs + jk] = delta;
-    }
-    const unsigned nz = __ballot_sync(0xffffffffu, lane < CT && delta != 0.0);
-    if (lane == 0) D.nzflag[jk] = nz != 0u;
-}
-
-// ---------------------------------------------------------------------------
-// residual update r += X_b delta (rows) and ra += U_b delta (augmented rows),
-// columns in subset order for every element (models.f90:164-174).
-// ---------------------------------------------------------------------------
-constexpr int UPD_CHUNK = 32;
+constexpr int UPD_CHUNK = 64;
 
 static inline size_t update_smem_bytes(int bs) { return sizeof(int) * ((size_t)bs + 32); }
 
 template <int MODE, int CT>
-__global__ void __launch_bounds__(ROW_THREADS) k_update(Dev D, int b)
+__global__ void __launch_bounds__(ROW_THREADS, 1) k_update(Dev D, int b, int nsplit)
 {
+    typedef typename std::conditional<MODE == SODAGPU_FP64, double, float>::type acc_t;
     extern __shared__ int s_list[];  // bs + 32 ints
     __shared__ int s_wcnt[ROW_THREADS / 32 + 1];
-    __shared__ int s_n;
-    __shared__ double s_xv[UPD_CHUNK][3];
-    __shared__ double s_dl[UPD_CHUNK][CT];
+    __shared__ int s_n, s_last;
+    __shared__ acc_t s_xv[UPD_CHUNK][3];
+    __shared__ acc_t s_dl[UPD_CHUNK][CT];
     __shared__ int64_t s_off[UPD_CHUNK];
     __shared__ int s_len[UPD_CHUNK];
     __shared__ double sh[33];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
-    // compact the positions with a non-zero delta in any chain, in order
+    // positions with a non-zero delta in any chain, in subset order
     if (tid == 0) s_n = 0;
     __syncthreads();
     for (int base = 0; base < N; base += ROW_THREADS) {
@@ -374,68 +270,121 @@ __global__ void __launch_bounds__(ROW_THREADS) k_update(Dev D, int b)
         __syncthreads();
     }
     const int nlist = s_n;
-    if (nlist == 0) return;
-    const bool rows = blockIdx.x < D.nr_ctas;
-    const int i = (rows ? blockIdx.x : blockIdx.x - D.nr_ctas) * ROW_THREADS + tid;
-    const bool active = rows ? i < D.n : i < D.bs;
-    double acc[CT];
+    if (nlist == 0) return;   // nothing changed: r, r32 and rsum stay valid
+    const int ntile_r = D.nr_ctas;
+    const int tile = blockIdx.x / nsplit, split = blockIdx.x % nsplit;
+    const bool rows = tile < ntile_r;
+    const int t0 = (rows ? tile : tile - ntile_r) * ROW_TILE;
+    const int nrow = rows ? D.n : D.bs;
+    const int i0 = t0 + tid * ROWS_PER_THREAD;     // 4 consecutive rows per thread
+    const int q0 = (int)(((long long)nlist * split) / nsplit);
+    const int q1 = (int)(((long long)nlist * (split + 1)) / nsplit);
+    acc_t acc[ROWS_PER_THREAD][CT];
 #pragma unroll
-    for (int c = 0; c < CT; ++c)
-        acc[c] = active ? (rows ? D.r[(size_t)c * D.ldr + i] : D.ra[(size_t)c * D.bs + i]) : 0.0;
-    for (int base = 0; base < nlist; base += UPD_CHUNK) {
-        const int cnt = min(UPD_CHUNK, nlist - base);
+    for (int e = 0; e < ROWS_PER_THREAD; ++e)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[e][c] = 0;
+    for (int base = q0; base < q1; base += UPD_CHUNK) {
+        const int cnt = min(UPD_CHUNK, q1 - base);
         __syncthreads();
         for (int t = tid; t < cnt * CT; t += ROW_THREADS) {
             const int q = t / CT, c = t % CT;
-            s_dl[q][c] = D.delta[(size_t)c * D.bs + s_list[base + q]];
+            s_dl[q][c] = (acc_t)D.delta[(size_t)c * D.bs + s_list[base + q]];
         }
         if (tid < cnt) {
             const int k = ls + s_list[base + tid];
-            s_xv[tid][0] = D.xv[(size_t)k * 4 + 0];
-            s_xv[tid][1] = D.xv[(size_t)k * 4 + 1];
-            s_xv[tid][2] = D.xv[(size_t)k * 4 + 2];
+            s_xv[tid][0] = (acc_t)D.xv[(size_t)k * 4 + 0];
+            s_xv[tid][1] = (acc_t)D.xv[(size_t)k * 4 + 1];
+            s_xv[tid][2] = (acc_t)D.xv[(size_t)k * 4 + 2];
             s_off[tid] = D.uoff[k];
             s_len[tid] = D.ulen[k];
         }
         __syncthreads();
-        if (!active) continue;
+        if (i0 >= nrow) continue;
+#pragma unroll 4
         for (int q = 0; q < cnt; ++q) {
-            const int k = ls + s_list[base + q];
-            double x;
+            acc_t x[ROWS_PER_THREAD];
             if (rows) {
+                const int k = ls + s_list[base + q];
                 if (MODE == SODAGPU_FP32) {
-                    x = (double)D.X32[(size_t)k * D.ldx + i];
+                    const float4 xx = *reinterpret_cast<const float4 *>(D.X32 + (size_t)k * D.ldx + i0);
+                    x[0] = xx.x; x[1] = xx.y; x[2] = xx.z; x[3] = xx.w;
                 } else {
-                    const int code = D.G[(size_t)k * D.ldx + i];
-                    x = s_xv[q][code];
+                    const uint32_t wv = *reinterpret_cast<const uint32_t *>(D.G + (size_t)k * D.ldx + i0);
+#pragma unroll
+                    for (int e = 0; e < ROWS_PER_THREAD; ++e) x[e] = s_xv[q][(wv >> (8 * e)) & 3];
                 }
             } else {
-                if (i >= s_len[q]) continue;
-                const int64_t o = s_off[q] + i;
-                if (MODE == SODAGPU_FP64) x = D.U64[o];
-                else if (MODE == SODAGPU_FP32) x = (double)D.U32[o];
-                else x = (double)__bfloat162float(D.Uhi[o]) + (double)__bfloat162float(D.Ulo[o]);
+                const int len = s_len[q];
+                const int64_t o = s_off[q] + i0;
+#pragma unroll
+                for (int e = 0; e < ROWS_PER_THREAD; ++e) {
+                    acc_t u = 0;
+                    if (i0 + e < len) {
+                        if (MODE == SODAGPU_FP64) u = (acc_t)D.U64[o + e];
+                        else if (MODE == SODAGPU_FP32) u = (acc_t)D.U32[o + e];
+                        else u = (acc_t)(__bfloat162float(D.Uhi[o + e]) + __bfloat162float(D.Ulo[o + e]));
+                    }
+                    x[e] = u;
+                }
             }
 #pragma unroll
-            for (int c = 0; c < CT; ++c) acc[c] = acc[c] + x * s_dl[q][c];
+            for (int e = 0; e < ROWS_PER_THREAD; ++e)
+#pragma unroll
+                for (int c = 0; c < CT; ++c) acc[e][c] += x[e] * s_dl[q][c];
         }
     }
-    if (active) {
+    // publish this split's partial sums, then the last CTA of the tile reduces
+    double *part = D.upart + (size_t)tile * nsplit * CT * ROW_TILE;
+    if (i0 < nrow) {
+#pragma unroll
+        for (int c = 0; c < CT; ++c)
+#pragma unroll
+            for (int e = 0; e < ROWS_PER_THREAD; ++e)
+                part[((size_t)split * CT + c) * ROW_TILE + tid * ROWS_PER_THREAD + e] = (double)acc[e][c];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        const int prev = atomicAdd(&D.ucount[tile], 1);
+        s_last = prev == nsplit - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double rsum_c[CT];
+#pragma unroll
+    for (int c = 0; c < CT; ++c) rsum_c[c] = 0.0;
+    if (i0 < nrow) {
 #pragma unroll
         for (int c = 0; c < CT; ++c) {
-            if (rows) {
-                D.r[(size_t)c * D.ldr + i] = acc[c];
-                D.r32[(size_t)c * D.ldr + i] = (float)acc[c];
-            } else {
-                D.ra[(size_t)c * D.bs + i] = acc[c];
+#pragma unroll
+            for (int e = 0; e < ROWS_PER_THREAD; ++e) {
+                const int i = i0 + e;
+                if (i >= nrow) continue;
+                double d = 0.0;
+                for (int sp = 0; sp < nsplit; ++sp)
+                    d += __ldcg(part + ((size_t)sp * CT + c) * ROW_TILE + tid * ROWS_PER_THREAD + e);
+                if (rows) {
+                    const size_t o = (size_t)c * D.ldr + i;
+                    const double v = D.r[o] + d;
+                    D.r[o] = v;
+                    D.r32[o] = (float)v;
+                    rsum_c[c] += v;
+                } else {
+                    const size_t o = (size_t)c * D.bs + i;
+                    D.ra[o] = D.ra[o] + d;
+                }
             }
         }
     }
+    if (tid == 0) D.ucount[tile] = 0;   // ready for the next subset
     if (MODE == SODAGPU_FP8 && rows) {
+        // refresh this tile's partial sum of r; rows outside the tile keep theirs
 #pragma unroll
         for (int c = 0; c < CT; ++c) {
-            const double t = block_sum(active ? acc[c] : 0.0, sh);
-            if (tid == 0) D.rsum[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+            const double t = block_sum(rsum_c[c], sh);
+            if (tid == 0) D.rsum[(size_t)c * D.nr_ctas + tile] = t;
         }
     }
 }
@@ -585,9 +534,15 @@ __global__ void __launch_bounds__(256) k_stats(Dev D)
         }
     } else {
         const int rb = blockIdx.x - NSTAT;
-        const int i = rb * 256 + threadIdx.x;
-        const double v = i < D.n ? D.r[(size_t)c * D.ldr + i] : 0.0;
-        const double t = block_sum(v * v, sh);
+        double v2 = 0.0;
+        for (int q = 0; q < ROWS_PER_THREAD; ++q) {
+            const int i = rb * ROW_TILE + q * 256 + threadIdx.x;
+            if (i < D.n) {
+                const double v = D.r[(size_t)c * D.ldr + i];
+                v2 += v * v;
+            }
+        }
+        const double t = block_sum(v2, sh);
         if (threadIdx.x == 0) D.rpart[(size_t)c * D.nr_ctas + rb] = t;
     }
 }
@@ -607,7 +562,8 @@ __global__ void __launch_bounds__(128) k_hyper(Dev D)
             cnt += D.cntpart[o];
         }
         S->varindist[e] = v;
-        S->snpindist[e] = cnt;
+        // BayesA tracks no class counts (models.f90:194): its trace shows none
+        S->snpindist[e] = m == SODAGPU_BAYES_A ? 0 : cnt;
     }
     __syncthreads();
     int err = 0;
@@ -871,25 +827,54 @@ __global__ void __launch_bounds__(256) k_init_snp(Dev D)
 // ---------------------------------------------------------------------------
 // host-side launch helpers
 // ---------------------------------------------------------------------------
+struct ProfScope {
+    ProfHook *h;
+    cudaStream_t st;
+    int slot;
+    ProfScope(ProfHook *h_, cudaStream_t st_, int cls) : h(h_), st(st_), slot(-1)
+    {
+        if (h && h->n < h->cap) {
+            slot = h->n++;
+            h->cls[slot] = cls;
+            cudaEventRecord(h->ev[2 * slot], st);
+        }
+    }
+    ~ProfScope()
+    {
+        if (slot >= 0) cudaEventRecord(h->ev[2 * slot + 1], st);
+    }
+};
+
 template <int MODE, int CT>
-static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int wpc, cudaStream_t st)
+static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count, cudaStream_t st, ProfHook *prof)
 {
-    const int grid1 = (nblk_snps + wpc - 1) / wpc;
-    k_rhs_draw<MODE, CT><<<grid1, 32 * wpc, 0, st>>>(D, b, wpc);
-    const int grid2 = D.nr_ctas + (D.bs + ROW_THREADS - 1) / ROW_THREADS;
-    k_update<MODE, CT><<<grid2, ROW_THREADS, update_smem_bytes(D.bs), st>>>(D, b);
+    constexpr int MTS = 8 * SptOf<CT>::v;
+    const int mtiles = (nblk_snps + MTS - 1) / MTS;
+    const int nst = (D.ldx + RhsCfg<MODE>::KST - 1) / RhsCfg<MODE>::KST;
+    int ks = (2 * sm_count + mtiles - 1) / mtiles;
+    ks = ks < 1 ? 1 : (ks > RHS_KSPLIT_MAX ? RHS_KSPLIT_MAX : ks);
+    ks = ks > nst ? nst : ks;
+    {
+        ProfScope ps(prof, st, PROF_RHS);
+        k_rhs<MODE, CT><<<mtiles * ks, 256, rhs_smem_bytes<MODE, CT>(), st>>>(D, b, ks);
+    }
+    const int ntile = D.nr_ctas + (D.bs + ROW_TILE - 1) / ROW_TILE;
+    {
+        ProfScope ps(prof, st, PROF_UPDATE);
+        k_update<MODE, CT><<<ntile * D.nsplit, ROW_THREADS, update_smem_bytes(D.bs), st>>>(D, b, D.nsplit);
+    }
     return cudaGetLastError();
 }
 
 template <int MODE>
-static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int wpc, cudaStream_t st)
+static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int sm_count, cudaStream_t st, ProfHook *prof)
 {
     switch (D.chains) {
-    case 1: return launch_block<MODE, 1>(D, b, nsnp, wpc, st);
-    case 2: return launch_block<MODE, 2>(D, b, nsnp, wpc, st);
-    case 4: return launch_block<MODE, 4>(D, b, nsnp, wpc, st);
-    case 8: return launch_block<MODE, 8>(D, b, nsnp, wpc, st);
-    case 16: return launch_block<MODE, 16>(D, b, nsnp, wpc, st);
+    case 1: return launch_block<MODE, 1>(D, b, nsnp, sm_count, st, prof);
+    case 2: return launch_block<MODE, 2>(D, b, nsnp, sm_count, st, prof);
+    case 4: return launch_block<MODE, 4>(D, b, nsnp, sm_count, st, prof);
+    case 8: return launch_block<MODE, 8>(D, b, nsnp, sm_count, st, prof);
+    case 16: return launch_block<MODE, 16>(D, b, nsnp, sm_count, st, prof);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -908,42 +893,68 @@ static cudaError_t set_update_smem_mode(size_t bytes)
     return e;
 }
 
-// Raises the dynamic shared-memory limit of the update kernels for large subsets.
+template <int MODE, int CT>
+static cudaError_t set_rhs_smem()
+{
+    return cudaFuncSetAttribute(k_rhs<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)rhs_smem_bytes<MODE, CT>());
+}
+
+template <int MODE>
+static cudaError_t set_rhs_smem_mode()
+{
+    cudaError_t e = set_rhs_smem<MODE, 1>();
+    if (e == cudaSuccess) e = set_rhs_smem<MODE, 2>();
+    if (e == cudaSuccess) e = set_rhs_smem<MODE, 4>();
+    if (e == cudaSuccess) e = set_rhs_smem<MODE, 8>();
+    if (e == cudaSuccess) e = set_rhs_smem<MODE, 16>();
+    return e;
+}
+
+// Raises the dynamic shared-memory limits of the rhs and update kernels.
 cudaError_t sweep_prepare(int bs)
 {
+    cudaError_t e = set_rhs_smem_mode<SODAGPU_FP64>();
+    if (e == cudaSuccess) e = set_rhs_smem_mode<SODAGPU_FP32>();
+    if (e == cudaSuccess) e = set_rhs_smem_mode<SODAGPU_FP8>();
+    if (e != cudaSuccess) return e;
     const size_t bytes = update_smem_bytes(bs);
     if (bytes <= 48 * 1024) return cudaSuccess;
     if (bytes > 200 * 1024) return cudaErrorInvalidValue;
-    cudaError_t e = set_update_smem_mode<SODAGPU_FP64>(bytes);
+    e = set_update_smem_mode<SODAGPU_FP64>(bytes);
     if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP32>(bytes);
     if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP8>(bytes);
     return e;
 }
 
-cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, cudaStream_t st)
+cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, cudaStream_t st,
+                                    ProfHook *prof)
 {
     const int C = D.chains;
-    k_iter_begin<<<1, 1, 0, st>>>(D);
-    k_mu_partial<<<dim3(D.nr_ctas, C), ROW_THREADS, 0, st>>>(D);
-    k_mu_apply<<<dim3(D.nr_ctas, C), ROW_THREADS, 0, st>>>(D);
+    {
+        ProfScope ps(prof, st, PROF_MU);
+        k_iter_begin<<<1, 1, 0, st>>>(D);
+        k_mu_partial<<<dim3(D.nr_ctas, C), ROW_THREADS, 0, st>>>(D);
+        k_mu_apply<<<dim3(D.nr_ctas, C), ROW_THREADS, 0, st>>>(D);
+    }
     for (int b = 0; b < D.nb; ++b) {
         const int nsnp = blk_sizes[b];
-        // about two CTAs per SM, at most 8 warps per CTA
-        int wpc = (nsnp + 2 * sm_count - 1) / (2 * sm_count);
-        wpc = wpc < 1 ? 1 : (wpc > 8 ? 8 : wpc);
         cudaError_t e;
-        if (D.precision == SODAGPU_FP64) e = launch_block_mode<SODAGPU_FP64>(D, b, nsnp, wpc, st);
-        else if (D.precision == SODAGPU_FP32) e = launch_block_mode<SODAGPU_FP32>(D, b, nsnp, wpc, st);
-        else e = launch_block_mode<SODAGPU_FP8>(D, b, nsnp, wpc, st);
+        if (D.precision == SODAGPU_FP64) e = launch_block_mode<SODAGPU_FP64>(D, b, nsnp, sm_count, st, prof);
+        else if (D.precision == SODAGPU_FP32) e = launch_block_mode<SODAGPU_FP32>(D, b, nsnp, sm_count, st, prof);
+        else e = launch_block_mode<SODAGPU_FP8>(D, b, nsnp, sm_count, st, prof);
         if (e != cudaSuccess) return e;
     }
-    if (D.nskipped > 0) k_skipped<<<C, 1024, 0, st>>>(D);
-    k_stats<<<dim3(NSTAT + D.nr_ctas, C), 256, 0, st>>>(D);
-    k_hyper<<<C, 128, 0, st>>>(D);
-    const int pgrid = (D.p + 255) / 256 < 4 * sm_count ? (D.p + 255) / 256 : 4 * sm_count;
-    k_post<<<dim3(pgrid > 0 ? pgrid : 1, C), 256, 0, st>>>(D);
-    k_recal_partial<<<dim3((D.n + 255) / 256, RECAL_SPLIT, C), 256, 0, st>>>(D, 0);
-    k_recal_apply<<<dim3((D.n + 255) / 256, C), 256, 0, st>>>(D, 0, -1);
+    {
+        ProfScope ps(prof, st, PROF_OTHER);
+        if (D.nskipped > 0) k_skipped<<<C, 1024, 0, st>>>(D);
+        k_stats<<<dim3(NSTAT + D.nr_ctas, C), 256, 0, st>>>(D);
+        k_hyper<<<C, 128, 0, st>>>(D);
+        const int pgrid = (D.p + 255) / 256 < 4 * sm_count ? (D.p + 255) / 256 : 4 * sm_count;
+        k_post<<<dim3(pgrid > 0 ? pgrid : 1, C), 256, 0, st>>>(D);
+        k_recal_partial<<<dim3((D.n + 255) / 256, RECAL_SPLIT, C), 256, 0, st>>>(D, 0);
+        k_recal_apply<<<dim3((D.n + 255) / 256, C), 256, 0, st>>>(D, 0, -1);
+    }
     return cudaGetLastError();
 }
 

@@ -7,8 +7,20 @@ namespace soda {
 
 int sweep_chain_count_supported(int chains);
 cudaError_t sweep_prepare(int bs);
-// Enqueues one Gibbs iteration of every chain on `st` (graph-capturable).
-cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, cudaStream_t st);
+// Optional per-launch event recording (eager profiling, never inside a graph):
+// before/after every launch an event pair is recorded and its kernel class
+// stored.  Classes: 0 rhs+draw, 1 residual update, 2 mu, 3 everything else.
+enum { PROF_RHS = 0, PROF_UPDATE = 1, PROF_MU = 2, PROF_OTHER = 3, PROF_NCLASS = 4 };
+struct ProfHook {
+    cudaEvent_t *ev;   // 2 * cap events
+    int *cls;          // cap classes
+    int n, cap;
+};
+
+// Enqueues one Gibbs iteration of every chain on `st` (graph-capturable when
+// prof == nullptr).
+cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, cudaStream_t st,
+                                    ProfHook *prof = nullptr);
 cudaError_t sweep_enqueue_init(const Dev &D, double vara0, double scale_va0, int sm_count, cudaStream_t st);
 cudaError_t sweep_enqueue_recal(const Dev &D, double unused, cudaStream_t st);
 

@@ -610,7 +610,8 @@ __global__ void __launch_bounds__(1024) k_psd_block(double *Wb, double *M, int N
             ulen[ls + jj] = (j + 1) > jj_stale ? (j + 1) : jj_stale;
             skip[ls + jj] = 0;
         } else {
-            ulen[ls + jj] = 0;
+            // skipped column: XA keeps the rows of the unpivoted attempt
+            ulen[ls + jj] = jj_stale;
             skip[ls + jj] = 1;
         }
     }

@@ -108,3 +108,66 @@ CONFIGS = {
     "c3": SynthSpec(n=20000, p=500000, maf_lo=0.01, maf_hi=0.5, ld_block=50, rho=0.7, ncausal=2000, h2=0.5,
                     seed=20260003),
 }
+
+
+def make_device(spec: SynthSpec, device="cuda"):
+    """The same generator on the GPU with torch, for the full-size workloads.
+
+    Returns (codes, y, b): codes is an int8 torch tensor of shape (p, n) on
+    `device` — SNP-major, i.e. the column-major (n, p) matrix the C ABI takes
+    as SODAGPU_GENO_CODES — y and b are numpy arrays.  The random streams
+    differ from make(); the distributions are the same."""
+    import torch
+
+    n, p = spec.n, spec.p
+    gen = torch.Generator(device=device)
+    gen.manual_seed(spec.seed)
+    maf = torch.rand(p, generator=gen, device=device, dtype=torch.float64) * (spec.maf_hi - spec.maf_lo) + spec.maf_lo
+    codes = torch.empty((p, n), dtype=torch.int8, device=device)
+    if spec.ld_block <= 1 or spec.rho == 0.0:
+        for j0 in range(0, p, 2048):
+            j1 = min(p, j0 + 2048)
+            u = torch.rand((j1 - j0, n, 2), generator=gen, device=device, dtype=torch.float32)
+            codes[j0:j1] = (u < maf[j0:j1, None, None].float()).sum(dim=2).to(torch.int8)
+    else:
+        L = spec.ld_block
+        nfull = p // L
+        thr = torch.special.ndtri(maf).float()
+        s = float(np.sqrt(1.0 - spec.rho * spec.rho))
+        chunk = max(1, (1 << 27) // max(n, 1))      # LD blocks per pass (~128M latent values)
+        for b0 in range(0, nfull, chunk):
+            b1 = min(nfull, b0 + chunk)
+            view = codes[b0 * L:b1 * L].view(b1 - b0, L, n)
+            acc = torch.zeros((b1 - b0, L, n), dtype=torch.int8, device=device)
+            for _h in range(2):
+                z = torch.randn((b1 - b0, n), generator=gen, device=device)
+                for t in range(L):
+                    if t:
+                        z = spec.rho * z + s * torch.randn((b1 - b0, n), generator=gen, device=device)
+                    acc[:, t, :] += (z < thr[b0 * L + t:b1 * L:L, None]).to(torch.int8)
+            view.copy_(acc)
+        if nfull * L < p:   # ragged tail: independent SNPs
+            j0 = nfull * L
+            u = torch.rand((p - j0, n, 2), generator=gen, device=device)
+            codes[j0:] = (u < maf[j0:, None, None].float()).sum(dim=2).to(torch.int8)
+    # phenotype
+    rng = np.random.default_rng(spec.seed + 1)
+    b = np.zeros(p)
+    k = min(spec.ncausal, p)
+    pos = np.sort(rng.choice(p, size=k, replace=False))
+    if spec.mixture:
+        var = np.asarray(spec.mixture, dtype=np.float64)
+        cls = rng.integers(0, len(var), size=k)
+        b[pos] = rng.standard_normal(k) * np.sqrt(var[cls])
+    else:
+        b[pos] = rng.standard_normal(k)
+    cols = codes[torch.as_tensor(pos, device=device)].double()             # (k, n)
+    f = cols.sum(dim=1) / (2.0 * n)
+    ok = (f > 0) & (f < 1)
+    sd = torch.where(ok, torch.sqrt(2.0 * f * (1.0 - f)), torch.ones_like(f))
+    X = torch.where(ok[:, None], (cols - 2.0 * f[:, None]) / sd[:, None], torch.zeros_like(cols))
+    g = (X.T @ torch.as_tensor(b[pos], device=device)).cpu().numpy()
+    vg = g.var()
+    ve = vg * (1.0 - spec.h2) / spec.h2 if vg > 0 else 1.0
+    y = spec.mean + g + rng.standard_normal(n) * np.sqrt(ve)
+    return codes, y, b
