@@ -213,6 +213,30 @@ int sodagpu_timings(sodagpu_ctx *ctx, double *build_z_s, double *run_s, double *
 #define SODAGPU_NPROF 4
 int sodagpu_profile_kernels(sodagpu_ctx *ctx, int32_t iters, double *ms, int32_t *launches);
 
+/* Genomic values pred = mu + X*effects for callers that cannot let this
+ * library allocate device memory (a host that owns the GPU through its own
+ * memory pool, or a latency-bound loop that must avoid cudaMalloc/cudaFree).
+ * No counterpart in the reference: it computes what compute_dgv does
+ * (utilities.f90:616-622) but allocates nothing, device or host.
+ *   codes   device, int8 0/1/2, column-major nind x nloci with leading dim ldg
+ *   freq    device, nloci allele frequencies (xscale centring, 0 if monomorphic)
+ *   effects device, nloci; pred device, nind (written)
+ *   stream  a cudaStream_t, or NULL for the default stream; the call only
+ *           enqueues work there, results are ready when the stream is.
+ * Scratch is one fixed array of SODAGPU_NOALLOC_SCRATCH doubles (16 MiB) in
+ * the library's device memory, held by every GPU that loads the library until
+ * the process exits; nind may not exceed SODAGPU_NOALLOC_SCRATCH
+ * (SODAGPU_E_ARG otherwise).  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress, with that device current), so
+ * make that first call before any stream capture.  All calls share the array
+ * and leave their partial sums in it: calls that overlap on the GPU race and
+ * must be serialised by the caller.  Errors are reported by the return code
+ * only (sodagpu_last_error is not updated). */
+#define SODAGPU_NOALLOC_SCRATCH (2 * 1024 * 1024)
+int sodagpu_compute_dgv_noalloc(int32_t nind, int32_t nloci, const int8_t *codes, int32_t ldg,
+                                const double *freq, double mu, const double *effects, double *pred,
+                                void *stream);
+
 void sodagpu_destroy(sodagpu_ctx *ctx);
 const char *sodagpu_errstr(int code);
 const char *sodagpu_last_error(void);

@@ -65,6 +65,7 @@ PROTOTYPES = {
     "sodagpu_predict": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int32, _DP, C.c_double, _DP, _DP]),
     "sodagpu_timings": (C.c_int, [_P, _DP, _DP, _DP]),
     "sodagpu_profile_kernels": (C.c_int, [_P, C.c_int32, _DP, _IP]),
+    "sodagpu_compute_dgv_noalloc": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int32, _P, C.c_double, _P, _P, _P]),
     "sodagpu_destroy": (None, [_P]),
 }
 

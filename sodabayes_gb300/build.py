@@ -20,7 +20,7 @@ LIB = os.path.join(PKG, "libsodagpu.so")
 CLI = os.path.join(PKG, "sodabayes")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["api.cu", "zbuild.cu", "sweep.cu"]
+CU_SOURCES = ["api.cu", "zbuild.cu", "sweep.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:
