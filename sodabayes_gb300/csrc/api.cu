@@ -101,6 +101,9 @@ struct sodagpu_ctx {
     double *xxd = nullptr, *xpx = nullptr;
     int32_t *perm = nullptr, *pos_of = nullptr, *iskipped = nullptr, *grp = nullptr, *blk_ls = nullptr;
     uint8_t *skip = nullptr;
+    float *ra32 = nullptr, *xv32 = nullptr, *delta32 = nullptr;
+    int32_t *blk_pd = nullptr;
+    int ldra = 0;
     double *r = nullptr, *ra = nullptr, *g = nullptr, *vara_s = nullptr, *gstore = nullptr,
            *vara_sstore = nullptr;
     float *r32 = nullptr;
@@ -394,6 +397,8 @@ int sodagpu_build_z(sodagpu_ctx *c, const int32_t *permvec, int32_t *nskipped_ou
     CUDA_TRY(cudaMemcpyAsync(c->pos_of, h_pos.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, c->st));
     CUDA_TRY(zb_gather(c->Gsnp, c->G, c->perm, p, c->ldx, c->st));
     CUDA_TRY(zb_xv(c->freq, c->perm, p, c->xv, c->st));
+    TRY(c->alloc(&c->xv32, (size_t)p * 4, false));
+    CUDA_TRY(zb_xv32(c->xv, p, c->xv32, c->st));
     CUDA_TRY(cudaStreamSynchronize(c->st));
     c->release(c->Gsnp);
     c->Gsnp = nullptr;
@@ -546,20 +551,26 @@ int sodagpu_build_z(sodagpu_ctx *c, const int32_t *permvec, int32_t *nskipped_ou
     std::vector<int32_t> h_len(p);
     CUDA_TRY(cudaMemcpyAsync(h_len.data(), c->ulen, sizeof(int32_t) * p, cudaMemcpyDeviceToHost, c->st));
     CUDA_TRY(cudaStreamSynchronize(c->st));
+    // columns of subset b spaced round_up(N_b, 8) apart: every column starts
+    // 16-byte aligned (FP32) and rows ulen..N-1 stay zero
     std::vector<int64_t> h_off(p + 1);
     int64_t tot = 0;
-    for (int k = 0; k < p; ++k) {
-        h_off[k] = tot;
-        tot += h_len[k];
+    for (int b = 0; b < nb; ++b) {
+        const int N = c->blk_sizes[b];
+        const int64_t npad = (int64_t)round_up((size_t)N, 8);
+        for (int jj = 0; jj < N; ++jj) h_off[c->h_blk_ls[b] + jj] = tot + jj * npad;
+        tot += npad * N;
     }
     h_off[p] = tot;
-    CUDA_TRY(cudaMemcpyAsync(c->uoff, h_off.data(), sizeof(int64_t) * (p + 1), cudaMemcpyHostToDevice, c->st));
-    TRY(c->alloc(&c->U64, (size_t)tot, false));
-    if (c->cfg.precision == SODAGPU_FP32) TRY(c->alloc(&c->U32, (size_t)tot, false));
-    if (c->cfg.precision == SODAGPU_FP8) {
-        TRY(c->alloc(&c->Uhi, (size_t)tot, false));
-        TRY(c->alloc(&c->Ulo, (size_t)tot, false));
+    {
+        std::vector<int32_t> pd(nb);
+        for (int b = 0; b < nb; ++b) pd[b] = h_status[b] == 0;
+        TRY(c->alloc(&c->blk_pd, nb, false));
+        CUDA_TRY(cudaMemcpyAsync(c->blk_pd, pd.data(), sizeof(int32_t) * nb, cudaMemcpyHostToDevice, c->st));
     }
+    CUDA_TRY(cudaMemcpyAsync(c->uoff, h_off.data(), sizeof(int64_t) * (p + 1), cudaMemcpyHostToDevice, c->st));
+    TRY(c->alloc(&c->U64, (size_t)tot));
+    if (c->cfg.precision != SODAGPU_FP64) TRY(c->alloc(&c->U32, (size_t)tot));
     for (int b0 = 0; b0 < nb; b0 += BATCH) {
         const int nbat = std::min(BATCH, nb - b0);
         batch_ids.resize(nbat);
@@ -651,6 +662,8 @@ int build_dev(sodagpu_ctx *c)
     D.G = c->G;
     D.X32 = c->X32;
     D.xv = c->xv;
+    D.xv32 = c->xv32;
+    D.delta32 = c->delta32;
     D.y = c->y;
     D.uoff = c->uoff;
     D.ulen = c->ulen;
@@ -669,6 +682,9 @@ int build_dev(sodagpu_ctx *c)
     D.r = c->r;
     D.r32 = c->r32;
     D.ra = c->ra;
+    D.ra32 = c->ra32;
+    D.ldra = c->ldra;
+    D.blk_pd = c->blk_pd;
     D.g = c->g;
     D.cls = c->cls;
     D.vara_s = c->vara_s;
@@ -684,9 +700,6 @@ int build_dev(sodagpu_ctx *c)
     D.statpart = c->statpart;
     D.cntpart = c->cntpart;
     D.recal_part = c->recal_part;
-    D.upart = c->upart;
-    D.ucount = c->ucount;
-    D.nsplit = c->nsplit;
     D.rpx = c->rpx;
     D.rpu = c->rpu;
     D.rticket = c->rticket;
@@ -705,7 +718,9 @@ int sodagpu_init_chains(sodagpu_ctx *c)
     if (!c->r) {
         TRY(c->alloc(&c->r, (size_t)C * c->ldr));
         TRY(c->alloc(&c->r32, (size_t)C * c->ldr));
-        TRY(c->alloc(&c->ra, (size_t)C * c->bs));
+        c->ldra = (int)round_up((size_t)c->bs, 8);
+        TRY(c->alloc(&c->ra, (size_t)C * c->ldra));
+        TRY(c->alloc(&c->ra32, (size_t)C * c->ldra));
         TRY(c->alloc(&c->g, (size_t)C * p));
         TRY(c->alloc(&c->cls, (size_t)C * p));
         TRY(c->alloc(&c->vara_s, (size_t)C * p));
@@ -714,16 +729,13 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         TRY(c->alloc(&c->indist, (size_t)C * p * nm));
         TRY(c->alloc(&c->scal, C));
         TRY(c->alloc(&c->delta, (size_t)C * c->bs));
+        TRY(c->alloc(&c->delta32, (size_t)C * c->bs));
         TRY(c->alloc(&c->nzflag, c->bs));
         TRY(c->alloc(&c->rpart, (size_t)C * c->nr_ctas));
         TRY(c->alloc(&c->rsum, (size_t)C * c->nr_ctas));
         TRY(c->alloc(&c->statpart, (size_t)C * NSTAT * ngm));
         TRY(c->alloc(&c->cntpart, (size_t)C * NSTAT * ngm));
         TRY(c->alloc(&c->recal_part, (size_t)C * RECAL_SPLIT * c->ldr));
-        const int ntile = c->nr_ctas + (c->bs + ROW_TILE - 1) / ROW_TILE;
-        c->nsplit = std::max(1, std::min(16, (2 * c->sm_count + ntile - 1) / ntile));
-        TRY(c->alloc(&c->upart, (size_t)ntile * c->nsplit * C * ROW_TILE));
-        TRY(c->alloc(&c->ucount, ntile));
         TRY(c->alloc(&c->rpx, (size_t)RHS_KSPLIT_MAX * C * c->bs));
         TRY(c->alloc(&c->rpu, (size_t)RHS_KSPLIT_MAX * C * c->bs));
         TRY(c->alloc(&c->rticket, c->bs));
@@ -859,7 +871,7 @@ int sodagpu_get_state(sodagpu_ctx *c, int32_t chain, double *g, int32_t *cls, do
     if (cls) CUDA_TRY(cudaMemcpy(cls, c->cls + off, sizeof(int32_t) * p, cudaMemcpyDeviceToHost));
     if (vara_s) CUDA_TRY(cudaMemcpy(vara_s, c->vara_s + off, sizeof(double) * p, cudaMemcpyDeviceToHost));
     if (yadj) CUDA_TRY(cudaMemcpy(yadj, c->r + (size_t)chain * c->ldr, sizeof(double) * c->n, cudaMemcpyDeviceToHost));
-    if (yaadj) CUDA_TRY(cudaMemcpy(yaadj, c->ra + (size_t)chain * c->bs, sizeof(double) * c->bs, cudaMemcpyDeviceToHost));
+    if (yaadj) CUDA_TRY(cudaMemcpy(yaadj, c->ra + (size_t)chain * c->ldra, sizeof(double) * c->bs, cudaMemcpyDeviceToHost));
     if (scalars) {
         ChainScal *S = new ChainScal;
         RunCtl h{};

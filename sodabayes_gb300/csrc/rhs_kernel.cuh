@@ -3,15 +3,17 @@
 //
 //   rhs[j][c] = x_j' r_c + u_j' ra_c (+ d g_j)
 //
-// is a tall-skinny GEMM (M = subset SNPs, N = chains, K = individuals).  The
-// grid is (M tiles of 8*SPT SNPs) x (K splits): each CTA streams its genotype
-// rows and the chains' residual rows through shared memory with cp.async
-// (double-buffered), keeps an SPT x CT accumulator block per thread, and adds
-// its share of the augmenting-matrix dots.  Partial sums go to scratch; the
-// last CTA of an M tile to finish (atomic ticket, no waiting) sums them in
-// split order and performs the draws of that tile, so the draws are spread
-// over the M tiles.  FP8 mode: the codes 0/1/2 are exact in FP32, the centring
-// is applied afterwards as x'r = (G'r) / sd - 2p/sd * sum(r).
+// is a tall-skinny GEMM: M = the subset's SNPs, N = chains, K = individuals
+// followed by the augmented rows.  The grid is (M tiles of 8*SPT SNPs) x
+// (K splits), sized to one wave.  Each CTA streams its share of both K
+// ranges through shared memory in one NS-stage cp.async pipeline — genotype
+// stages (codes or FP32 columns with r) first, then augmenting-matrix stages
+// (U columns with ra; the factor is upper triangular, so a tile needs only
+// the rows up to its last column) — keeping an SPT x CT accumulator block per
+// thread.  Partial sums go to scratch; the last CTA of an M tile to finish
+// (atomic ticket, no waiting) adds them in split order and performs that
+// tile's draws.  FP8 mode: codes 0/1/2 are exact in FP32 and the centring is
+// applied once per SNP, x'r = (G'r)/sd - 2p/sd * sum(r).
 #pragma once
 #include <cuda_pipeline_primitives.h>
 
@@ -20,34 +22,51 @@ namespace soda {
 template <int MODE>
 struct RhsCfg;
 template <>
-struct RhsCfg<SODAGPU_FP8> {       // int8 codes, FP32 residual
-    static constexpr int KST = 512;            // individuals per stage
-    static constexpr int XB = 1;               // bytes per genotype element in smem
+struct RhsCfg<SODAGPU_FP8> {       // int8 codes, FP32 residual, FP32 U
+    static constexpr int KST = 512;            // genotype elements per row per stage
+    static constexpr int XB = 1;               // bytes per genotype element
     static constexpr int RB = 4;               // bytes per residual element
+    static constexpr int UB = 4;               // bytes per U / ra element
 };
 template <>
-struct RhsCfg<SODAGPU_FP32> {      // FP32 columns, FP32 residual
+struct RhsCfg<SODAGPU_FP32> {      // FP32 columns, FP32 residual, FP32 U
     static constexpr int KST = 256;
     static constexpr int XB = 4;
     static constexpr int RB = 4;
+    static constexpr int UB = 4;
 };
 template <>
-struct RhsCfg<SODAGPU_FP64> {      // int8 codes looked up as FP64, FP64 residual
+struct RhsCfg<SODAGPU_FP64> {      // int8 codes looked up as FP64, FP64 residual and U
     static constexpr int KST = 512;
     static constexpr int XB = 1;
     static constexpr int RB = 8;
+    static constexpr int UB = 8;
 };
 
 template <int CT>
 struct SptOf { static constexpr int v = CT >= 8 ? 4 : 8; };
 
-// smem bytes of k_rhs for a mode / chain count
+template <int MODE>
+constexpr int rhs_ku() { return RhsCfg<MODE>::KST * RhsCfg<MODE>::XB / RhsCfg<MODE>::UB; }   // U rows per stage
+
 template <int MODE, int CT>
-constexpr size_t rhs_smem_bytes()
+constexpr size_t rhs_xpart_bytes() { return (size_t)8 * SptOf<CT>::v * RhsCfg<MODE>::KST * RhsCfg<MODE>::XB; }
+template <int MODE, int CT>
+constexpr size_t rhs_rpart_bytes()
 {
-    return 2 * ((size_t)8 * SptOf<CT>::v * RhsCfg<MODE>::KST * RhsCfg<MODE>::XB +
-                (size_t)CT * RhsCfg<MODE>::KST * RhsCfg<MODE>::RB);
+    return (size_t)CT * (RhsCfg<MODE>::KST * RhsCfg<MODE>::RB > rhs_ku<MODE>() * RhsCfg<MODE>::UB
+                             ? RhsCfg<MODE>::KST * RhsCfg<MODE>::RB
+                             : rhs_ku<MODE>() * RhsCfg<MODE>::UB);
 }
+template <int MODE, int CT>
+constexpr size_t rhs_stage_bytes() { return rhs_xpart_bytes<MODE, CT>() + rhs_rpart_bytes<MODE, CT>(); }
+template <int MODE, int CT>
+constexpr int rhs_nstage()
+{
+    return 4 * rhs_stage_bytes<MODE, CT>() <= 200 * 1024 ? 4 : (3 * rhs_stage_bytes<MODE, CT>() <= 200 * 1024 ? 3 : 2);
+}
+template <int MODE, int CT>
+constexpr size_t rhs_smem_bytes() { return rhs_nstage<MODE, CT>() * rhs_stage_bytes<MODE, CT>(); }
 
 __device__ __forceinline__ float code_to_f32(uint32_t w, int k)
 {
@@ -62,10 +81,12 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     constexpr int SPT = SptOf<CT>::v;
     constexpr int MTS = 8 * SPT;                 // SNPs per M tile (8 warps)
     constexpr int KST = Cfg::KST;
+    constexpr int KU = rhs_ku<MODE>();
+    constexpr int NS = rhs_nstage<MODE, CT>();
+    constexpr size_t XPART = rhs_xpart_bytes<MODE, CT>();
+    constexpr size_t SBYTES = rhs_stage_bytes<MODE, CT>();
     typedef typename std::conditional<MODE == SODAGPU_FP64, double, float>::type acc_t;
     extern __shared__ __align__(16) unsigned char smem[];
-    unsigned char *sX = smem;                                        // [2][MTS][KST*XB]
-    unsigned char *sR = smem + 2 * (size_t)MTS * KST * Cfg::XB;      // [2][CT][KST*RB]
     __shared__ int s_last;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -74,47 +95,76 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     const int mt = blockIdx.x / ksplit, ks = blockIdx.x % ksplit;
     const int j0 = mt * MTS;
     if (j0 >= N) return;
-    // K range of this split, in whole stages
-    const int nst_tot = (D.ldx + KST - 1) / KST;
-    const int st0 = (int)(((long long)nst_tot * ks) / ksplit);
-    const int st1 = (int)(((long long)nst_tot * (ks + 1)) / ksplit);
+    const int npad = (N + 7) & ~7;             // spacing of the subset's U columns
+    // K ranges of this split: genotype stages, then augmenting-matrix stages
+    const int nG = (D.ldx + KST - 1) / KST;
+    const int rowsU = D.blk_pd[b] ? min(npad, j0 + MTS) : npad;   // triangular: rows up to the tile's last column
+    const int nU = (rowsU + KU - 1) / KU;
+    const int g0 = (int)(((long long)nG * ks) / ksplit), g1 = (int)(((long long)nG * (ks + 1)) / ksplit);
+    const int u0 = (int)(((long long)nU * ks) / ksplit), u1 = (int)(((long long)nU * (ks + 1)) / ksplit);
+    const int ng = g1 - g0, nv = ng + (u1 - u0);
 
-    auto issue = [&](int stage, int buf) {
-        const int k0 = stage * KST;
-        // genotype rows: MTS rows of KST*XB bytes, 16-byte chunks
-        constexpr int XCH = KST * Cfg::XB / 16;
-        unsigned char *dx = sX + (size_t)buf * MTS * KST * Cfg::XB;
-        for (int t = tid; t < MTS * XCH; t += 256) {
-            const int row = t / XCH, ch = t % XCH;
-            unsigned char *dst = dx + (size_t)row * KST * Cfg::XB + ch * 16;
-            const int jk = j0 + row;
-            const long long e0 = (long long)k0 + (long long)ch * 16 / Cfg::XB;   // first element of the chunk
-            if (jk < N && e0 + 16 / Cfg::XB <= D.ldx) {
-                const unsigned char *src;
-                if (MODE == SODAGPU_FP32)
-                    src = reinterpret_cast<const unsigned char *>(D.X32 + (size_t)(ls + jk) * D.ldx + e0);
-                else
-                    src = reinterpret_cast<const unsigned char *>(D.G + (size_t)(ls + jk) * D.ldx + e0);
-                __pipeline_memcpy_async(dst, src, 16);
-            } else {
-                *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+    auto issue = [&](int v, int buf) {
+        unsigned char *dx = smem + (size_t)buf * SBYTES;
+        unsigned char *dr = dx + XPART;
+        if (v < ng) {     // genotype stage
+            const int k0 = (g0 + v) * KST;
+            constexpr int XCH = KST * Cfg::XB / 16;
+            for (int t = tid; t < MTS * XCH; t += 256) {
+                const int row = t / XCH, ch = t % XCH;
+                unsigned char *dst = dx + (size_t)row * KST * Cfg::XB + ch * 16;
+                const int jk = j0 + row;
+                const int e0 = k0 + ch * (16 / Cfg::XB);
+                if (jk < N && e0 + 16 / Cfg::XB <= D.ldx) {
+                    const void *src = MODE == SODAGPU_FP32
+                                          ? (const void *)(D.X32 + (size_t)(ls + jk) * D.ldx + e0)
+                                          : (const void *)(D.G + (size_t)(ls + jk) * D.ldx + e0);
+                    __pipeline_memcpy_async(dst, src, 16);
+                } else {
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+                }
             }
-        }
-        constexpr int RCH = KST * Cfg::RB / 16;
-        unsigned char *dr = sR + (size_t)buf * CT * KST * Cfg::RB;
-        for (int t = tid; t < CT * RCH; t += 256) {
-            const int c = t / RCH, ch = t % RCH;
-            unsigned char *dst = dr + (size_t)c * KST * Cfg::RB + ch * 16;
-            const long long e0 = (long long)k0 + (long long)ch * 16 / Cfg::RB;
-            if (e0 + 16 / Cfg::RB <= D.ldr) {
-                const unsigned char *src;
-                if (MODE == SODAGPU_FP64)
-                    src = reinterpret_cast<const unsigned char *>(D.r + (size_t)c * D.ldr + e0);
-                else
-                    src = reinterpret_cast<const unsigned char *>(D.r32 + (size_t)c * D.ldr + e0);
-                __pipeline_memcpy_async(dst, src, 16);
-            } else {
-                *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+            constexpr int RCH = KST * Cfg::RB / 16;
+            for (int t = tid; t < CT * RCH; t += 256) {
+                const int c = t / RCH, ch = t % RCH;
+                unsigned char *dst = dr + (size_t)c * KST * Cfg::RB + ch * 16;
+                const int e0 = k0 + ch * (16 / Cfg::RB);
+                if (e0 + 16 / Cfg::RB <= D.ldr) {
+                    const void *src = MODE == SODAGPU_FP64 ? (const void *)(D.r + (size_t)c * D.ldr + e0)
+                                                           : (const void *)(D.r32 + (size_t)c * D.ldr + e0);
+                    __pipeline_memcpy_async(dst, src, 16);
+                } else {
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+                }
+            }
+        } else {          // augmenting-matrix stage: rows [i0, i0+KU) of the tile's U columns
+            const int i0 = (u0 + v - ng) * KU;
+            constexpr int UCH = KU * Cfg::UB / 16;
+            for (int t = tid; t < MTS * UCH; t += 256) {
+                const int row = t / UCH, ch = t % UCH;
+                unsigned char *dst = dx + (size_t)row * KU * Cfg::UB + ch * 16;
+                const int jk = j0 + row;
+                const int e0 = i0 + ch * (16 / Cfg::UB);
+                if (jk < N && e0 + 16 / Cfg::UB <= npad) {
+                    const int64_t off = D.uoff[ls + jk] + e0;
+                    const void *src = MODE == SODAGPU_FP64 ? (const void *)(D.U64 + off) : (const void *)(D.U32 + off);
+                    __pipeline_memcpy_async(dst, src, 16);
+                } else {
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+                }
+            }
+            constexpr int RCH = KU * Cfg::UB / 16;
+            for (int t = tid; t < CT * RCH; t += 256) {
+                const int c = t / RCH, ch = t % RCH;
+                unsigned char *dst = dr + (size_t)c * KU * Cfg::UB + ch * 16;
+                const int e0 = i0 + ch * (16 / Cfg::UB);
+                if (e0 + 16 / Cfg::UB <= D.ldra) {
+                    const void *src = MODE == SODAGPU_FP64 ? (const void *)(D.ra + (size_t)c * D.ldra + e0)
+                                                           : (const void *)(D.ra32 + (size_t)c * D.ldra + e0);
+                    __pipeline_memcpy_async(dst, src, 16);
+                } else {
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+                }
             }
         }
         __pipeline_commit();
@@ -136,22 +186,41 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
             xl[s][2] = D.xv[(size_t)k * 4 + 2];
         }
     }
-
-    if (st0 < st1) issue(st0, 0);
-    for (int st = st0; st < st1; ++st) {
-        const int buf = (st - st0) & 1;
-        if (st + 1 < st1) {
-            issue(st + 1, buf ^ 1);
-            __pipeline_wait_prior(1);
-        } else {
-            __pipeline_wait_prior(0);
+    // publishes the accumulators as this split's genotype (is_u = false) or
+    // augmenting (is_u = true) partial sums and clears them
+    auto publish = [&](bool is_u) {
+        double *dstp = is_u ? D.rpu : D.rpx;
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) {
+            const int jk = j0 + warp * SPT + s;
+#pragma unroll
+            for (int c = 0; c < CT; ++c) {
+                const double a = MODE == SODAGPU_FP64 ? warp_sum((double)acc[s][c]) : (double)warp_sumf((float)acc[s][c]);
+                if (lane == 0 && jk < N) dstp[((size_t)ks * CT + c) * D.bs + jk] = a;
+                acc[s][c] = 0;
+            }
         }
+    };
+
+#pragma unroll
+    for (int pp = 0; pp < NS - 1; ++pp) {
+        if (pp < nv) issue(pp, pp);
+        else __pipeline_commit();
+    }
+    for (int v = 0; v < nv; ++v) {
+        const int buf = v % NS;
+        // the buffer of stage v+NS-1 was last read in iteration v-1, which
+        // ended with a barrier: refill it before waiting for stage v
+        if (v + NS - 1 < nv) issue(v + NS - 1, (v + NS - 1) % NS);
+        else __pipeline_commit();
+        __pipeline_wait_prior(NS - 1);
         __syncthreads();
-        const unsigned char *bx = sX + (size_t)buf * MTS * KST * Cfg::XB;
-        const unsigned char *br = sR + (size_t)buf * CT * KST * Cfg::RB;
-        if (MODE == SODAGPU_FP8) {
-            // lane covers individuals q*128 + 4*lane + {0..3}, q = 0..3:
-            // genotype words and residual float4s are contiguous across lanes
+        if (v == ng) publish(false);
+        const unsigned char *bx = smem + (size_t)buf * SBYTES;
+        const unsigned char *br = bx + XPART;
+        if (v < ng && MODE == SODAGPU_FP8) {
+            // lane covers individuals q*128 + 4*lane + {0..3}: genotype words
+            // and residual float4s are contiguous across lanes
 #pragma unroll
             for (int q = 0; q < KST / 128; ++q) {
                 float x[SPT][4];
@@ -176,16 +245,19 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
                     }
                 }
             }
-        } else if (MODE == SODAGPU_FP32) {
+        } else if (MODE != SODAGPU_FP64) {
+            // FP32 columns (FP32 mode genotype stages) or FP32 U columns (both modes)
+            constexpr int KF = KST * Cfg::XB / 4;    // floats per row of the stage
+            const int rstride = v < ng ? KST : KU;
 #pragma unroll
-            for (int q = 0; q < KST / 128; ++q) {
+            for (int q = 0; q < KF / 128; ++q) {
                 float4 xx[SPT];
 #pragma unroll
                 for (int s = 0; s < SPT; ++s)
-                    xx[s] = *reinterpret_cast<const float4 *>(bx + ((size_t)(warp * SPT + s) * KST + q * 128 + lane * 4) * 4);
+                    xx[s] = *reinterpret_cast<const float4 *>(bx + ((size_t)(warp * SPT + s) * KF + q * 128 + lane * 4) * 4);
 #pragma unroll
                 for (int c = 0; c < CT; ++c) {
-                    const float4 rr = *reinterpret_cast<const float4 *>(br + ((size_t)c * KST + q * 128 + lane * 4) * 4);
+                    const float4 rr = *reinterpret_cast<const float4 *>(br + ((size_t)c * rstride + q * 128 + lane * 4) * 4);
 #pragma unroll
                     for (int s = 0; s < SPT; ++s) {
                         acc[s][c] = fmaf(xx[s].x, rr.x, acc[s][c]);
@@ -195,7 +267,7 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
                     }
                 }
             }
-        } else {   // FP64: codes looked up in the column's exact x values
+        } else if (v < ng) {   // FP64 genotype stage: codes looked up in the column's exact x values
 #pragma unroll 4
             for (int q = 0; q < KST / 32; ++q) {
                 const int idx = q * 32 + lane;
@@ -212,50 +284,28 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
                     for (int s = 0; s < SPT; ++s) acc[s][c] = fma(x[s], rv, acc[s][c]);
                 }
             }
+        } else {               // FP64 augmenting stage
+#pragma unroll
+            for (int q = 0; q < KU / 32; ++q) {
+                const int idx = q * 32 + lane;
+                double x[SPT];
+#pragma unroll
+                for (int s = 0; s < SPT; ++s)
+                    x[s] = *reinterpret_cast<const double *>(bx + ((size_t)(warp * SPT + s) * KU + idx) * 8);
+#pragma unroll
+                for (int c = 0; c < CT; ++c) {
+                    const double rv = *reinterpret_cast<const double *>(br + ((size_t)c * KU + idx) * 8);
+#pragma unroll
+                    for (int s = 0; s < SPT; ++s) acc[s][c] = fma(x[s], rv, acc[s][c]);
+                }
+            }
         }
         __syncthreads();
     }
+    __pipeline_wait_prior(0);
+    if (nv == ng) publish(false);   // no augmenting stage in this split
+    publish(true);
 
-    // publish this split's genotype partial sums
-#pragma unroll
-    for (int s = 0; s < SPT; ++s) {
-        const int jk = j0 + warp * SPT + s;
-#pragma unroll
-        for (int c = 0; c < CT; ++c) {
-            const double a = MODE == SODAGPU_FP64 ? warp_sum((double)acc[s][c]) : (double)warp_sumf((float)acc[s][c]);
-            if (lane == 0 && jk < N) D.rpx[((size_t)ks * CT + c) * D.bs + jk] = a;
-        }
-    }
-    // augmenting-matrix share: rows [ks*RS, (ks+1)*RS) of each column
-    {
-        const int RS = (D.bs + ksplit - 1) / ksplit;
-        const int r0 = ks * RS, r1 = min(D.bs, r0 + RS);
-#pragma unroll
-        for (int s = 0; s < SPT; ++s) {
-            const int jk = j0 + warp * SPT + s;
-            acc_t accu[CT];
-#pragma unroll
-            for (int c = 0; c < CT; ++c) accu[c] = 0;
-            if (jk < N) {
-                const int k = ls + jk;
-                const int64_t off = D.uoff[k];
-                const int len = min(D.ulen[k], r1);
-                for (int i = r0 + lane; i < len; i += 32) {
-                    acc_t u;
-                    if (MODE == SODAGPU_FP64) u = (acc_t)D.U64[off + i];
-                    else if (MODE == SODAGPU_FP32) u = (acc_t)D.U32[off + i];
-                    else u = (acc_t)(__bfloat162float(D.Uhi[off + i]) + __bfloat162float(D.Ulo[off + i]));
-#pragma unroll
-                    for (int c = 0; c < CT; ++c) accu[c] += u * (acc_t)D.ra[(size_t)c * D.bs + i];
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < CT; ++c) {
-                const double u = MODE == SODAGPU_FP64 ? warp_sum((double)accu[c]) : (double)warp_sumf((float)accu[c]);
-                if (lane == 0 && jk < N) D.rpu[((size_t)ks * CT + c) * D.bs + jk] = u;
-            }
-        }
-    }
     __threadfence();
     __syncthreads();
     if (tid == 0) s_last = atomicAdd(&D.rticket[mt], 1) == ksplit - 1;
@@ -266,6 +316,15 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     const int rep = cur_rep(D);
     const double zz = D.xxd[b];
     const int cnt = min(MTS, N - j0);
+    __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring), once per CTA
+    if (MODE == SODAGPU_FP8) {
+        if (tid < CT) {
+            double rs = 0.0;
+            for (int q = 0; q < D.nr_ctas; ++q) rs += D.rsum[(size_t)tid * D.nr_ctas + q];
+            s_rs[tid] = rs;
+        }
+        __syncthreads();
+    }
     for (int t = tid; t < ((cnt * CT + 31) & ~31); t += 256) {
         const int jl = t / CT, c = t % CT;
         const int jk = j0 + jl;
@@ -273,28 +332,27 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
         double delta = 0.0;
         if (act) {
             const int k = ls + jk;
-            if (D.skip[k]) {
-                delta = 0.0;
-            } else {
+            if (!D.skip[k]) {
                 double xr = 0.0, ur = 0.0;
                 for (int sp = 0; sp < ksplit; ++sp) {
                     const size_t o = ((size_t)sp * CT + c) * D.bs + jk;
                     xr += __ldcg(D.rpx + o);
                     ur += __ldcg(D.rpu + o);
                 }
-                if (MODE == SODAGPU_FP8) {
-                    double rs = 0.0;
-                    for (int q = 0; q < D.nr_ctas; ++q) rs += D.rsum[(size_t)c * D.nr_ctas + q];
-                    xr = xr * D.xv[(size_t)k * 4 + 3] + D.xv[(size_t)k * 4 + 0] * rs;
-                }
+                if (MODE == SODAGPU_FP8) xr = xr * D.xv[(size_t)k * 4 + 3] + D.xv[(size_t)k * 4 + 0] * s_rs[c];
                 const ChainScal *S = &D.scal[c];
                 CRng R;
                 crng_init(R, D.seed, c, rep, D.perm[k], P_SNP);
                 int err = 0;
-                delta = draw_snp(D, S, c, rep, D.perm[k], xr + ur, zz, zz / S->vare, R, &err);
+                if (MODE == SODAGPU_FP64)
+                    delta = draw_snp(D, S, c, rep, D.perm[k], xr + ur, zz, zz / S->vare, R, &err);
+                else
+                    delta = draw_snp_f(D, S, c, D.perm[k], (float)(xr + ur), (float)zz, (float)(zz / S->vare), R,
+                                       &err);
                 if (err) flag_err(D, 1);
             }
             D.delta[(size_t)c * D.bs + jk] = delta;
+            if (MODE != SODAGPU_FP64) D.delta32[(size_t)jk * CT + c] = (float)delta;   // chain-contiguous
         }
         // chains of one SNP are CT consecutive lanes (CT divides 32)
         const unsigned m = __ballot_sync(0xffffffffu, act && delta != 0.0);

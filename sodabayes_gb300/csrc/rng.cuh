@@ -144,4 +144,60 @@ __device__ __forceinline__ double d_rscinvchi2(double dof, double scale, CRng &s
     return 1.0 / d_rgamma(shape, 1.0 / sc, s, err);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 transforms for the reduced-precision sweeps (same counter streams).
+// Uniforms take the top 24 bits of each word, offset by half a unit so they
+// lie strictly inside (0,1): log(u) is always finite.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float crng_unit_f(CRng &s)
+{
+    return ((float)(uint32_t)(crng_u64(s) >> 40) + 0.5f) * 5.9604644775390625e-8f;
+}
+
+__device__ __forceinline__ float d_rnorm_f(float mean, float sd, CRng &s)
+{
+    if (sd <= 0.0f) return mean;
+    const float u1 = crng_unit_f(s), u2 = crng_unit_f(s);
+    const float rr = sqrtf(-2.0f * logf(u1));
+    const float th = 6.2831854820251465f * u2;
+    return mean + sd * rr * sinf(th);
+}
+
+__device__ __forceinline__ float d_rgamma_f(float shape, float scale, CRng &s, int *err)
+{
+    const bool small = shape < 1.0f;
+    const float sh = small ? shape + 1.0f : shape;
+    const float sc = small ? 1.0f : scale;
+    const float d = sh - 1.0f / 3.0f;
+    const float c = 1.0f / sqrtf(9.0f * d);
+    float res = d;
+    int tries = 0;
+    for (;;) {
+        float x = d_rnorm_f(0.0f, 1.0f, s);
+        float v = 1.0f + c * x;
+        while (v <= 0.0f && tries < 100000) {
+            x = d_rnorm_f(0.0f, 1.0f, s);
+            v = 1.0f + c * x;
+            ++tries;
+        }
+        v = v * v * v;
+        const float u = crng_unit_f(s);
+        const float xsq = x * x;
+        res = sc * d * v;
+        if ((u < 1.0f - 0.0331f * xsq * xsq) || (logf(u) < 0.5f * xsq + d * (1.0f - v + logf(v)))) break;
+        if (++tries >= 100000) { if (err) *err = 1; break; }
+    }
+    if (small) {
+        const float w = crng_unit_f(s);
+        return scale * res * powf(w, 1.0f / shape);
+    }
+    return res;
+}
+
+__device__ __forceinline__ float d_rscinvchi2_f(float dof, float scale, CRng &s, int *err)
+{
+    const float shape = 0.5f * dof, sc = 0.5f * dof * scale;
+    return 1.0f / d_rgamma_f(shape, 1.0f / sc, s, err);
+}
+
 }  // namespace soda

@@ -7,11 +7,13 @@
 //   xv     double [nloci][4]     the three values (code - 2p)/sqrt(2p(1-p))
 //                                of each column and 1/sqrt(2p(1-p)); all 0
 //                                for monomorphic SNPs
-//   U*     packed ragged columns of the augmenting matrix: column k holds
-//          rows 0..ulen[k]-1 at uoff[k]; FP64 / FP32 / BF16 hi+lo by mode
+//   U*     columns of the augmenting matrix: column k holds rows
+//          0..ulen[k]-1 at uoff[k]; columns of a subset are spaced
+//          round_up(N,8) apart (16-byte aligned, zero below ulen), FP64 in the
+//          FP64 mode, FP32 otherwise
 //   r      double [C][ldr]       residual yadj (master copy, FP64)
 //   r32    float  [C][ldr]       FP32 copy read by the FP32/FP8 dot products
-//   ra     double [C][bs]        augmented residual yAadj
+//   ra     double [C][ldra]      augmented residual yAadj (ra32: FP32 copy)
 //   g, vara_s double [C][nloci], cls int32 [C][nloci] (by SNP id)
 #pragma once
 #include <cuda_bf16.h>
@@ -65,6 +67,7 @@ struct Dev {
     const int8_t *G;
     const float *X32;
     const double *xv;          // [p][4]: x for codes 0,1,2 and 1/sd (0 if monomorphic)
+    const float *xv32;         // the same table in FP32 (FP32/FP8 inner loops)
     const double *y;
     const int64_t *uoff;
     const int32_t *ulen;
@@ -79,10 +82,13 @@ struct Dev {
     const int32_t *iskipped;   // skipped SNP ids
     const int32_t *grp;        // by SNP, 1-based
     const int32_t *blk_ls;     // [nb+1] first position of each subset
+    const int32_t *blk_pd;     // [nb] 1 when the subset's factor is the unpivoted one
     // chain state
     double *r;
     float *r32;
-    double *ra;
+    double *ra;                // [C][ldra]
+    float *ra32;               // [C][ldra] FP32 copy read by the FP32/FP8 dot products
+    int ldra;                  // chain stride of ra / ra32 (bs rounded up to 8)
     double *g;
     int32_t *cls;
     double *vara_s;
@@ -92,15 +98,13 @@ struct Dev {
     RunCtl *ctl;
     // scratch
     double *delta;             // [C][bs]
+    float *delta32;            // [bs][C] FP32 copy for the FP32/FP8 update (chain-contiguous)
     uint8_t *nzflag;           // [bs]
     double *rpart;             // [C][nr_ctas] row-CTA partial sums (mu, rsum, r^2)
     double *rsum;              // [C][nr_ctas] partial sums of r for the FP8 centring
     double *statpart;          // [C][NSTAT][ngroup*nmix] sum g^2
     int32_t *cntpart;          // [C][NSTAT][ngroup*nmix] counts
     double *recal_part;        // [C][RECAL_SPLIT][ldr]
-    double *upart;             // [tiles][nsplit][C][ROW_TILE] update partial sums
-    int32_t *ucount;           // [tiles] update tickets (self-resetting)
-    int nsplit;                // column splits of the update
     double *rpx, *rpu;         // [RHS_KSPLIT_MAX][C][bs] rhs partial sums (genotype / augmented part)
     int32_t *rticket;          // [bs] rhs tickets per M tile (self-resetting)
 };
@@ -108,9 +112,9 @@ struct Dev {
 constexpr int RHS_KSPLIT_MAX = 16;
 
 constexpr int NSTAT = 64;          // CTAs of the per-iteration SNP statistics
-constexpr int ROW_THREADS = 256;   // threads of the row kernels
-constexpr int ROWS_PER_THREAD = 4;
-constexpr int ROW_TILE = ROW_THREADS * ROWS_PER_THREAD;   // rows per row CTA
+constexpr int ROW_THREADS = 128;   // threads of the row kernels
+constexpr int ROWS_PER_THREAD = 1;
+constexpr int ROW_TILE = ROW_THREADS * ROWS_PER_THREAD;   // rows per row tile (= the update's tile)
 constexpr int RECAL_SPLIT = 32;    // column splits of the residual recalibration
 
 }  // namespace soda

@@ -148,6 +148,95 @@ __device__ double draw_snp(const Dev &D, const ChainScal *S, int c, int rep, int
     return gold - gnew;
 }
 
+// The same draw in FP32 arithmetic, for the FP32/FP8 sweeps: GB300 executes
+// FP64 at a small fraction of its FP32 rate, and the draws of a subset sit on
+// the critical path of every subset.  State stays FP64.
+__device__ double draw_snp_f(const Dev &D, const ChainScal *S, int c, int snploc, float rhs, float zz,
+                             float zz_vare, CRng &R, int *err)
+{
+    const size_t o = (size_t)c * D.p + snploc;
+    const float vare = (float)S->vare;
+    const double gold = D.g[o];
+    float gk = (float)gold;
+    const int m = D.method;
+    const float df_va = (float)D.df_va, scale_va = (float)S->scale_va;
+    if (m == SODAGPU_BAYES_A) {
+        rhs = rhs + zz * gk;
+        const float vs = (float)D.vara_s[o];
+        const float v1 = zz + vare / vs;
+        gk = d_rnorm_f(rhs / v1, sqrtf(vare / v1), R);
+        D.g[o] = (double)gk;
+        const float scale = (gk * gk + scale_va * df_va) / (df_va + 1.0f);
+        D.vara_s[o] = (double)d_rscinvchi2_f(df_va + 1.0f, scale, R, err);
+        return gold - (double)gk;
+    }
+    const int cl = D.cls[o];
+    if (cl > 1) rhs = rhs + zz * gk;
+    const int ng = D.ngroup;
+    if (m == SODAGPU_BAYES_B) {
+        const float vs = (float)D.vara_s[o];
+        const float s1 = (float)S->log_p[0];
+        const float logdetV = logf(vs * zz_vare + 1.0f);
+        const float uhat = rhs / (zz + vare / vs);
+        const float s2 = -0.5f * (logdetV - (rhs * uhat / vare)) + (float)S->log_p[ng];
+        const float clike = s1 - s2;
+        float sk;
+        if (clike > 700.0f) sk = 0.0f;
+        else if (clike < -700.0f) sk = 1.0f;
+        else sk = 1.0f / (1.0f + expf(clike));
+        const float u = crng_unit_f(R);
+        const int flag = u < sk ? 2 : 1;
+        double gnew;
+        if (flag == 1) {
+            gk = d_rnorm_f(0.0f, sqrtf(vs), R);
+            gnew = 0.0;
+        } else {
+            const float v1 = zz + vare / vs;
+            gk = d_rnorm_f(rhs / v1, sqrtf(vare / v1), R);
+            gnew = (double)gk;
+        }
+        D.g[o] = gnew;
+        D.cls[o] = flag;
+        const float scale = (gk * gk + scale_va * df_va) / (df_va + 1.0f);
+        D.vara_s[o] = (double)d_rscinvchi2_f(df_va + 1.0f, scale, R, err);
+        return gold - gnew;
+    }
+    const int nm = D.nmix;
+    const int sg = D.grp[snploc] - 1;
+    float sv[MAXDIST];
+    sv[0] = (float)S->log_p[sg];
+    for (int kk = 1; kk < nm; ++kk) {
+        const float logdetV = logf((float)S->gp[kk] * zz_vare + 1.0f);
+        const float uhat = rhs / (zz + (float)S->vare_gp[kk]);
+        sv[kk] = -0.5f * (logdetV - (rhs * uhat / vare)) + (float)S->log_p[sg + kk * ng];
+    }
+    const float u = crng_unit_f(R);
+    float ssculm = 0.0f;
+    int flag = 1;
+    for (int kk = 0; kk < nm; ++kk) {
+        const float skk = sv[kk];
+        float sk = 0.0f;
+        bool overflow = false;
+        for (int j = 0; j < nm; ++j) {
+            if (j == kk) continue;
+            const float clike = sv[j] - skk;
+            if (clike < -700.0f) continue;
+            if (clike > 700.0f) { overflow = true; break; }
+            sk = sk + expf(clike);
+        }
+        ssculm = ssculm + (overflow ? 0.0f : 1.0f / (1.0f + sk));
+        if (u < ssculm) { flag = kk + 1; break; }
+    }
+    double gnew = 0.0;
+    if (flag != 1) {
+        const float v1 = zz + vare / (float)S->gp[flag - 1];
+        gnew = (double)d_rnorm_f(rhs / v1, sqrtf(vare / v1), R);
+    }
+    D.cls[o] = flag;
+    D.g[o] = gnew;
+    return gold - gnew;
+}
+
 }  // namespace soda
 
 #include "rhs_kernel.cuh"
@@ -217,177 +306,11 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
     }
 }
 
-// ---------------------------------------------------------------------------
-// residual update r += X_b delta (rows of r) and ra += U_b delta (rows of ra)
-// (models.f90:164-174).  Only positions with a non-zero delta in some chain
-// contribute.  Each row tile (1024 rows) is split over `nsplit` CTAs by
-// column chunks; every CTA writes its partial sums, and the last CTA of the
-// tile to finish (atomic ticket) adds them in split order — deterministic,
-// no waiting.  FP64 mode accumulates in FP64, the FP32/FP8 modes in FP32;
-// the master residual is FP64 in every mode.
-// ---------------------------------------------------------------------------
-constexpr int UPD_CHUNK = 64;
+}  // namespace soda
 
-static inline size_t update_smem_bytes(int bs) { return sizeof(int) * ((size_t)bs + 32); }
+#include "update_kernel.cuh"
 
-template <int MODE, int CT>
-__global__ void __launch_bounds__(ROW_THREADS, 1) k_update(Dev D, int b, int nsplit)
-{
-    typedef typename std::conditional<MODE == SODAGPU_FP64, double, float>::type acc_t;
-    extern __shared__ int s_list[];  // bs + 32 ints
-    __shared__ int s_wcnt[ROW_THREADS / 32 + 1];
-    __shared__ int s_n, s_last;
-    __shared__ acc_t s_xv[UPD_CHUNK][3];
-    __shared__ acc_t s_dl[UPD_CHUNK][CT];
-    __shared__ int64_t s_off[UPD_CHUNK];
-    __shared__ int s_len[UPD_CHUNK];
-    __shared__ double sh[33];
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int ls = D.blk_ls[b];
-    const int N = D.blk_ls[b + 1] - ls;
-    // positions with a non-zero delta in any chain, in subset order
-    if (tid == 0) s_n = 0;
-    __syncthreads();
-    for (int base = 0; base < N; base += ROW_THREADS) {
-        const int jk = base + tid;
-        const bool f = jk < N && D.nzflag[jk];
-        const unsigned m = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) s_wcnt[w] = __popc(m);
-        __syncthreads();
-        if (tid == 0) {
-            int acc = s_n;
-            for (int q = 0; q < ROW_THREADS / 32; ++q) {
-                const int t = s_wcnt[q];
-                s_wcnt[q] = acc;
-                acc += t;
-            }
-            s_wcnt[ROW_THREADS / 32] = acc;
-        }
-        __syncthreads();
-        if (f) s_list[s_wcnt[w] + __popc(m & ((1u << lane) - 1u))] = jk;
-        __syncthreads();
-        if (tid == 0) s_n = s_wcnt[ROW_THREADS / 32];
-        __syncthreads();
-    }
-    const int nlist = s_n;
-    if (nlist == 0) return;   // nothing changed: r, r32 and rsum stay valid
-    const int ntile_r = D.nr_ctas;
-    const int tile = blockIdx.x / nsplit, split = blockIdx.x % nsplit;
-    const bool rows = tile < ntile_r;
-    const int t0 = (rows ? tile : tile - ntile_r) * ROW_TILE;
-    const int nrow = rows ? D.n : D.bs;
-    const int i0 = t0 + tid * ROWS_PER_THREAD;     // 4 consecutive rows per thread
-    const int q0 = (int)(((long long)nlist * split) / nsplit);
-    const int q1 = (int)(((long long)nlist * (split + 1)) / nsplit);
-    acc_t acc[ROWS_PER_THREAD][CT];
-#pragma unroll
-    for (int e = 0; e < ROWS_PER_THREAD; ++e)
-#pragma unroll
-        for (int c = 0; c < CT; ++c) acc[e][c] = 0;
-    for (int base = q0; base < q1; base += UPD_CHUNK) {
-        const int cnt = min(UPD_CHUNK, q1 - base);
-        __syncthreads();
-        for (int t = tid; t < cnt * CT; t += ROW_THREADS) {
-            const int q = t / CT, c = t % CT;
-            s_dl[q][c] = (acc_t)D.delta[(size_t)c * D.bs + s_list[base + q]];
-        }
-        if (tid < cnt) {
-            const int k = ls + s_list[base + tid];
-            s_xv[tid][0] = (acc_t)D.xv[(size_t)k * 4 + 0];
-            s_xv[tid][1] = (acc_t)D.xv[(size_t)k * 4 + 1];
-            s_xv[tid][2] = (acc_t)D.xv[(size_t)k * 4 + 2];
-            s_off[tid] = D.uoff[k];
-            s_len[tid] = D.ulen[k];
-        }
-        __syncthreads();
-        if (i0 >= nrow) continue;
-#pragma unroll 4
-        for (int q = 0; q < cnt; ++q) {
-            acc_t x[ROWS_PER_THREAD];
-            if (rows) {
-                const int k = ls + s_list[base + q];
-                if (MODE == SODAGPU_FP32) {
-                    const float4 xx = *reinterpret_cast<const float4 *>(D.X32 + (size_t)k * D.ldx + i0);
-                    x[0] = xx.x; x[1] = xx.y; x[2] = xx.z; x[3] = xx.w;
-                } else {
-                    const uint32_t wv = *reinterpret_cast<const uint32_t *>(D.G + (size_t)k * D.ldx + i0);
-#pragma unroll
-                    for (int e = 0; e < ROWS_PER_THREAD; ++e) x[e] = s_xv[q][(wv >> (8 * e)) & 3];
-                }
-            } else {
-                const int len = s_len[q];
-                const int64_t o = s_off[q] + i0;
-#pragma unroll
-                for (int e = 0; e < ROWS_PER_THREAD; ++e) {
-                    acc_t u = 0;
-                    if (i0 + e < len) {
-                        if (MODE == SODAGPU_FP64) u = (acc_t)D.U64[o + e];
-                        else if (MODE == SODAGPU_FP32) u = (acc_t)D.U32[o + e];
-                        else u = (acc_t)(__bfloat162float(D.Uhi[o + e]) + __bfloat162float(D.Ulo[o + e]));
-                    }
-                    x[e] = u;
-                }
-            }
-#pragma unroll
-            for (int e = 0; e < ROWS_PER_THREAD; ++e)
-#pragma unroll
-                for (int c = 0; c < CT; ++c) acc[e][c] += x[e] * s_dl[q][c];
-        }
-    }
-    // publish this split's partial sums, then the last CTA of the tile reduces
-    double *part = D.upart + (size_t)tile * nsplit * CT * ROW_TILE;
-    if (i0 < nrow) {
-#pragma unroll
-        for (int c = 0; c < CT; ++c)
-#pragma unroll
-            for (int e = 0; e < ROWS_PER_THREAD; ++e)
-                part[((size_t)split * CT + c) * ROW_TILE + tid * ROWS_PER_THREAD + e] = (double)acc[e][c];
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) {
-        const int prev = atomicAdd(&D.ucount[tile], 1);
-        s_last = prev == nsplit - 1;
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    double rsum_c[CT];
-#pragma unroll
-    for (int c = 0; c < CT; ++c) rsum_c[c] = 0.0;
-    if (i0 < nrow) {
-#pragma unroll
-        for (int c = 0; c < CT; ++c) {
-#pragma unroll
-            for (int e = 0; e < ROWS_PER_THREAD; ++e) {
-                const int i = i0 + e;
-                if (i >= nrow) continue;
-                double d = 0.0;
-                for (int sp = 0; sp < nsplit; ++sp)
-                    d += __ldcg(part + ((size_t)sp * CT + c) * ROW_TILE + tid * ROWS_PER_THREAD + e);
-                if (rows) {
-                    const size_t o = (size_t)c * D.ldr + i;
-                    const double v = D.r[o] + d;
-                    D.r[o] = v;
-                    D.r32[o] = (float)v;
-                    rsum_c[c] += v;
-                } else {
-                    const size_t o = (size_t)c * D.bs + i;
-                    D.ra[o] = D.ra[o] + d;
-                }
-            }
-        }
-    }
-    if (tid == 0) D.ucount[tile] = 0;   // ready for the next subset
-    if (MODE == SODAGPU_FP8 && rows) {
-        // refresh this tile's partial sum of r; rows outside the tile keep theirs
-#pragma unroll
-        for (int c = 0; c < CT; ++c) {
-            const double t = block_sum(rsum_c[c], sh);
-            if (tid == 0) D.rsum[(size_t)c * D.nr_ctas + tile] = t;
-        }
-    }
-}
+namespace soda {
 
 // ---------------------------------------------------------------------------
 // skipped SNPs (pivoted fallback only), one CTA per chain, SNPs in order.
@@ -535,12 +458,10 @@ __global__ void __launch_bounds__(256) k_stats(Dev D)
     } else {
         const int rb = blockIdx.x - NSTAT;
         double v2 = 0.0;
-        for (int q = 0; q < ROWS_PER_THREAD; ++q) {
-            const int i = rb * ROW_TILE + q * 256 + threadIdx.x;
-            if (i < D.n) {
-                const double v = D.r[(size_t)c * D.ldr + i];
-                v2 += v * v;
-            }
+        const int i = rb * ROW_TILE + threadIdx.x;
+        if (threadIdx.x < ROW_TILE && i < D.n) {
+            const double v = D.r[(size_t)c * D.ldr + i];
+            v2 = v * v;
         }
         const double t = block_sum(v2, sh);
         if (threadIdx.x == 0) D.rpart[(size_t)c * D.nr_ctas + rb] = t;
@@ -661,7 +582,9 @@ __global__ void __launch_bounds__(256) k_post(Dev D)
     for (int i = t0; i < D.naind; i += stride) {
         CRng R;
         crng_init(R, D.seed, c, rep, i, P_RA);
-        D.ra[(size_t)c * D.bs + i] = d_rnorm(0.0, sd, R);
+        const double v = d_rnorm(0.0, sd, R);
+        D.ra[(size_t)c * D.ldra + i] = v;
+        D.ra32[(size_t)c * D.ldra + i] = (float)v;
     }
     if (!S->keep) return;
     const int m = D.method;
@@ -804,7 +727,8 @@ __global__ void __launch_bounds__(256) k_init_chain(Dev D, double vara0, double 
             crng_init(R, D.seed, c, 0, i, P_RA);
             v = d_rnorm(0.0, sd, R);
         }
-        D.ra[(size_t)c * D.bs + i] = v;
+        D.ra[(size_t)c * D.ldra + i] = v;
+        D.ra32[(size_t)c * D.ldra + i] = (float)v;
     }
 }
 
@@ -851,17 +775,18 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
     constexpr int MTS = 8 * SptOf<CT>::v;
     const int mtiles = (nblk_snps + MTS - 1) / MTS;
     const int nst = (D.ldx + RhsCfg<MODE>::KST - 1) / RhsCfg<MODE>::KST;
-    int ks = (2 * sm_count + mtiles - 1) / mtiles;
+    // one wave: a CTA per SM (the pipeline fills most of its shared memory)
+    int ks = sm_count / mtiles;
     ks = ks < 1 ? 1 : (ks > RHS_KSPLIT_MAX ? RHS_KSPLIT_MAX : ks);
     ks = ks > nst ? nst : ks;
     {
         ProfScope ps(prof, st, PROF_RHS);
         k_rhs<MODE, CT><<<mtiles * ks, 256, rhs_smem_bytes<MODE, CT>(), st>>>(D, b, ks);
     }
-    const int ntile = D.nr_ctas + (D.bs + ROW_TILE - 1) / ROW_TILE;
+    const int ntile = D.nr_ctas + (D.bs + UT - 1) / UT;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
-        k_update<MODE, CT><<<ntile * D.nsplit, ROW_THREADS, update_smem_bytes(D.bs), st>>>(D, b, D.nsplit);
+        k_update<MODE, CT><<<ntile, 32 * UpdWarps<MODE, CT>::v, update_smem_bytes_ct<MODE, CT>(D.bs), st>>>(D, b);
     }
     return cudaGetLastError();
 }
@@ -881,15 +806,21 @@ static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int sm_count
 
 int sweep_chain_count_supported(int c) { return c == 1 || c == 2 || c == 4 || c == 8 || c == 16; }
 
-template <int MODE>
-static cudaError_t set_update_smem_mode(size_t bytes)
+template <int MODE, int CT>
+static cudaError_t set_update_smem(int bs)
 {
-    cudaError_t e = cudaSuccess;
-    e = cudaFuncSetAttribute(k_update<MODE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_update<MODE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return cudaFuncSetAttribute(k_update<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)update_smem_bytes_ct<MODE, CT>(bs));
+}
+
+template <int MODE>
+static cudaError_t set_update_smem_mode(int bs)
+{
+    cudaError_t e = set_update_smem<MODE, 1>(bs);
+    if (e == cudaSuccess) e = set_update_smem<MODE, 2>(bs);
+    if (e == cudaSuccess) e = set_update_smem<MODE, 4>(bs);
+    if (e == cudaSuccess) e = set_update_smem<MODE, 8>(bs);
+    if (e == cudaSuccess) e = set_update_smem<MODE, 16>(bs);
     return e;
 }
 
@@ -918,12 +849,10 @@ cudaError_t sweep_prepare(int bs)
     if (e == cudaSuccess) e = set_rhs_smem_mode<SODAGPU_FP32>();
     if (e == cudaSuccess) e = set_rhs_smem_mode<SODAGPU_FP8>();
     if (e != cudaSuccess) return e;
-    const size_t bytes = update_smem_bytes(bs);
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    if (bytes > 200 * 1024) return cudaErrorInvalidValue;
-    e = set_update_smem_mode<SODAGPU_FP64>(bytes);
-    if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP32>(bytes);
-    if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP8>(bytes);
+    if (update_smem_bytes_ct<SODAGPU_FP64, 16>(bs) > 220 * 1024) return cudaErrorInvalidValue;
+    e = set_update_smem_mode<SODAGPU_FP64>(bs);
+    if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP32>(bs);
+    if (e == cudaSuccess) e = set_update_smem_mode<SODAGPU_FP8>(bs);
     return e;
 }
 

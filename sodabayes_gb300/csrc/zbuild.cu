@@ -83,6 +83,12 @@ __global__ void k_gather(const int8_t *Gsnp, int8_t *Gpos, const int32_t *perm, 
     }
 }
 
+__global__ void k_xv32(const double *xv, int p, float *xv32)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 4 * p) xv32[t] = (float)xv[t];
+}
+
 __global__ void k_xv(const double *freq, const int32_t *perm, int p, double *xv)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -707,6 +713,12 @@ cudaError_t zb_gather(const int8_t *Gsnp, int8_t *Gpos, const int32_t *perm, int
 cudaError_t zb_xv(const double *freq, const int32_t *perm, int p, double *xv, cudaStream_t st)
 {
     k_xv<<<(p + 255) / 256, 256, 0, st>>>(freq, perm, p, xv);
+    return cudaGetLastError();
+}
+
+cudaError_t zb_xv32(const double *xv, int p, float *xv32, cudaStream_t st)
+{
+    k_xv32<<<(4 * p + 255) / 256, 256, 0, st>>>(xv, p, xv32);
     return cudaGetLastError();
 }
 

@@ -10,6 +10,7 @@ cudaError_t zb_decode_bed(const uint8_t *bed, int n, int p, int8_t *G, int ldx, 
 cudaError_t zb_freq(int8_t *G, int n, int p, int ldx, double *freq, int *bad, cudaStream_t st);
 cudaError_t zb_gather(const int8_t *Gsnp, int8_t *Gpos, const int32_t *perm, int p, int ldx, cudaStream_t st);
 cudaError_t zb_xv(const double *freq, const int32_t *perm, int p, double *xv, cudaStream_t st);
+cudaError_t zb_xv32(const double *xv, int p, float *xv32, cudaStream_t st);
 cudaError_t zb_x32(const int8_t *G, const double *xv, float *X32, int n, int p, int ldx, cudaStream_t st);
 cudaError_t zb_gram(const int8_t *G, int ldx, const int32_t *blk_ls, const int32_t *batch_blocks, int nbatch,
                     int maxN, const int64_t *wofs, const double *freq, const int32_t *perm, int n, double *W,
