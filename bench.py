@@ -152,10 +152,15 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+# Priors on the scale of the simulated data: per-SNP effect variance ~1 (true
+# effects N(0,1)) and residual variance ~2000 (var(y) ~ 4000 at h2 = 0.5).
+PRIORS = dict(scale_va=1.0, df_va=4.0, scale_ve=2000.0, df_ve=4.0)
+
+
 def _opts(prec, chains, seed, numit):
     from sodabayes_gb300 import JobOptions
-    return JobOptions(method=METHOD, numit=numit, burnin=0, blocksize=BLOCKSIZE, seed=seed, scale_va=0.01,
-                      df_va=4.0, scale_ve=0.01, df_ve=4.0, precision=prec, chains=chains)
+    return JobOptions(method=METHOD, numit=numit, burnin=0, blocksize=BLOCKSIZE, seed=seed, precision=prec,
+                      chains=chains, **PRIORS)
 
 
 def _make_job(spec, codes_dev, y, prec, chains, seed, numit=100000):
@@ -338,7 +343,7 @@ def main():
     rank, ws = _dist_init()
     config = {"workload": "config 3: SODA BayesCpi n=20000 p=500000 subset 2000 (250 subsets), LD generator "
                           "(50-SNP AR(1) blocks rho=0.7, maf~U(0.01,0.5)), 2000 causal effects, h2=0.5",
-              "n": 20000, "p": 500000, "blocksize": BLOCKSIZE, "method": METHOD,
+              "n": 20000, "p": 500000, "blocksize": BLOCKSIZE, "method": METHOD, "priors": PRIORS,
               "l2_policy": "inputs larger than L2 (10 GB of genotype codes per iteration vs 126 MB L2)"}
     if args.impl == "reference":
         if rank != 0:

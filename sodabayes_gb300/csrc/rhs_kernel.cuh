@@ -195,8 +195,14 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
             const int jk = j0 + warp * SPT + s;
 #pragma unroll
             for (int c = 0; c < CT; ++c) {
-                const double a = MODE == SODAGPU_FP64 ? warp_sum((double)acc[s][c]) : (double)warp_sumf((float)acc[s][c]);
-                if (lane == 0 && jk < N) dstp[((size_t)ks * CT + c) * D.bs + jk] = a;
+                // FP32 modes reduce in FP32; only lane 0 widens (the FP64 pipe is narrow)
+                if (MODE == SODAGPU_FP64) {
+                    const double a = warp_sum((double)acc[s][c]);
+                    if (lane == 0 && jk < N) dstp[((size_t)ks * CT + c) * D.bs + jk] = a;
+                } else {
+                    const float a = warp_sumf((float)acc[s][c]);
+                    if (lane == 0 && jk < N) dstp[((size_t)ks * CT + c) * D.bs + jk] = (double)a;
+                }
                 acc[s][c] = 0;
             }
         }
