@@ -52,6 +52,11 @@ enum sodagpu_method {
  *         FP32 rank-1 correction, U as BF16 hi+lo pairs.                      */
 enum sodagpu_precision { SODAGPU_FP64 = 0, SODAGPU_FP32 = 1, SODAGPU_FP8 = 2 };
 
+/* Sweep kernels.  AUTO puts the genotype products of the FP8 mode with 4, 8
+   or 16 chains on the tensor cores (tcgen05); CUDA_CORES keeps every product
+   on the FP32/FP64 cores.  Results agree to rounding. */
+enum sodagpu_kernels { SODAGPU_KERNELS_AUTO = 0, SODAGPU_KERNELS_CUDA_CORES = 1 };
+
 /* Genotype input layouts for sodagpu_load_genotypes(). */
 enum sodagpu_geno_layout {
     /* int8 codes 0/1/2, column-major nind x nloci (one SNP per column);
@@ -104,7 +109,8 @@ typedef struct sodagpu_config {
     double alpha[SODAGPU_MAXDIST]; /* -alpha (Dirichlet prior)                  */
     double vara0;       /* value of the module variable `vara` on entry: the
                            df_va<=0 branch adds to it (models.f90:99-102)       */
-    int32_t reserved[8];
+    int32_t kernels;    /* enum sodagpu_kernels: which sweep kernels run        */
+    int32_t reserved[7];
 } sodagpu_config;
 
 /* One thinned iteration of the .hyp trace (models.f90:549-569). */

@@ -112,6 +112,7 @@ class JobOptions:
     chains: int = 1
     recal_every: int = 1000
     vara0: float = 0.0
+    kernels: str = "auto"          # "auto" (tensor cores where they apply) or "cuda_cores"
 
 
 def make_config(nind: int, nloci: int, opts: JobOptions) -> Config:
@@ -164,6 +165,10 @@ def make_config(nind: int, nloci: int, opts: JobOptions) -> Config:
     cfg.chains = opts.chains
     cfg.recal_every = opts.recal_every
     cfg.vara0 = opts.vara0
+    kern = {"auto": 0, "cuda_cores": 1}
+    if opts.kernels not in kern:
+        raise ValueError("kernels must be 'auto' or 'cuda_cores'")
+    cfg.kernels = kern[opts.kernels]
     return cfg
 
 

@@ -115,6 +115,11 @@ struct sodagpu_ctx {
            *upart = nullptr, *rpx = nullptr, *rpu = nullptr;
     int32_t *cntpart = nullptr, *ucount = nullptr, *rticket = nullptr;
     uint8_t *nzflag = nullptr;
+    int tc = 0, ldd = 0;                 // tensor-core sweep
+    uint16_t *dsplit = nullptr;
+    double *k0part = nullptr;
+    float *rapart = nullptr;
+    int32_t *raticket = nullptr;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
     cudaGraphExec_t graph = nullptr;
@@ -218,6 +223,8 @@ int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out)
     if (cfg->precision < 0 || cfg->precision > 2) return fail(SODAGPU_E_ARG, "precision out of range");
     if (cfg->chains < 1 || !sweep_chain_count_supported(cfg->chains))
         return fail(SODAGPU_E_UNSUPPORTED, "chains must be 1, 2, 4, 8 or 16");
+    if (cfg->kernels != SODAGPU_KERNELS_AUTO && cfg->kernels != SODAGPU_KERNELS_CUDA_CORES)
+        return fail(SODAGPU_E_ARG, "kernels %d out of range", cfg->kernels);
     for (int j = 1; j < cfg->nmix; ++j)
         if (cfg->method >= SODAGPU_BAYES_C && !(cfg->mix[j] > 0.0))
             return fail(SODAGPU_E_ARG, "mix[%d] must be > 0", j);
@@ -703,6 +710,12 @@ int build_dev(sodagpu_ctx *c)
     D.rpx = c->rpx;
     D.rpu = c->rpu;
     D.rticket = c->rticket;
+    D.tc = c->tc;
+    D.ldd = c->ldd;
+    D.dsplit = c->dsplit;
+    D.k0part = c->k0part;
+    D.rapart = c->rapart;
+    D.raticket = c->raticket;
     return 0;
 }
 
@@ -739,6 +752,15 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         TRY(c->alloc(&c->rpx, (size_t)RHS_KSPLIT_MAX * C * c->bs));
         TRY(c->alloc(&c->rpu, (size_t)RHS_KSPLIT_MAX * C * c->bs));
         TRY(c->alloc(&c->rticket, c->bs));
+        c->tc = c->cfg.kernels == SODAGPU_KERNELS_AUTO && sweep_tc_supported(c->cfg.precision, C, c->bs);
+        if (c->tc) {
+            const int mt = (c->bs + 127) / 128;
+            c->ldd = (int)round_up((size_t)c->bs, 128);
+            TRY(c->alloc(&c->dsplit, (size_t)sweep_tc_rows(C) * c->ldd));
+            TRY(c->alloc(&c->k0part, (size_t)mt * C));
+            TRY(c->alloc(&c->rapart, (size_t)mt * sweep_tc_ra_split() * C * 128));
+            TRY(c->alloc(&c->raticket, mt));
+        }
     }
     build_dev(c);
     RunCtl h{};

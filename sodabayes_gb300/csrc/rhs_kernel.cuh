@@ -74,6 +74,99 @@ __device__ __forceinline__ float code_to_f32(uint32_t w, int k)
     return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k)) - 8388608.0f;
 }
 
+// Ends one CTA of an M tile of `mts` SNPs whose split partial sums are in
+// rpx/rpu.  The last CTA of the tile to arrive (atomic ticket, no waiting)
+// adds the partial sums in split order and draws the tile's SNPs (256
+// threads).  With TC, it also writes what the tensor-core update reads: the
+// bf16 three-way split of delta/sd per chain (dsplit, zero past the subset's
+// end) and the tile's share of sum_j x0_j delta_j (k0part).
+template <int MODE, int CT, bool TC>
+__device__ void rhs_finish(const Dev &D, int b, int mt, int ksplit, int j0, int mts)
+{
+    __shared__ int s_last;
+    __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring), once per CTA
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int ls = D.blk_ls[b];
+    const int N = D.blk_ls[b + 1] - ls;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&D.rticket[mt], 1) == ksplit - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    // the last CTA of the M tile: totals in split order, then the draws
+    const int rep = cur_rep(D);
+    const double zz = D.xxd[b];
+    const int cnt = min(mts, N - j0);
+    if (MODE == SODAGPU_FP8) {
+        if (tid < CT) {
+            double rs = 0.0;
+            for (int q = 0; q < D.nr_ctas; ++q) rs += D.rsum[(size_t)tid * D.nr_ctas + q];
+            s_rs[tid] = rs;
+        }
+        __syncthreads();
+    }
+    const int span = TC ? mts : cnt;   // the tensor path also clears the tile's columns past the subset
+    for (int t = tid; t < ((span * CT + 31) & ~31); t += blockDim.x) {
+        const int jl = t / CT, c = t % CT;
+        const int jk = j0 + jl;
+        const bool act = jl < cnt;
+        double delta = 0.0;
+        if (act) {
+            const int k = ls + jk;
+            if (!D.skip[k]) {
+                double xr = 0.0, ur = 0.0;
+                for (int sp = 0; sp < ksplit; ++sp) {
+                    const size_t o = ((size_t)sp * CT + c) * D.bs + jk;
+                    xr += __ldcg(D.rpx + o);
+                    ur += __ldcg(D.rpu + o);
+                }
+                if (MODE == SODAGPU_FP8) xr = xr * D.xv[(size_t)k * 4 + 3] + D.xv[(size_t)k * 4 + 0] * s_rs[c];
+                const ChainScal *S = &D.scal[c];
+                CRng R;
+                crng_init(R, D.seed, c, rep, D.perm[k], P_SNP);
+                int err = 0;
+                if (MODE == SODAGPU_FP64)
+                    delta = draw_snp(D, S, c, rep, D.perm[k], xr + ur, zz, zz / S->vare, R, &err);
+                else
+                    delta = draw_snp_f(D, S, c, D.perm[k], (float)(xr + ur), (float)zz, (float)(zz / S->vare), R,
+                                       &err);
+                if (err) flag_err(D, 1);
+            }
+            D.delta[(size_t)c * D.bs + jk] = delta;
+            if (MODE != SODAGPU_FP64) D.delta32[(size_t)jk * CT + c] = (float)delta;   // chain-contiguous
+        }
+        if (TC && jl < mts) {
+            uint32_t hi = 0, mid = 0, lo = 0;
+            if (act && delta != 0.0) tc::split3((float)(delta * D.xv[(size_t)(ls + jk) * 4 + 3]), hi, mid, lo);
+            D.dsplit[(size_t)c * D.ldd + jk] = (uint16_t)hi;
+            D.dsplit[(size_t)(CT + c) * D.ldd + jk] = (uint16_t)mid;
+            D.dsplit[(size_t)(2 * CT + c) * D.ldd + jk] = (uint16_t)lo;
+        }
+        // chains of one SNP are CT consecutive lanes (CT divides 32)
+        const unsigned m = __ballot_sync(0xffffffffu, act && delta != 0.0);
+        const unsigned grp = CT >= 32 ? 0xffffffffu : (((1u << CT) - 1u) << ((lane / CT) * CT));
+        if (act && c == 0) D.nzflag[jk] = (m & grp) != 0u;
+    }
+    if (TC) {
+        // k0part[mt][c] = sum over the tile of x0_j delta_j (fixed order)
+        __shared__ double s_k0[256];
+        __syncthreads();   // this CTA's delta stores are visible to the block
+        const int c = tid % CT, part = tid / CT, nparts = blockDim.x / CT;
+        double a = 0.0;
+        for (int jl = part; jl < cnt; jl += nparts)
+            a += D.xv[(size_t)(ls + j0 + jl) * 4 + 0] * D.delta[(size_t)c * D.bs + j0 + jl];
+        s_k0[tid] = a;
+        __syncthreads();
+        if (tid < CT) {
+            double s = 0.0;
+            for (int q = 0; q < nparts; ++q) s += s_k0[q * CT + tid];
+            D.k0part[(size_t)mt * CT + tid] = s;
+        }
+    }
+    if (tid == 0) D.rticket[mt] = 0;
+}
+
 template <int MODE, int CT>
 __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
 {
@@ -87,7 +180,6 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     constexpr size_t SBYTES = rhs_stage_bytes<MODE, CT>();
     typedef typename std::conditional<MODE == SODAGPU_FP64, double, float>::type acc_t;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_last;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ls = D.blk_ls[b];
@@ -312,60 +404,7 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     if (nv == ng) publish(false);   // no augmenting stage in this split
     publish(true);
 
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&D.rticket[mt], 1) == ksplit - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    // the last CTA of the M tile: totals in split order, then the draws
-    const int rep = cur_rep(D);
-    const double zz = D.xxd[b];
-    const int cnt = min(MTS, N - j0);
-    __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring), once per CTA
-    if (MODE == SODAGPU_FP8) {
-        if (tid < CT) {
-            double rs = 0.0;
-            for (int q = 0; q < D.nr_ctas; ++q) rs += D.rsum[(size_t)tid * D.nr_ctas + q];
-            s_rs[tid] = rs;
-        }
-        __syncthreads();
-    }
-    for (int t = tid; t < ((cnt * CT + 31) & ~31); t += 256) {
-        const int jl = t / CT, c = t % CT;
-        const int jk = j0 + jl;
-        const bool act = jl < cnt;
-        double delta = 0.0;
-        if (act) {
-            const int k = ls + jk;
-            if (!D.skip[k]) {
-                double xr = 0.0, ur = 0.0;
-                for (int sp = 0; sp < ksplit; ++sp) {
-                    const size_t o = ((size_t)sp * CT + c) * D.bs + jk;
-                    xr += __ldcg(D.rpx + o);
-                    ur += __ldcg(D.rpu + o);
-                }
-                if (MODE == SODAGPU_FP8) xr = xr * D.xv[(size_t)k * 4 + 3] + D.xv[(size_t)k * 4 + 0] * s_rs[c];
-                const ChainScal *S = &D.scal[c];
-                CRng R;
-                crng_init(R, D.seed, c, rep, D.perm[k], P_SNP);
-                int err = 0;
-                if (MODE == SODAGPU_FP64)
-                    delta = draw_snp(D, S, c, rep, D.perm[k], xr + ur, zz, zz / S->vare, R, &err);
-                else
-                    delta = draw_snp_f(D, S, c, D.perm[k], (float)(xr + ur), (float)zz, (float)(zz / S->vare), R,
-                                       &err);
-                if (err) flag_err(D, 1);
-            }
-            D.delta[(size_t)c * D.bs + jk] = delta;
-            if (MODE != SODAGPU_FP64) D.delta32[(size_t)jk * CT + c] = (float)delta;   // chain-contiguous
-        }
-        // chains of one SNP are CT consecutive lanes (CT divides 32)
-        const unsigned m = __ballot_sync(0xffffffffu, act && delta != 0.0);
-        const unsigned grp = CT >= 32 ? 0xffffffffu : (((1u << CT) - 1u) << ((lane / CT) * CT));
-        if (act && c == 0) D.nzflag[jk] = (m & grp) != 0u;
-    }
-    if (tid == 0) D.rticket[mt] = 0;
+    rhs_finish<MODE, CT, false>(D, b, mt, ksplit, j0, MTS);
 }
 
 }  // namespace soda

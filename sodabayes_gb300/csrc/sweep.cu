@@ -17,6 +17,7 @@
 #include "rng.cuh"
 #include "state.cuh"
 #include "sweep.cuh"
+#include "tc.cuh"
 
 namespace soda {
 
@@ -309,6 +310,8 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
 }  // namespace soda
 
 #include "update_kernel.cuh"
+#include "rhs_tc.cuh"
+#include "update_tc.cuh"
 
 namespace soda {
 
@@ -769,9 +772,35 @@ struct ProfScope {
     }
 };
 
+// Tensor-core subset: rhs tiles of 128 SNPs x K splits (one wave of one CTA
+// per SM), then the update (row tiles of r on the tensor cores, ra tiles on
+// the FP32 cores; two CTAs per SM).
+template <int CT>
+static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_count, cudaStream_t st, ProfHook *prof)
+{
+    const int mtiles = (nblk_snps + TC_TM - 1) / TC_TM;
+    const int nst = D.ldx / TC_KC;
+    int ks = sm_count / mtiles;
+    ks = ks < 1 ? 1 : (ks > RHS_KSPLIT_MAX ? RHS_KSPLIT_MAX : ks);
+    ks = ks > nst ? nst : ks;
+    {
+        ProfScope ps(prof, st, PROF_RHS);
+        k_rhs_tc<CT><<<mtiles * ks, 256, RhsTc<CT>::SMEM, st>>>(D, b, ks);
+    }
+    const int ra_tiles = (nblk_snps + 127) / 128;
+    {
+        ProfScope ps(prof, st, PROF_UPDATE);
+        k_update_tc<CT><<<D.nr_ctas + ra_tiles * TU_RA_SPLIT, 256, UpdTc<CT>::SMEM, st>>>(D, b, TU_RA_SPLIT);
+    }
+    return cudaGetLastError();
+}
+
 template <int MODE, int CT>
 static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count, cudaStream_t st, ProfHook *prof)
 {
+    if constexpr (MODE == SODAGPU_FP8 && CT >= 4) {
+        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, sm_count, st, prof);
+    }
     constexpr int MTS = 8 * SptOf<CT>::v;
     const int mtiles = (nblk_snps + MTS - 1) / MTS;
     const int nst = (D.ldx + RhsCfg<MODE>::KST - 1) / RhsCfg<MODE>::KST;
@@ -842,9 +871,34 @@ static cudaError_t set_rhs_smem_mode()
     return e;
 }
 
+template <int CT>
+static cudaError_t set_tc_smem()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_rhs_tc<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)RhsTc<CT>::SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_update_tc<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UpdTc<CT>::SMEM);
+    return e;
+}
+
+int sweep_tc_supported(int precision, int chains, int bs)
+{
+    return precision == SODAGPU_FP8 && (chains == 4 || chains == 8 || chains == 16) && bs <= TU_MAXQ * TU_KC;
+}
+
+int sweep_tc_rows(int chains) { return ((3 * chains + 15) / 16) * 16; }
+
+int sweep_tc_ra_split() { return TU_RA_SPLIT; }
+
 // Raises the dynamic shared-memory limits of the rhs and update kernels.
 cudaError_t sweep_prepare(int bs)
 {
+    {
+        cudaError_t e = set_tc_smem<4>();
+        if (e == cudaSuccess) e = set_tc_smem<8>();
+        if (e == cudaSuccess) e = set_tc_smem<16>();
+        if (e != cudaSuccess) return e;
+    }
     cudaError_t e = set_rhs_smem_mode<SODAGPU_FP64>();
     if (e == cudaSuccess) e = set_rhs_smem_mode<SODAGPU_FP32>();
     if (e == cudaSuccess) e = set_rhs_smem_mode<SODAGPU_FP8>();

@@ -7,6 +7,11 @@ namespace soda {
 
 int sweep_chain_count_supported(int chains);
 cudaError_t sweep_prepare(int bs);
+// Tensor-core sweep: whether it applies, the rows of its delta split
+// (3 * chains rounded up to 16) and the CTAs per 128-row tile of ra.
+int sweep_tc_supported(int precision, int chains, int bs);
+int sweep_tc_rows(int chains);
+int sweep_tc_ra_split();
 // Optional per-launch event recording (eager profiling, never inside a graph):
 // before/after every launch an event pair is recorded and its kernel class
 // stored.  Classes: 0 rhs+draw, 1 residual update, 2 mu, 3 everything else.

@@ -1,0 +1,187 @@
+// tc.cuh — fifth-generation tensor-core primitives (tcgen05, sm_100a family)
+// written as inline PTX: tensor-memory allocation, the single-thread MMA
+// issue with shared-memory operand descriptors, completion through an
+// mbarrier, and tensor-memory loads for the epilogue.
+//
+// Operand layout used throughout: K-major, 128-byte swizzle.  A tile of R rows
+// by 64 bf16 of K is R/8 atoms of 1024 bytes; row r of an atom holds its 128
+// bytes as 16-byte chunks, logical chunk c stored at chunk c ^ (r % 8).  Tiles
+// wider than 64 in K are consecutive such regions.  Atoms must start on a
+// 1024-byte boundary.
+#pragma once
+#include <stdint.h>
+
+namespace soda {
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start address, leading/stride byte offsets
+// (both >> 4), descriptor version 1, 128-byte swizzle.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr, uint32_t sbo_bytes)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1u << 16;                          // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;                          // version
+    d |= (uint64_t)2u << 61;                          // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor for kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// byte offset of the 16-byte chunk holding (row, k..k+7) in a K-major SW128
+// tile with `rows` rows (k a multiple of 8)
+__device__ __forceinline__ uint32_t sw128_off(int row, int k, int rows)
+{
+    const int region = k >> 6, chunk = (k >> 3) & 7;
+    return (uint32_t)region * (uint32_t)rows * 128u + (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u +
+           (uint32_t)((chunk ^ (row & 7)) << 4);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int limit = 1 << 22)
+{
+    for (int i = 0; i < limit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void fence_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_after_sync()
+{
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Warp-wide: allocate ncols tensor-memory columns (power of two, >= 32); the
+// address is written to *slot.
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on *bar once every MMA issued so far by this thread has completed.
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+// 8 consecutive FP32 columns of this thread's lane (warp w reads lanes
+// 32*(w%4) .. 32*(w%4)+31; taddr carries lane << 16 | column).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld()
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// bf16 bits of a float, round to nearest even (finite inputs)
+__device__ __forceinline__ uint32_t bf16_bits(float x)
+{
+    const uint32_t u = __float_as_uint(x);
+    return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
+}
+
+__device__ __forceinline__ float bf16_val(uint32_t b)
+{
+    return __uint_as_float(b << 16);
+}
+
+// x ~ hi + mid + lo, each a bf16 (about 24 significant bits together)
+__device__ __forceinline__ void split3(float x, uint32_t &hi, uint32_t &mid, uint32_t &lo)
+{
+    hi = bf16_bits(x);
+    const float r1 = x - bf16_val(hi);
+    mid = bf16_bits(r1);
+    const float r2 = r1 - bf16_val(mid);
+    lo = bf16_bits(r2);
+}
+
+// Four genotype codes (bytes, each 0..2) -> two words of two bf16 each:
+// w01 = bf16(b0) | bf16(b1) << 16, w23 likewise.  bf16(0) = 0x0000,
+// bf16(1) = 0x3F80, bf16(2) = 0x4000: the codes select the high and low
+// bytes from two small tables.
+__device__ __forceinline__ void codes_to_bf16x4(uint32_t w, uint32_t &w01, uint32_t &w23)
+{
+    const uint32_t t = w | (w >> 4);                            // nibbles b0 b1 in byte 0, b2 b3 in byte 2
+    const uint32_t sel = (t & 0xFFu) | ((t >> 8) & 0xFF00u);    // selector nibbles b0 b1 b2 b3
+    const uint32_t hb = __byte_perm(0x00403F00u, 0u, sel);      // high bytes
+    const uint32_t lb = __byte_perm(0x00008000u, 0u, sel);      // low bytes
+    w01 = __byte_perm(lb, hb, 0x5140u);
+    w23 = __byte_perm(lb, hb, 0x7362u);
+}
+
+}  // namespace tc
+}  // namespace soda

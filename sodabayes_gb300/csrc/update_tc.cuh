@@ -1,0 +1,319 @@
+// update_tc.cuh — tensor-core residual update of one subset for FP8 mode with
+// several chains (models.f90:164-174 for every chain at once), included by
+// sweep.cu after rhs_tc.cuh.
+//
+//   r  += X_b delta = sum_j x0_j delta_j + G_b (delta / sd)
+//   ra += U_b delta
+//
+// Row tiles of r (128 individuals, one CTA each) run on tcgen05: A = the
+// tile's codes of 64 subset positions per stage, transposed to individual-major
+// bf16 in shared memory, B = the three-way bf16 split of delta/sd written by
+// the draws (rhs_finish), D = 128 x 3*chains FP32 in tensor memory.  Stages
+// whose 64 positions have no non-zero delta in any chain are skipped.  The
+// centring term sum_j x0_j delta_j is added in FP64 from the per-tile sums of
+// the draws.  The augmented rows ra (U_b is FP32, one tile of 128 rows per
+// ra_split CTAs over column ranges) run on the FP32 cores; the last CTA of a
+// row tile adds the split partial sums in split order (deterministic).
+#pragma once
+
+namespace soda {
+
+constexpr int TU_KC = 64;          // subset positions per stage
+constexpr int TU_NS = 4;           // raw stages in flight
+constexpr int TU_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
+constexpr int TU_RA_SPLIT = 8;     // CTAs per 128-row tile of ra
+constexpr int TU_UNR = 4;          // U columns in flight per warp
+
+template <int CT>
+struct UpdTc {
+    static constexpr int NB = RhsTc<CT>::NB;
+    static constexpr int RAW_A = TU_KC * 128;          // codes: 64 positions x 128 individuals
+    static constexpr int RAW_B = NB * TU_KC * 2;       // bf16 split of delta/sd
+    static constexpr int RAW = RAW_A + RAW_B;
+    static constexpr int OP_A = 128 * TU_KC * 2;
+    static constexpr int OP_B = RAW_B;
+    static constexpr int OP = OP_A + OP_B;
+    static constexpr int PIPE = 2 * OP + TU_NS * RAW;
+    static constexpr int RED = 8 * CT * 128 * 4;       // warp partials of the ra tiles
+    static constexpr size_t SMEM = 1024 + (size_t)(PIPE > RED ? PIPE : RED);
+    static_assert(OP % 1024 == 0 && RAW % 1024 == 0, "operand buffers must keep 1024-byte alignment");
+};
+
+template <int CT>
+__device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned char *base)
+{
+    using T = UpdTc<CT>;
+    constexpr int NB = T::NB;
+    __shared__ uint64_t s_bar[2];
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_err, s_nact, s_wcnt[9];
+    __shared__ int s_act[TU_MAXQ];
+    __shared__ double s_k0[CT];
+    __shared__ double s_rsw[4][CT];
+    unsigned char *op0 = base;
+    unsigned char *raw0 = base + 2 * T::OP;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ls = D.blk_ls[b];
+    const int N = D.blk_ls[b + 1] - ls;
+    const int tile = blockIdx.x, t0 = tile * 128;
+    const int nq = (N + TU_KC - 1) / TU_KC;
+
+    // stages with a non-zero delta, in subset order (nq <= 256 = blockDim)
+    {
+        bool f = false;
+        if (tid < nq) {
+            const int e = min(N, (tid + 1) * TU_KC);
+            for (int jk = tid * TU_KC; jk < e && !f; ++jk) f = D.nzflag[jk] != 0;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_wcnt[warp] = __popc(m);
+        __syncthreads();
+        if (tid == 0) {
+            int acc = 0;
+            for (int q = 0; q < 8; ++q) {
+                const int t = s_wcnt[q];
+                s_wcnt[q] = acc;
+                acc += t;
+            }
+            s_nact = acc;
+        }
+        __syncthreads();
+        if (f) s_act[s_wcnt[warp] + __popc(m & ((1u << lane) - 1u))] = tid;
+        if (tid < CT) {   // the centring term, summed over the draw tiles in order
+            double s = 0.0;
+            for (int q = 0; q < (N + TC_TM - 1) / TC_TM; ++q) s += D.k0part[(size_t)q * CT + tid];
+            s_k0[tid] = s;
+        }
+        __syncthreads();
+    }
+    const int nact = s_nact;
+    if (nact == 0) return;   // nothing changed: r, r32 and rsum stay valid
+
+    if (tid == 0) {
+        tc::mbar_init(&s_bar[0], 1);
+        tc::mbar_init(&s_bar[1], 1);
+        tc::mbar_fence_init();
+        s_err = 0;
+    }
+    if (warp == 0) tc::tmem_alloc(&s_tmem, 64);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tm = s_tmem;
+
+    auto issue = [&](int s, int buf) {
+        unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
+        const int k0 = s_act[s] * TU_KC;
+        for (int t = tid; t < TU_KC * 8; t += 256) {   // codes: 64 positions x 8 chunks of 16 individuals
+            const int kk = t >> 3, ch = t & 7;
+            unsigned char *dst = ra_ + kk * 128 + ((ch ^ ((kk >> 3) & 7)) << 4);
+            const int jk = k0 + kk;
+            if (jk < N) __pipeline_memcpy_async(dst, D.G + (size_t)(ls + jk) * D.ldx + t0 + ch * 16, 16);
+            else *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+        }
+        for (int t = tid; t < NB * 8; t += 256) {      // delta split: NB rows x 8 chunks of 8 positions
+            const int n = t >> 3, ch = t & 7;
+            __pipeline_memcpy_async(ra_ + T::RAW_A + tc::sw128_off(n, 8 * ch, NB),
+                                    D.dsplit + (size_t)n * D.ldd + k0 + 8 * ch, 16);
+        }
+        __pipeline_commit();
+    };
+
+#pragma unroll
+    for (int pp = 0; pp < TU_NS - 1; ++pp) {
+        if (pp < nact) issue(pp, pp);
+        else __pipeline_commit();
+    }
+    const uint32_t idesc = tc::idesc_bf16(128, NB);
+    const int iq_l = lane >> 3, kc = lane & 7;
+    const int rq = 4 * (4 * warp + iq_l);   // first of this thread's four individuals
+    for (int s = 0; s < nact; ++s) {
+        if (s + TU_NS - 1 < nact) issue(s + TU_NS - 1, (s + TU_NS - 1) % TU_NS);
+        else __pipeline_commit();
+        __pipeline_wait_prior(TU_NS - 1);
+        const int ob = s & 1;
+        if (s >= 2 && !tc::mbar_wait(&s_bar[ob], ((s - 2) >> 1) & 1)) s_err = 1;
+        __syncthreads();
+        const unsigned char *ra_ = raw0 + (size_t)(s % TU_NS) * T::RAW;
+        unsigned char *opa = op0 + ob * T::OP;
+        unsigned char *opb = opa + T::OP_A;
+        // transpose: positions 8kc..8kc+7 of individuals rq..rq+3 (a word per position)
+        {
+            uint32_t w[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                w[e] = *reinterpret_cast<const uint32_t *>(ra_ + (8 * kc + e) * 128 + ((warp ^ kc) << 4) + iq_l * 4);
+            uint32_t row[4][2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t a0 = __byte_perm(w[4 * h + 0], w[4 * h + 1], 0x5140u);
+                const uint32_t a1 = __byte_perm(w[4 * h + 2], w[4 * h + 3], 0x5140u);
+                const uint32_t a2 = __byte_perm(w[4 * h + 0], w[4 * h + 1], 0x7362u);
+                const uint32_t a3 = __byte_perm(w[4 * h + 2], w[4 * h + 3], 0x7362u);
+                row[0][h] = __byte_perm(a0, a1, 0x5410u);
+                row[1][h] = __byte_perm(a0, a1, 0x7632u);
+                row[2][h] = __byte_perm(a2, a3, 0x5410u);
+                row[3][h] = __byte_perm(a2, a3, 0x7632u);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                uint4 v;
+                tc::codes_to_bf16x4(row[r][0], v.x, v.y);
+                tc::codes_to_bf16x4(row[r][1], v.z, v.w);
+                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(rq + r, 8 * kc, 128)) = v;
+            }
+        }
+        for (int t = tid; t < T::OP_B / 16; t += 256)
+            reinterpret_cast<uint4 *>(opb)[t] = reinterpret_cast<const uint4 *>(ra_ + T::RAW_A)[t];
+        tc::fence_async_smem();
+        __syncthreads();
+        if (tid == 0 && !s_err) {
+            tc::fence_after_sync();
+            const uint32_t a0 = tc::smem_u32(opa), b0 = tc::smem_u32(opb);
+#pragma unroll
+            for (int kk = 0; kk < TU_KC / 16; ++kk)
+                tc::mma_bf16(tm, tc::desc_sw128(a0 + kk * 32, 1024), tc::desc_sw128(b0 + kk * 32, 1024), idesc,
+                             (s | kk) != 0 ? 1u : 0u);
+            tc::mma_commit(&s_bar[ob]);
+        }
+    }
+    __pipeline_wait_prior(0);
+    {
+        const int last = nact - 1;
+        if (!tc::mbar_wait(&s_bar[last & 1], (last >> 1) & 1)) s_err = 1;
+    }
+    __syncthreads();
+    const bool ok = !s_err;
+    if (!ok && tid == 0) flag_err(D, 4);
+    tc::fence_after_sync();
+    if (warp < 4) {
+        const int i = t0 + warp * 32 + lane;
+        float acc[NB];
+#pragma unroll
+        for (int g = 0; g < NB / 8; ++g) {
+            float v[8];
+            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + g * 8, v);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int e = 0; e < 8; ++e) acc[g * 8 + e] = v[e];
+        }
+#pragma unroll
+        for (int c = 0; c < CT; ++c) {
+            double v = 0.0;
+            if (ok && i < D.n) {
+                const size_t o = (size_t)c * D.ldr + i;
+                v = D.r[o] + ((double)((acc[c] + acc[CT + c]) + acc[2 * CT + c]) + s_k0[c]);
+                D.r[o] = v;
+                D.r32[o] = (float)v;
+            } else if (i < D.n) {
+                v = D.r[(size_t)c * D.ldr + i];
+            }
+            v = warp_sum(v);
+            if (lane == 0) s_rsw[warp][c] = v;
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tm, 64);
+    }
+    // this tile's partial sum of r (the centring of the next subset)
+    if (tid < CT)
+        D.rsum[(size_t)tid * D.nr_ctas + tile] = ((s_rsw[0][tid] + s_rsw[1][tid]) + s_rsw[2][tid]) + s_rsw[3][tid];
+}
+
+template <int CT>
+__device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, unsigned char *base)
+{
+    __shared__ int s_last;
+    float *s_red = reinterpret_cast<float *>(base);   // [8][CT][128]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ls = D.blk_ls[b];
+    const int N = D.blk_ls[b + 1] - ls;
+    const int npad = (N + 7) & ~7;
+    const int idx = blockIdx.x - D.nr_ctas;
+    const int tr = idx / ra_split, sp = idx % ra_split;
+    const int i0 = tr * 128;
+    const int kbeg = D.blk_pd[b] ? min(i0, N) : 0;   // upper triangular: rows i only meet columns k >= i
+    const int ka = kbeg + (int)(((long long)(N - kbeg) * sp) / ra_split);
+    const int kb = kbeg + (int)(((long long)(N - kbeg) * (sp + 1)) / ra_split);
+    const int ii = i0 + 4 * lane;
+    const bool rows_ok = ii + 4 <= npad;
+    float acc[4][CT];
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[e][c] = 0.0f;
+    for (int k0 = ka + warp; k0 < kb; k0 += 8 * TU_UNR) {
+        float4 u[TU_UNR];
+        int kk[TU_UNR];
+#pragma unroll
+        for (int q = 0; q < TU_UNR; ++q) {
+            const int k = k0 + 8 * q;
+            kk[q] = (k < kb && D.nzflag[k]) ? k : -1;
+            u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (kk[q] >= 0 && rows_ok) u[q] = *reinterpret_cast<const float4 *>(D.U32 + D.uoff[ls + k] + ii);
+        }
+#pragma unroll
+        for (int q = 0; q < TU_UNR; ++q) {
+            if (kk[q] < 0) continue;
+            float dl[CT];
+#pragma unroll
+            for (int c = 0; c < CT; c += 4) {
+                const float4 v = *reinterpret_cast<const float4 *>(D.delta32 + (size_t)kk[q] * CT + c);
+                dl[c] = v.x; dl[c + 1] = v.y; dl[c + 2] = v.z; dl[c + 3] = v.w;
+            }
+#pragma unroll
+            for (int c = 0; c < CT; ++c) {
+                acc[0][c] = fmaf(u[q].x, dl[c], acc[0][c]);
+                acc[1][c] = fmaf(u[q].y, dl[c], acc[1][c]);
+                acc[2][c] = fmaf(u[q].z, dl[c], acc[2][c]);
+                acc[3][c] = fmaf(u[q].w, dl[c], acc[3][c]);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < CT; ++c)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) s_red[(warp * CT + c) * 128 + 4 * lane + e] = acc[e][c];
+    __syncthreads();
+    float *part = D.rapart + ((size_t)(tr * ra_split + sp) * CT) * 128;
+    if (tid < 128) {
+        for (int c = 0; c < CT; ++c) {
+            float s = 0.0f;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) s += s_red[(w * CT + c) * 128 + tid];
+            part[c * 128 + tid] = s;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&D.raticket[tr], 1) == ra_split - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int i = i0 + tid;
+    if (tid < 128 && i < D.bs) {
+        for (int c = 0; c < CT; ++c) {
+            float s = 0.0f;
+            for (int q = 0; q < ra_split; ++q) s += __ldcg(D.rapart + ((size_t)(tr * ra_split + q) * CT + c) * 128 + tid);
+            const size_t o = (size_t)c * D.ldra + i;
+            const double v = D.ra[o] + (double)s;
+            D.ra[o] = v;
+            D.ra32[o] = (float)v;
+        }
+    }
+    if (tid == 0) D.raticket[tr] = 0;
+}
+
+template <int CT>
+__global__ void __launch_bounds__(256, 2) k_update_tc(Dev D, int b, int ra_split)
+{
+    extern __shared__ __align__(1024) unsigned char smem_dyn[];
+    unsigned char *base = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
+    if ((int)blockIdx.x < D.nr_ctas) update_tc_rows<CT>(D, b, base);
+    else update_tc_ra<CT>(D, b, ra_split, base);
+}
+
+}  // namespace soda
