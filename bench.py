@@ -216,16 +216,16 @@ def bench_ours(args, rank, ws):
     res["clocks"] = clk.summary()
     res["included_at_timing"] = st["included"]
     nb = spec.p // BLOCKSIZE
-    rhs_ms = prof["rhs_draw"][0] / prof["rhs_draw"][1]
+    rhs_ms = prof["rhs"][0] / prof["rhs"][1]
     hbm, peak_kind = _peaks()
     bytes_rhs = _rhs_bytes(spec.n, BLOCKSIZE, C, "fp8")
     achieved = bytes_rhs / (rhs_ms / 1000.0) / 1e9
-    res["roofline"] = {"bound": "hbm", "kernel": "k_rhs_draw<FP8,%d>" % C, "achieved": round(achieved, 1),
+    res["roofline"] = {"bound": "hbm", "kernel": "k_rhs_tc<%d>" % C, "achieved": round(achieved, 1),
                        "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
                        "peak_source": peak_kind, "bytes_per_launch": bytes_rhs,
                        "launch_ms": round(rhs_ms, 5),
                        "kernel_ms_per_iter": {k: round(v[0] / 2, 4) for k, v in prof.items()}}
-    res["gpu_launches"] = K * (3 + 2 * nb + 5)
+    res["gpu_launches"] = K * (3 + 3 * nb + 5)   # mu; rhs, draws, update per subset; hyper/stats/recal
 
     # ---- plain FP32 path (1 chain), same timing -----------------------------------
     job = _make_job(spec, codes, y, "fp32", 1, 77 + rank)

@@ -214,9 +214,9 @@ int sodagpu_timings(sodagpu_ctx *ctx, double *build_z_s, double *run_s, double *
 /* Measurement hook: runs `iters` iterations (advancing the chains exactly like
  * sodagpu_run) with kernels launched one by one and a CUDA-event pair around
  * each launch.  ms[c] receives the summed device time and launches[c] the
- * launch count of kernel class c: 0 rhs + per-SNP draws, 1 residual update,
- * 2 mu draw, 3 hyper-parameter draws and accumulators. */
-#define SODAGPU_NPROF 4
+ * launch count of kernel class c: 0 rhs products, 1 residual update,
+ * 2 mu draw, 3 hyper-parameter draws and accumulators, 4 per-SNP draws. */
+#define SODAGPU_NPROF 5
 int sodagpu_profile_kernels(sodagpu_ctx *ctx, int32_t iters, double *ms, int32_t *launches);
 
 /* Genomic values pred = mu + X*effects for callers that cannot let this

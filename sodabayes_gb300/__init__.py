@@ -309,11 +309,11 @@ class SodaJob:
 
     def profile_kernels(self, iters: int) -> dict:
         """Per-kernel-class device time (ms) and launch counts over `iters` eager iterations."""
-        ms = np.zeros(4)
-        n = np.zeros(4, dtype=np.int32)
+        names = ("rhs", "update", "mu", "other", "draw")
+        ms = np.zeros(len(names))
+        n = np.zeros(len(names), dtype=np.int32)
         _check(self._lib.sodagpu_profile_kernels(self._ctx, int(iters), _dp(ms), _ip(n)), "sodagpu_profile_kernels")
-        names = ("rhs_draw", "update", "mu", "other")
-        return {names[k]: (float(ms[k]), int(n[k])) for k in range(4)}
+        return {names[k]: (float(ms[k]), int(n[k])) for k in range(len(names))}
 
 
 def predict(codes=None, freq=None, mu: float = 0.0, effects=None, bed: Optional[np.ndarray] = None,

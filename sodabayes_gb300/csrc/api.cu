@@ -113,7 +113,7 @@ struct sodagpu_ctx {
     RunCtl *ctl = nullptr;
     double *delta = nullptr, *rpart = nullptr, *rsum = nullptr, *statpart = nullptr, *recal_part = nullptr,
            *upart = nullptr, *rpx = nullptr, *rpu = nullptr;
-    int32_t *cntpart = nullptr, *ucount = nullptr, *rticket = nullptr;
+    int32_t *cntpart = nullptr, *ucount = nullptr;
     uint8_t *nzflag = nullptr;
     int tc = 0, ldd = 0;                 // tensor-core sweep
     uint16_t *dsplit = nullptr;
@@ -709,7 +709,6 @@ int build_dev(sodagpu_ctx *c)
     D.recal_part = c->recal_part;
     D.rpx = c->rpx;
     D.rpu = c->rpu;
-    D.rticket = c->rticket;
     D.tc = c->tc;
     D.ldd = c->ldd;
     D.dsplit = c->dsplit;
@@ -751,13 +750,12 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         TRY(c->alloc(&c->recal_part, (size_t)C * RECAL_SPLIT * c->ldr));
         TRY(c->alloc(&c->rpx, (size_t)RHS_KSPLIT_MAX * C * c->bs));
         TRY(c->alloc(&c->rpu, (size_t)RHS_KSPLIT_MAX * C * c->bs));
-        TRY(c->alloc(&c->rticket, c->bs));
         c->tc = c->cfg.kernels == SODAGPU_KERNELS_AUTO && sweep_tc_supported(c->cfg.precision, C, c->bs);
         if (c->tc) {
             const int mt = (c->bs + 127) / 128;
             c->ldd = (int)round_up((size_t)c->bs, 128);
             TRY(c->alloc(&c->dsplit, (size_t)sweep_tc_rows(C) * c->ldd));
-            TRY(c->alloc(&c->k0part, (size_t)mt * C));
+            TRY(c->alloc(&c->k0part, (((size_t)c->ldd * C + 255) / 256) * C));
             TRY(c->alloc(&c->rapart, (size_t)mt * sweep_tc_ra_split() * C * 128));
             TRY(c->alloc(&c->raticket, mt));
         }

@@ -1,5 +1,6 @@
-// rhs_kernel.cuh — right-hand sides of one SODA subset and the per-SNP draws
-// (models.f90:146-162, 211-256, 350-413), included by sweep.cu.
+// rhs_kernel.cuh — right-hand sides of one SODA subset (models.f90:154) on
+// the FP32/FP64 cores, and the per-SNP draws (models.f90:146-162, 211-256,
+// 350-413), included by sweep.cu.
 //
 //   rhs[j][c] = x_j' r_c + u_j' ra_c (+ d g_j)
 //
@@ -10,10 +11,10 @@
 // stages (codes or FP32 columns with r) first, then augmenting-matrix stages
 // (U columns with ra; the factor is upper triangular, so a tile needs only
 // the rows up to its last column) — keeping an SPT x CT accumulator block per
-// thread.  Partial sums go to scratch; the last CTA of an M tile to finish
-// (atomic ticket, no waiting) adds them in split order and performs that
-// tile's draws.  FP8 mode: codes 0/1/2 are exact in FP32 and the centring is
-// applied once per SNP, x'r = (G'r)/sd - 2p/sd * sum(r).
+// thread.  Partial sums go to scratch (one slice per K split), which k_draw
+// adds in split order before the draws.  FP8 mode: codes 0/1/2 are exact in
+// FP32 and the centring is applied once per SNP, x'r = (G'r)/sd - 2p/sd *
+// sum(r).
 #pragma once
 #include <cuda_pipeline_primitives.h>
 
@@ -74,97 +75,121 @@ __device__ __forceinline__ float code_to_f32(uint32_t w, int k)
     return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k)) - 8388608.0f;
 }
 
-// Ends one CTA of an M tile of `mts` SNPs whose split partial sums are in
-// rpx/rpu.  The last CTA of the tile to arrive (atomic ticket, no waiting)
-// adds the partial sums in split order and draws the tile's SNPs (256
-// threads).  With TC, it also writes what the tensor-core update reads: the
-// bf16 three-way split of delta/sd per chain (dsplit, zero past the subset's
-// end) and the tile's share of sum_j x0_j delta_j (k0part).
+// Per-SNP draws of one subset (models.f90:146-162, 211-256, 350-413) after
+// the rhs kernel left its split partial sums in rpx/rpu: one thread per
+// (SNP, chain) pair, chains of a SNP in consecutive lanes (CT divides 32).
+// Every load a draw needs is issued up front: the SNP's metadata and state,
+// and the partial sums of all splits at once (added in split order).  With
+// TC the kernel also writes what the tensor-core update reads: the bf16
+// three-way split of delta/sd per chain (dsplit; pairs up to `span`, past the
+// subset's end, write zeros) and per-CTA sums of x0_j delta_j (k0part).
 template <int MODE, int CT, bool TC>
-__device__ void rhs_finish(const Dev &D, int b, int mt, int ksplit, int j0, int mts)
+__global__ void __launch_bounds__(256) k_draw(Dev D, int b, int ksplit, int span)
 {
-    __shared__ int s_last;
-    __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring), once per CTA
+    __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring)
+    __shared__ double s_k[256];
     const int tid = threadIdx.x, lane = tid & 31;
+    const int t = blockIdx.x * 256 + tid;
+    const int jl = t / CT, c = t % CT;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&D.rticket[mt], 1) == ksplit - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    // the last CTA of the M tile: totals in split order, then the draws
-    const int rep = cur_rep(D);
-    const double zz = D.xxd[b];
-    const int cnt = min(mts, N - j0);
+    const bool act = jl < N;
+    const int k = ls + (act ? jl : 0);
+    const int snp = act && !D.skip[k] ? D.perm[k] : -1;
+    double inv = 0.0, x0 = 0.0, gold = 0.0;
+    int cl = 0;
+    if (snp >= 0) {
+        if (MODE == SODAGPU_FP8 || TC) {
+            inv = D.xv[(size_t)k * 4 + 3];
+            x0 = D.xv[(size_t)k * 4 + 0];
+        }
+        if (MODE != SODAGPU_FP64) {
+            gold = D.g[(size_t)c * D.p + snp];
+            cl = D.cls[(size_t)c * D.p + snp];
+        }
+    }
+    double xr = 0.0, ur = 0.0;
+    if (snp >= 0) {
+        double px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
+#pragma unroll
+        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+            if (sp < ksplit) {
+                const size_t o = ((size_t)sp * CT + c) * D.bs + jl;
+                px[sp] = __ldcg(D.rpx + o);
+                pu[sp] = __ldcg(D.rpu + o);
+            }
+        }
+#pragma unroll
+        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+            if (sp < ksplit) {
+                xr += px[sp];
+                ur += pu[sp];
+            }
+        }
+    }
     if (MODE == SODAGPU_FP8) {
+        // sum(r) per chain: 256/CT threads per chain over interleaved row tiles, then in part order
+        constexpr int PARTS = 256 / CT;
+        const int cc = tid / PARTS, part = tid % PARTS;
+        double a = 0.0;
+        for (int q0 = part; q0 < D.nr_ctas; q0 += 4 * PARTS) {
+            double v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int q = q0 + u * PARTS;
+                v[u] = q < D.nr_ctas ? D.rsum[(size_t)cc * D.nr_ctas + q] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a += v[u];
+        }
+        s_k[tid] = a;
+        __syncthreads();
         if (tid < CT) {
-            double rs = 0.0;
-            for (int q = 0; q < D.nr_ctas; ++q) rs += D.rsum[(size_t)tid * D.nr_ctas + q];
-            s_rs[tid] = rs;
+            double tt = 0.0;
+            for (int q = 0; q < PARTS; ++q) tt += s_k[tid * PARTS + q];
+            s_rs[tid] = tt;
         }
         __syncthreads();
     }
-    const int span = TC ? mts : cnt;   // the tensor path also clears the tile's columns past the subset
-    for (int t = tid; t < ((span * CT + 31) & ~31); t += blockDim.x) {
-        const int jl = t / CT, c = t % CT;
-        const int jk = j0 + jl;
-        const bool act = jl < cnt;
-        double delta = 0.0;
-        if (act) {
-            const int k = ls + jk;
-            if (!D.skip[k]) {
-                double xr = 0.0, ur = 0.0;
-                for (int sp = 0; sp < ksplit; ++sp) {
-                    const size_t o = ((size_t)sp * CT + c) * D.bs + jk;
-                    xr += __ldcg(D.rpx + o);
-                    ur += __ldcg(D.rpu + o);
-                }
-                if (MODE == SODAGPU_FP8) xr = xr * D.xv[(size_t)k * 4 + 3] + D.xv[(size_t)k * 4 + 0] * s_rs[c];
-                const ChainScal *S = &D.scal[c];
-                CRng R;
-                crng_init(R, D.seed, c, rep, D.perm[k], P_SNP);
-                int err = 0;
-                if (MODE == SODAGPU_FP64)
-                    delta = draw_snp(D, S, c, rep, D.perm[k], xr + ur, zz, zz / S->vare, R, &err);
-                else
-                    delta = draw_snp_f(D, S, c, D.perm[k], (float)(xr + ur), (float)zz, (float)(zz / S->vare), R,
-                                       &err);
-                if (err) flag_err(D, 1);
-            }
-            D.delta[(size_t)c * D.bs + jk] = delta;
-            if (MODE != SODAGPU_FP64) D.delta32[(size_t)jk * CT + c] = (float)delta;   // chain-contiguous
-        }
-        if (TC && jl < mts) {
-            uint32_t hi = 0, mid = 0, lo = 0;
-            if (act && delta != 0.0) tc::split3((float)(delta * D.xv[(size_t)(ls + jk) * 4 + 3]), hi, mid, lo);
-            D.dsplit[(size_t)c * D.ldd + jk] = (uint16_t)hi;
-            D.dsplit[(size_t)(CT + c) * D.ldd + jk] = (uint16_t)mid;
-            D.dsplit[(size_t)(2 * CT + c) * D.ldd + jk] = (uint16_t)lo;
-        }
-        // chains of one SNP are CT consecutive lanes (CT divides 32)
-        const unsigned m = __ballot_sync(0xffffffffu, act && delta != 0.0);
-        const unsigned grp = CT >= 32 ? 0xffffffffu : (((1u << CT) - 1u) << ((lane / CT) * CT));
-        if (act && c == 0) D.nzflag[jk] = (m & grp) != 0u;
+    double delta = 0.0;
+    if (snp >= 0) {
+        if (MODE == SODAGPU_FP8) xr = xr * inv + x0 * s_rs[c];
+        const ChainScal *S = &D.scal[c];
+        const double zz = D.xxd[b];
+        CRng R;
+        crng_init(R, D.seed, c, cur_rep(D), snp, P_SNP);
+        int err = 0;
+        if (MODE == SODAGPU_FP64)
+            delta = draw_snp(D, S, c, cur_rep(D), snp, xr + ur, zz, zz / S->vare, R, &err);
+        else
+            delta = draw_snp_f(D, S, c, snp, (float)(xr + ur), (float)zz, (float)(zz / S->vare), R, &err, gold, cl);
+        if (err) flag_err(D, 1);
+    }
+    if (act) {
+        D.delta[(size_t)c * D.bs + jl] = delta;
+        if (MODE != SODAGPU_FP64) D.delta32[(size_t)jl * CT + c] = (float)delta;   // chain-contiguous
     }
     if (TC) {
-        // k0part[mt][c] = sum over the tile of x0_j delta_j (fixed order)
-        __shared__ double s_k0[256];
-        __syncthreads();   // this CTA's delta stores are visible to the block
-        const int c = tid % CT, part = tid / CT, nparts = blockDim.x / CT;
-        double a = 0.0;
-        for (int jl = part; jl < cnt; jl += nparts)
-            a += D.xv[(size_t)(ls + j0 + jl) * 4 + 0] * D.delta[(size_t)c * D.bs + j0 + jl];
-        s_k0[tid] = a;
+        if (jl < span) {
+            uint32_t hi = 0, mid = 0, lo = 0;
+            if (delta != 0.0) tc::split3((float)(delta * inv), hi, mid, lo);
+            D.dsplit[(size_t)c * D.ldd + jl] = (uint16_t)hi;
+            D.dsplit[(size_t)(CT + c) * D.ldd + jl] = (uint16_t)mid;
+            D.dsplit[(size_t)(2 * CT + c) * D.ldd + jl] = (uint16_t)lo;
+        }
+        // this CTA's sum of x0_j delta_j per chain, SNPs in order
+        __syncthreads();
+        s_k[tid] = x0 * delta;
         __syncthreads();
         if (tid < CT) {
-            double s = 0.0;
-            for (int q = 0; q < nparts; ++q) s += s_k0[q * CT + tid];
-            D.k0part[(size_t)mt * CT + tid] = s;
+            double tt = 0.0;
+            for (int q = 0; q < 256 / CT; ++q) tt += s_k[q * CT + tid];
+            D.k0part[(size_t)blockIdx.x * CT + tid] = tt;
         }
     }
-    if (tid == 0) D.rticket[mt] = 0;
+    const unsigned m = __ballot_sync(0xffffffffu, act && delta != 0.0);
+    const unsigned grp = CT >= 32 ? 0xffffffffu : (((1u << CT) - 1u) << ((lane / CT) * CT));
+    if (act && c == 0) D.nzflag[jl] = (m & grp) != 0u;
 }
 
 template <int MODE, int CT>
@@ -404,7 +429,6 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     if (nv == ng) publish(false);   // no augmenting stage in this split
     publish(true);
 
-    rhs_finish<MODE, CT, false>(D, b, mt, ksplit, j0, MTS);
 }
 
 }  // namespace soda

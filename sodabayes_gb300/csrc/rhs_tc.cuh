@@ -15,9 +15,7 @@
 // a double-buffered 128-byte-swizzled operand buffer, and one thread issues
 // eight K=16 MMAs whose completion an mbarrier reports when the operand buffer
 // is needed again.  The augmenting part u_j' ra_c (5% of the work) runs on
-// the FP32 cores.  Partial sums, the ticket and the draws are those of
-// rhs_finish; the last CTA of a tile also leaves the bf16 split of delta/sd
-// for the tensor-core update.
+// the FP32 cores.  Partial sums go to rpx/rpu, added and drawn by k_draw.
 #pragma once
 
 namespace soda {
@@ -25,7 +23,7 @@ namespace soda {
 constexpr int TC_TM = 128;   // SNPs per M tile
 constexpr int TC_KC = 128;   // individuals per stage
 constexpr int TC_NS = 4;     // raw stages in flight
-constexpr int TC_UW = 1024;  // augmented rows per ra staging window
+constexpr int TC_UWR = 256;  // augmented rows per staging window of the U part
 
 template <int CT>
 struct RhsTc {
@@ -38,9 +36,51 @@ struct RhsTc {
     static constexpr int OP = OP_A + OP_B;
     static constexpr size_t SMEM = 1024 + 2 * (size_t)OP + (size_t)TC_NS * RAW;
     static_assert(OP % 1024 == 0, "operand buffers must keep 1024-byte alignment");
-    static_assert((size_t)CT * TC_UW * 4 <= (size_t)TC_NS * RAW, "ra window must fit the raw buffers");
-    static_assert((size_t)TC_TM * CT * 4 <= 2 * (size_t)OP, "u partials must fit the operand buffers");
+    // U part: a window of the tile's 128 U columns and the chains' ra, plus the partial sums
+    static constexpr size_t UPART = (size_t)(TC_TM + CT) * TC_UWR * 4 + (size_t)TC_TM * CT * 4;
+    static_assert(UPART <= 2 * (size_t)OP + (size_t)TC_NS * RAW, "U window must fit the pipeline buffers");
 };
+
+// Transposing butterfly: V values per lane summed over the warp's 32 lanes.
+// Each round with CNT > 1 exchanges half of the values with lane ^ OFF and
+// keeps the other half (upper half when lane & OFF); once one value is left
+// the remaining rounds add it across lanes.  Afterwards a lane holds the
+// totals of values xreduce_base(lane) + 0 .. FIN-1 (FIN = V/32, or 1 with
+// V < 32, where lanes differing in the low bits hold the same totals).
+template <int CNT, int OFF, int V>
+__device__ __forceinline__ void xreduce_round(float (&v)[V], int lane)
+{
+    if constexpr (OFF >= 1) {
+        if constexpr (CNT > 1) {
+            constexpr int H = CNT / 2;
+            const bool up = (lane & OFF) != 0;
+#pragma unroll
+            for (int i = 0; i < H; ++i) {
+                const float send = up ? v[i] : v[i + H];
+                const float keep = up ? v[i + H] : v[i];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, send, OFF);
+            }
+            xreduce_round<H, OFF / 2, V>(v, lane);
+        } else {
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], OFF);
+            xreduce_round<1, OFF / 2, V>(v, lane);
+        }
+    }
+}
+
+template <int V>
+__device__ __forceinline__ int xreduce_base(int lane)
+{
+    int base = 0, cnt = V;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        if (cnt > 1) {
+            cnt >>= 1;
+            if (lane & off) base += cnt;
+        }
+    }
+    return base;
+}
 
 template <int CT>
 __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
@@ -139,16 +179,14 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
             const int c = t / (TC_KC / 8), q = t % (TC_KC / 8);
             const float4 a = *reinterpret_cast<const float4 *>(ra_ + T::RAW_A + c * 512 + q * 32);
             const float4 bq = *reinterpret_cast<const float4 *>(ra_ + T::RAW_A + c * 512 + q * 32 + 16);
-            const float v[8] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w};
-            uint32_t h[8], md[8], l[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) tc::split3(v[e], h[e], md[e], l[e]);
-            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(c, 8 * q, NB)) =
-                make_uint4(h[0] | h[1] << 16, h[2] | h[3] << 16, h[4] | h[5] << 16, h[6] | h[7] << 16);
-            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(CT + c, 8 * q, NB)) =
-                make_uint4(md[0] | md[1] << 16, md[2] | md[3] << 16, md[4] | md[5] << 16, md[6] | md[7] << 16);
-            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(2 * CT + c, 8 * q, NB)) =
-                make_uint4(l[0] | l[1] << 16, l[2] | l[3] << 16, l[4] | l[5] << 16, l[6] | l[7] << 16);
+            uint4 h, md, l;
+            tc::split3x2(a.x, a.y, h.x, md.x, l.x);
+            tc::split3x2(a.z, a.w, h.y, md.y, l.y);
+            tc::split3x2(bq.x, bq.y, h.z, md.z, l.z);
+            tc::split3x2(bq.z, bq.w, h.w, md.w, l.w);
+            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(c, 8 * q, NB)) = h;
+            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(CT + c, 8 * q, NB)) = md;
+            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(2 * CT + c, 8 * q, NB)) = l;
         }
         tc::fence_async_smem();
         __syncthreads();
@@ -208,56 +246,63 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
     }
 
     // augmenting part on the FP32 cores: this split's share of the U rows of
-    // the tile's columns (upper triangular: rows up to the tile's last column)
+    // the tile's columns (upper triangular: rows up to the tile's last
+    // column), staged by windows of TC_UWR rows with cp.async; warp w owns
+    // columns 16w..16w+15 (four at a time), lanes run over rows, and the
+    // 4 x CT lane sums are reduced by a transposing butterfly.
     const int npad = (N + 7) & ~7;
     const int rowsU = D.blk_pd[b] ? min(npad, j0 + TC_TM) : npad;
     const int nUc = (rowsU + 31) / 32;
     const int l0 = 32 * (int)(((long long)nUc * ks) / ksplit);
     const int l1 = min(rowsU, 32 * (int)(((long long)nUc * (ks + 1)) / ksplit));
-    float *s_u = reinterpret_cast<float *>(op0);     // [TC_TM][CT] partial u'ra
-    float *s_ra = reinterpret_cast<float *>(raw0);   // [CT][TC_UW] window of ra
+    float *sU = reinterpret_cast<float *>(base);      // [TC_TM][TC_UWR]
+    float *sRa = sU + TC_TM * TC_UWR;                 // [CT][TC_UWR]
+    float *s_u = sRa + CT * TC_UWR;                   // [TC_TM][CT]
     for (int t = tid; t < TC_TM * CT; t += 256) s_u[t] = 0.0f;
-    for (int w0 = l0; w0 < l1; w0 += TC_UW) {
-        const int len = min(TC_UW, l1 - w0);
+    for (int w0 = l0; w0 < l1; w0 += TC_UWR) {
+        const int len = min(TC_UWR, l1 - w0);        // a multiple of 8
         __syncthreads();
-        for (int t = tid; t < CT * len; t += 256) {
-            const int c = t / len, l = t % len;
-            s_ra[c * TC_UW + l] = D.ra32[(size_t)c * D.ldra + w0 + l];
+        for (int t = tid; t < TC_TM * (len / 4); t += 256) {
+            const int jj = t / (len / 4), q = t % (len / 4);
+            const int jk = j0 + jj;
+            float *dst = sU + jj * TC_UWR + 4 * q;
+            if (jk < N) __pipeline_memcpy_async(dst, D.U32 + D.uoff[ls + jk] + w0 + 4 * q, 16);
+            else *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        for (int t = tid; t < CT * (len / 4); t += 256) {
+            const int c = t / (len / 4), q = t % (len / 4);
+            __pipeline_memcpy_async(sRa + c * TC_UWR + 4 * q, D.ra32 + (size_t)c * D.ldra + w0 + 4 * q, 16);
+        }
+        __pipeline_commit();
+        __pipeline_wait_prior(0);
         __syncthreads();
-        // warp w: tile columns 16w .. 16w+15, four at a time; lanes over rows
 #pragma unroll 1
         for (int g = 0; g < 4; ++g) {
             const int jq = warp * 16 + g * 4;
-            float acc[4][CT];
+            float acc[4 * CT];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int c = 0; c < CT; ++c) acc[q][c] = 0.0f;
-            const float *ucol[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int jk = j0 + jq + q;
-                ucol[q] = jk < N ? D.U32 + D.uoff[ls + jk] + w0 : nullptr;
-            }
+            for (int v = 0; v < 4 * CT; ++v) acc[v] = 0.0f;
             for (int l = lane; l < len; l += 32) {
                 float u[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) u[q] = ucol[q] ? ucol[q][l] : 0.0f;
+                for (int q = 0; q < 4; ++q) u[q] = sU[(jq + q) * TC_UWR + l];
 #pragma unroll
                 for (int c = 0; c < CT; ++c) {
-                    const float rv = s_ra[c * TC_UW + l];
+                    const float rv = sRa[c * TC_UWR + l];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[q][c] = fmaf(u[q], rv, acc[q][c]);
+                    for (int q = 0; q < 4; ++q) acc[q * CT + c] = fmaf(u[q], rv, acc[q * CT + c]);
                 }
             }
+            xreduce_round<4 * CT, 16>(acc, lane);
+            constexpr int FIN = 4 * CT >= 32 ? 4 * CT / 32 : 1;
+            const int vb = xreduce_base<4 * CT>(lane);
+            if (4 * CT >= 32 || (lane & (32 / (4 * CT) - 1)) == 0) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int c = 0; c < CT; ++c) {
-                    const float v = warp_sumf(acc[q][c]);
-                    if (lane == 0) s_u[(jq + q) * CT + c] += v;
+                for (int f = 0; f < FIN; ++f) {
+                    const int v = vb + f;
+                    s_u[(jq + v / CT) * CT + v % CT] += acc[f];
                 }
+            }
         }
     }
     __syncthreads();
@@ -265,7 +310,6 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
         const int m = t / CT, c = t % CT, jk = j0 + m;
         if (jk < N) D.rpu[((size_t)ks * CT + c) * D.bs + jk] = (double)s_u[t];
     }
-    rhs_finish<SODAGPU_FP8, CT, true>(D, b, mt, ksplit, j0, TC_TM);
 }
 
 }  // namespace soda

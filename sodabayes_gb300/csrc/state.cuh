@@ -106,12 +106,11 @@ struct Dev {
     int32_t *cntpart;          // [C][NSTAT][ngroup*nmix] counts
     double *recal_part;        // [C][RECAL_SPLIT][ldr]
     double *rpx, *rpu;         // [RHS_KSPLIT_MAX][C][bs] rhs partial sums (genotype / augmented part)
-    int32_t *rticket;          // [bs] rhs tickets per M tile (self-resetting)
     // tensor-core sweep (FP8 mode, 4/8/16 chains)
     int tc;                    // 1 when the tensor-core kernels run
     int ldd;                   // row stride of dsplit (bs rounded up to 128)
     uint16_t *dsplit;          // [round_up(3C,16)][ldd] bf16 hi/mid/lo of delta/sd per chain
-    double *k0part;            // [M tiles][C] per-tile sums of x0_j delta_j
+    double *k0part;            // [draw CTAs][C] per-CTA sums of x0_j delta_j
     float *rapart;             // [ra tiles][TU_RA_SPLIT][C][128] ra update partial sums
     int32_t *raticket;         // [ra tiles] ra update tickets (self-resetting)
 };

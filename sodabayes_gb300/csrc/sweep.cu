@@ -152,12 +152,13 @@ __device__ double draw_snp(const Dev &D, const ChainScal *S, int c, int rep, int
 // The same draw in FP32 arithmetic, for the FP32/FP8 sweeps: GB300 executes
 // FP64 at a small fraction of its FP32 rate, and the draws of a subset sit on
 // the critical path of every subset.  State stays FP64.
+// gold = g and cl = class of the SNP in this chain, loaded by the caller
+// ahead of the draw (they sit on the draw's critical path).
 __device__ double draw_snp_f(const Dev &D, const ChainScal *S, int c, int snploc, float rhs, float zz,
-                             float zz_vare, CRng &R, int *err)
+                             float zz_vare, CRng &R, int *err, double gold, int cl)
 {
     const size_t o = (size_t)c * D.p + snploc;
     const float vare = (float)S->vare;
-    const double gold = D.g[o];
     float gk = (float)gold;
     const int m = D.method;
     const float df_va = (float)D.df_va, scale_va = (float)S->scale_va;
@@ -171,7 +172,6 @@ __device__ double draw_snp_f(const Dev &D, const ChainScal *S, int c, int snploc
         D.vara_s[o] = (double)d_rscinvchi2_f(df_va + 1.0f, scale, R, err);
         return gold - (double)gk;
     }
-    const int cl = D.cls[o];
     if (cl > 1) rhs = rhs + zz * gk;
     const int ng = D.ngroup;
     if (m == SODAGPU_BAYES_B) {
@@ -787,6 +787,11 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
         ProfScope ps(prof, st, PROF_RHS);
         k_rhs_tc<CT><<<mtiles * ks, 256, RhsTc<CT>::SMEM, st>>>(D, b, ks);
     }
+    {
+        const int span = mtiles * TC_TM;
+        ProfScope ps(prof, st, PROF_DRAW);
+        k_draw<SODAGPU_FP8, CT, true><<<(span * CT + 255) / 256, 256, 0, st>>>(D, b, ks, span);
+    }
     const int ra_tiles = (nblk_snps + 127) / 128;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
@@ -811,6 +816,10 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
     {
         ProfScope ps(prof, st, PROF_RHS);
         k_rhs<MODE, CT><<<mtiles * ks, 256, rhs_smem_bytes<MODE, CT>(), st>>>(D, b, ks);
+    }
+    {
+        ProfScope ps(prof, st, PROF_DRAW);
+        k_draw<MODE, CT, false><<<(nblk_snps * CT + 255) / 256, 256, 0, st>>>(D, b, ks, nblk_snps);
     }
     const int ntile = D.nr_ctas + (D.bs + UT - 1) / UT;
     {

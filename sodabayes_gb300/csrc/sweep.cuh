@@ -14,8 +14,8 @@ int sweep_tc_rows(int chains);
 int sweep_tc_ra_split();
 // Optional per-launch event recording (eager profiling, never inside a graph):
 // before/after every launch an event pair is recorded and its kernel class
-// stored.  Classes: 0 rhs+draw, 1 residual update, 2 mu, 3 everything else.
-enum { PROF_RHS = 0, PROF_UPDATE = 1, PROF_MU = 2, PROF_OTHER = 3, PROF_NCLASS = 4 };
+// stored.  Classes: 0 rhs, 1 residual update, 2 mu, 3 everything else, 4 draws.
+enum { PROF_RHS = 0, PROF_UPDATE = 1, PROF_MU = 2, PROF_OTHER = 3, PROF_DRAW = 4, PROF_NCLASS = 5 };
 struct ProfHook {
     cudaEvent_t *ev;   // 2 * cap events
     int *cls;          // cap classes

@@ -170,17 +170,39 @@ __device__ __forceinline__ void split3(float x, uint32_t &hi, uint32_t &mid, uin
 }
 
 // Four genotype codes (bytes, each 0..2) -> two words of two bf16 each:
-// w01 = bf16(b0) | bf16(b1) << 16, w23 likewise.  bf16(0) = 0x0000,
-// bf16(1) = 0x3F80, bf16(2) = 0x4000: the codes select the high and low
-// bytes from two small tables.
+// w01 = bf16(b0) | bf16(b1) << 16, w23 likewise.  Each code goes into the
+// mantissa of bf16 0x43cc = 128 + c, and one packed bf16 subtraction of 128
+// (exact) leaves c.
+__device__ __forceinline__ uint32_t bf16x2_sub128(uint32_t x)
+{
+    uint32_t r;
+    asm("sub.rn.bf16x2 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(0x43004300u));
+    return r;
+}
+
 __device__ __forceinline__ void codes_to_bf16x4(uint32_t w, uint32_t &w01, uint32_t &w23)
 {
-    const uint32_t t = w | (w >> 4);                            // nibbles b0 b1 in byte 0, b2 b3 in byte 2
-    const uint32_t sel = (t & 0xFFu) | ((t >> 8) & 0xFF00u);    // selector nibbles b0 b1 b2 b3
-    const uint32_t hb = __byte_perm(0x00403F00u, 0u, sel);      // high bytes
-    const uint32_t lb = __byte_perm(0x00008000u, 0u, sel);      // low bytes
-    w01 = __byte_perm(lb, hb, 0x5140u);
-    w23 = __byte_perm(lb, hb, 0x7362u);
+    w01 = bf16x2_sub128(__byte_perm(w, 0x43u, 0x4140u));
+    w23 = bf16x2_sub128(__byte_perm(w, 0x43u, 0x4342u));
+}
+
+// (bf16(b) << 16) | bf16(a), round to nearest even
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
+{
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+    return r;
+}
+
+// (a, b) ~ hi + mid + lo elementwise, three packed bf16 pairs (about 24
+// significant bits together)
+__device__ __forceinline__ void split3x2(float a, float b, uint32_t &hi, uint32_t &mid, uint32_t &lo)
+{
+    hi = pack_bf16x2(a, b);
+    const float ra = a - __uint_as_float(hi << 16), rb = b - __uint_as_float(hi & 0xFFFF0000u);
+    mid = pack_bf16x2(ra, rb);
+    const float sa = ra - __uint_as_float(mid << 16), sb = rb - __uint_as_float(mid & 0xFFFF0000u);
+    lo = pack_bf16x2(sa, sb);
 }
 
 }  // namespace tc

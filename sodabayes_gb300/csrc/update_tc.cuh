@@ -8,9 +8,9 @@
 // Row tiles of r (128 individuals, one CTA each) run on tcgen05: A = the
 // tile's codes of 64 subset positions per stage, transposed to individual-major
 // bf16 in shared memory, B = the three-way bf16 split of delta/sd written by
-// the draws (rhs_finish), D = 128 x 3*chains FP32 in tensor memory.  Stages
+// the draws (k_draw), D = 128 x 3*chains FP32 in tensor memory.  Stages
 // whose 64 positions have no non-zero delta in any chain are skipped.  The
-// centring term sum_j x0_j delta_j is added in FP64 from the per-tile sums of
+// centring term sum_j x0_j delta_j is added in FP64 from the per-CTA sums of
 // the draws.  The augmented rows ra (U_b is FP32, one tile of 128 rows per
 // ra_split CTAs over column ranges) run on the FP32 cores; the last CTA of a
 // row tile adds the split partial sums in split order (deterministic).
@@ -49,6 +49,7 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
     __shared__ int s_err, s_nact, s_wcnt[9];
     __shared__ int s_act[TU_MAXQ];
     __shared__ double s_k0[CT];
+    __shared__ double s_k0p[256];
     __shared__ double s_rsw[4][CT];
     unsigned char *op0 = base;
     unsigned char *raw0 = base + 2 * T::OP;
@@ -62,11 +63,29 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
     {
         bool f = false;
         if (tid < nq) {
-            const int e = min(N, (tid + 1) * TU_KC);
-            for (int jk = tid * TU_KC; jk < e && !f; ++jk) f = D.nzflag[jk] != 0;
+            const int jb = tid * TU_KC, e = min(N, jb + TU_KC);
+            if (e - jb == TU_KC) {   // full stage: four 16-byte loads
+                const uint4 *q = reinterpret_cast<const uint4 *>(D.nzflag + jb);
+                const uint4 a = q[0], bq = q[1], c2 = q[2], d2 = q[3];
+                f = ((a.x | a.y | a.z | a.w) | (bq.x | bq.y | bq.z | bq.w) | (c2.x | c2.y | c2.z | c2.w) |
+                     (d2.x | d2.y | d2.z | d2.w)) != 0u;
+            } else {
+                uint32_t o = 0;
+                for (int jk = jb; jk < e; ++jk) o |= D.nzflag[jk];
+                f = o != 0u;
+            }
         }
         const unsigned m = __ballot_sync(0xffffffffu, f);
         if (lane == 0) s_wcnt[warp] = __popc(m);
+        // the centring term: 256/CT threads per chain over interleaved draw CTAs, then in part order
+        constexpr int PARTS = 256 / CT;
+        {
+            const int c = tid / PARTS, part = tid % PARTS;
+            const int ntl = (((N + TC_TM - 1) / TC_TM) * TC_TM * CT + 255) / 256;
+            double a = 0.0;
+            for (int q = part; q < ntl; q += PARTS) a += D.k0part[(size_t)q * CT + c];
+            s_k0p[tid] = a;
+        }
         __syncthreads();
         if (tid == 0) {
             int acc = 0;
@@ -77,13 +96,13 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
             }
             s_nact = acc;
         }
+        if (tid < CT) {
+            double t = 0.0;
+            for (int q = 0; q < PARTS; ++q) t += s_k0p[tid * PARTS + q];
+            s_k0[tid] = t;
+        }
         __syncthreads();
         if (f) s_act[s_wcnt[warp] + __popc(m & ((1u << lane) - 1u))] = tid;
-        if (tid < CT) {   // the centring term, summed over the draw tiles in order
-            double s = 0.0;
-            for (int q = 0; q < (N + TC_TM - 1) / TC_TM; ++q) s += D.k0part[(size_t)q * CT + tid];
-            s_k0[tid] = s;
-        }
         __syncthreads();
     }
     const int nact = s_nact;
