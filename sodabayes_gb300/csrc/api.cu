@@ -4,6 +4,8 @@
 // zbuild.cu and sweep.cu.  The host computes block bounds, prefix sums of the
 // factor column lengths, the top eigenvalue of the small Lanczos tridiagonal
 // matrices, and formats results.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -12,6 +14,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -23,6 +26,39 @@
 using namespace soda;
 
 namespace {
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link-time dependency on libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// 2-D tile map over a row-major array of d1 rows of d0 elements (row stride
+// `stride` bytes), loaded in boxes of b0 x b1 elements.
+CUresult make_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, const void *base, uint64_t d0, uint64_t d1,
+                      uint64_t stride, uint32_t b0, uint32_t b1, CUtensorMapSwizzle sw)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 fn = tmap_encoder();
+    if (!fn) return CUDA_ERROR_NOT_SUPPORTED;
+    const cuuint64_t dims[2] = {d0, d1};
+    const cuuint64_t strides[1] = {stride};
+    const cuuint32_t box[2] = {b0, b1};
+    const cuuint32_t es[2] = {1, 1};
+    return fn(m, dt, 2, const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
 
 thread_local std::string g_last_error;
 
@@ -120,6 +156,7 @@ struct sodagpu_ctx {
     double *k0part = nullptr;
     float *rapart = nullptr;
     int32_t *raticket = nullptr;
+    TcMaps maps{};
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
     cudaGraphExec_t graph = nullptr;
@@ -761,6 +798,21 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         }
     }
     build_dev(c);
+    if (c->tc) {
+        const int NB = sweep_tc_rows(C);
+        CUresult r = make_tmap_2d(&c->maps.codes128, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 128,
+                                  128, CU_TENSOR_MAP_SWIZZLE_128B);
+        if (r == CUDA_SUCCESS)
+            r = make_tmap_2d(&c->maps.codes64, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 128, 64,
+                             CU_TENSOR_MAP_SWIZZLE_128B);
+        if (r == CUDA_SUCCESS)
+            r = make_tmap_2d(&c->maps.r, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, c->r32, c->ldr, C, (uint64_t)c->ldr * 4, 128,
+                             C, CU_TENSOR_MAP_SWIZZLE_NONE);
+        if (r == CUDA_SUCCESS)
+            r = make_tmap_2d(&c->maps.d, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->dsplit, c->ldd, NB, (uint64_t)c->ldd * 2,
+                             64, NB, CU_TENSOR_MAP_SWIZZLE_128B);
+        if (r != CUDA_SUCCESS) return fail(SODAGPU_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    }
     RunCtl h{};
     CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
     if (c->nskipped)
@@ -776,7 +828,7 @@ int sodagpu_init_chains(sodagpu_ctx *c)
     }
     cudaGraph_t gr;
     CUDA_TRY(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = sweep_enqueue_iteration(c->D, c->blk_sizes.data(), c->sm_count, c->st);
+    cudaError_t e = sweep_enqueue_iteration(c->D, c->blk_sizes.data(), c->sm_count, &c->maps, c->st);
     cudaError_t e2 = cudaStreamEndCapture(c->st, &gr);
     if (e != cudaSuccess) return fail(SODAGPU_E_CUDA, "capturing the iteration failed: %s", cudaGetErrorString(e));
     if (e2 != cudaSuccess) return fail(SODAGPU_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
@@ -1034,7 +1086,7 @@ int sodagpu_profile_kernels(sodagpu_ctx *c, int32_t iters, double *ms, int32_t *
     int rc = 0;
     for (int t = 0; t < iters && rc == 0; ++t) {
         ProfHook hook{ev.data(), cls.data(), 0, cap};
-        cudaError_t e = sweep_enqueue_iteration(c->D, c->blk_sizes.data(), c->sm_count, c->st, &hook);
+        cudaError_t e = sweep_enqueue_iteration(c->D, c->blk_sizes.data(), c->sm_count, &c->maps, c->st, &hook);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
         if (e != cudaSuccess) {
             rc = fail(SODAGPU_E_CUDA, "profiled iteration failed: %s", cudaGetErrorString(e));

@@ -9,33 +9,42 @@
 // residual column is split into three bf16 terms (hi + mid + lo carry about
 // 24 significant bits), so one MMA of N = 3 * chains (padded to 16) gives
 // FP32-accurate products with FP32 accumulation in tensor memory.  A CTA owns
-// one M tile and one K split of 128-individual stages; per stage, cp.async
-// brings the tile's codes (XOR-swizzled 16-byte chunks, conflict-free reads)
-// and the chains' FP32 residuals into a raw buffer, the CTA converts them into
-// a double-buffered 128-byte-swizzled operand buffer, and one thread issues
-// eight K=16 MMAs whose completion an mbarrier reports when the operand buffer
-// is needed again.  The augmenting part u_j' ra_c (5% of the work) runs on
-// the FP32 cores.  Partial sums go to rpx/rpu, added and drawn by k_draw.
+// one M tile and one K split of 128-individual stages and runs a
+// warp-specialised pipeline synchronised by mbarriers:
+//   warp 8  (one thread) TMA: the stage's 128 x 128 code tile (hardware
+//           128-byte swizzle) and the chains' 128 residuals into a raw buffer
+//           (TC_NS buffers in flight);
+//   warps 0-7 convert the raw buffer into the double-buffered bf16 operand
+//           tiles (codes; residual hi/mid/lo rows) and release both;
+//   warp 9  (one thread) issues the eight K=16 MMAs of the stage and commits
+//           their completion, which frees the operand buffer.
+// The augmenting part u_j' ra_c (5% of the work) then runs on the FP32 cores
+// from staged windows of U.  Partial sums go to rpx/rpu, added and drawn by
+// k_draw.
 #pragma once
+#include <cuda.h>
 
 namespace soda {
 
-constexpr int TC_TM = 128;   // SNPs per M tile
-constexpr int TC_KC = 128;   // individuals per stage
-constexpr int TC_NS = 4;     // raw stages in flight
-constexpr int TC_UWR = 256;  // augmented rows per staging window of the U part
+constexpr int TC_TM = 128;       // SNPs per M tile
+constexpr int TC_KC = 128;       // individuals per stage
+constexpr int TC_NS = 4;         // raw stages in flight
+constexpr int TC_UWR = 256;      // augmented rows per staging window of the U part
+constexpr int TC_THREADS = 320;  // 8 converter warps, the TMA warp, the MMA warp
+constexpr int TC_CONV = 256;     // converter threads
+constexpr int TC_WARP_TMA = 8, TC_WARP_MMA = 9;
 
 template <int CT>
 struct RhsTc {
     static constexpr int NB = ((3 * CT + 15) / 16) * 16;   // MMA N: hi, mid, lo per chain
-    static constexpr int RAW_A = TC_TM * TC_KC;            // codes
-    static constexpr int RAW_B = CT * TC_KC * 4;           // FP32 residuals
+    static constexpr int RAW_A = TC_TM * TC_KC;            // codes (TMA box 128 x 128, 128-byte swizzle)
+    static constexpr int RAW_B = CT * TC_KC * 4;           // FP32 residuals (TMA box 128 x CT)
     static constexpr int RAW = RAW_A + RAW_B;
     static constexpr int OP_A = TC_TM * TC_KC * 2;         // bf16 codes, two 64-wide K regions
     static constexpr int OP_B = NB * TC_KC * 2;
     static constexpr int OP = OP_A + OP_B;
     static constexpr size_t SMEM = 1024 + 2 * (size_t)OP + (size_t)TC_NS * RAW;
-    static_assert(OP % 1024 == 0, "operand buffers must keep 1024-byte alignment");
+    static_assert(OP % 1024 == 0 && RAW % 1024 == 0, "operand and raw buffers must keep 1024-byte alignment");
     // U part: a window of the tile's 128 U columns and the chains' ra, plus the partial sums
     static constexpr size_t UPART = (size_t)(TC_TM + CT) * TC_UWR * 4 + (size_t)TC_TM * CT * 4;
     static_assert(UPART <= 2 * (size_t)OP + (size_t)TC_NS * RAW, "U window must fit the pipeline buffers");
@@ -83,12 +92,14 @@ __device__ __forceinline__ int xreduce_base(int lane)
 }
 
 template <int CT>
-__global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_rhs_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_r, Dev D, int b,
+             int ksplit)
 {
     using T = RhsTc<CT>;
     constexpr int NB = T::NB;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
-    __shared__ uint64_t s_bar[2];
+    __shared__ uint64_t s_full[TC_NS], s_empty[TC_NS], s_conv[2], s_opfree[2], s_done;
     __shared__ uint32_t s_tmem;
     __shared__ int s_err;
     unsigned char *base = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
@@ -107,7 +118,7 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
 
     // padding rows of B (n >= 3*CT) stay zero in both operand buffers
     if constexpr (NB > 3 * CT) {
-        for (int t = tid; t < 2 * (NB - 3 * CT) * (TC_KC / 8); t += 256) {
+        for (int t = tid; t < 2 * (NB - 3 * CT) * (TC_KC / 8); t += TC_THREADS) {
             const int ob = t / ((NB - 3 * CT) * (TC_KC / 8)), r = t % ((NB - 3 * CT) * (TC_KC / 8));
             const int n = 3 * CT + r / (TC_KC / 8), q = r % (TC_KC / 8);
             *reinterpret_cast<uint4 *>(op0 + ob * T::OP + T::OP_A + tc::sw128_off(n, 8 * q, NB)) =
@@ -115,106 +126,116 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
         }
     }
     if (tid == 0) {
-        tc::mbar_init(&s_bar[0], 1);
-        tc::mbar_init(&s_bar[1], 1);
+        for (int i = 0; i < TC_NS; ++i) {
+            tc::mbar_init(&s_full[i], 1);
+            tc::mbar_init(&s_empty[i], TC_CONV);
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&s_conv[i], TC_CONV);
+            tc::mbar_init(&s_opfree[i], 1);
+        }
+        tc::mbar_init(&s_done, 1);
         tc::mbar_fence_init();
         s_err = 0;
     }
-    if (warp == 0) tc::tmem_alloc(&s_tmem, 64);
+    if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 64);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tm = s_tmem;
 
-    auto issue = [&](int s, int buf) {
-        unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
-        const int i0 = (c0 + s) * TC_KC;
-        for (int t = tid; t < TC_TM * 8; t += 256) {   // codes: 128 SNPs x 8 chunks of 16
-            const int m = t >> 3, ch = t & 7;
-            unsigned char *dst = ra_ + m * 128 + ((ch ^ (m & 7)) << 4);
-            const int jk = j0 + m;
-            if (jk < N) __pipeline_memcpy_async(dst, D.G + (size_t)(ls + jk) * D.ldx + i0 + ch * 16, 16);
-            else *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
-        }
-        for (int t = tid; t < CT * 32; t += 256) {     // residuals: CT rows of 128 floats
-            const int c = t >> 5, ch = t & 31;
-            __pipeline_memcpy_async(ra_ + T::RAW_A + c * 512 + ch * 16, D.r32 + (size_t)c * D.ldr + i0 + ch * 4, 16);
-        }
-        __pipeline_commit();
-    };
-
-#pragma unroll
-    for (int pp = 0; pp < TC_NS - 1; ++pp) {
-        if (pp < nck) issue(pp, pp);
-        else __pipeline_commit();
-    }
-    const uint32_t idesc = tc::idesc_bf16(TC_TM, NB);
-    for (int s = 0; s < nck; ++s) {
-        if (s + TC_NS - 1 < nck) issue(s + TC_NS - 1, (s + TC_NS - 1) % TC_NS);
-        else __pipeline_commit();
-        __pipeline_wait_prior(TC_NS - 1);
-        const int ob = s & 1;
-        // the operand buffer was last read by the MMAs of stage s-2
-        if (s >= 2 && !tc::mbar_wait(&s_bar[ob], ((s - 2) >> 1) & 1)) s_err = 1;
-        __syncthreads();
-        const unsigned char *ra_ = raw0 + (size_t)(s % TC_NS) * T::RAW;
-        unsigned char *opa = op0 + ob * T::OP;
-        unsigned char *opb = opa + T::OP_A;
-        // codes -> bf16: a warp converts 4 SNP rows x 8 chunks of 16 codes
-#pragma unroll
-        for (int it = 0; it < TC_TM * 8 / 256; ++it) {
-            const int t = tid + 256 * it;
-            const int m = t >> 3, ch = t & 7;
-            const uint4 w = *reinterpret_cast<const uint4 *>(ra_ + m * 128 + ((ch ^ (m & 7)) << 4));
-            uint4 lo, hi;
-            tc::codes_to_bf16x4(w.x, lo.x, lo.y);
-            tc::codes_to_bf16x4(w.y, lo.z, lo.w);
-            tc::codes_to_bf16x4(w.z, hi.x, hi.y);
-            tc::codes_to_bf16x4(w.w, hi.z, hi.w);
-            *reinterpret_cast<uint4 *>(opa + tc::sw128_off(m, 16 * ch, TC_TM)) = lo;
-            *reinterpret_cast<uint4 *>(opa + tc::sw128_off(m, 16 * ch + 8, TC_TM)) = hi;
-        }
-        // residuals -> three bf16 rows per chain
-        for (int t = tid; t < CT * (TC_KC / 8); t += 256) {
-            const int c = t / (TC_KC / 8), q = t % (TC_KC / 8);
-            const float4 a = *reinterpret_cast<const float4 *>(ra_ + T::RAW_A + c * 512 + q * 32);
-            const float4 bq = *reinterpret_cast<const float4 *>(ra_ + T::RAW_A + c * 512 + q * 32 + 16);
-            uint4 h, md, l;
-            tc::split3x2(a.x, a.y, h.x, md.x, l.x);
-            tc::split3x2(a.z, a.w, h.y, md.y, l.y);
-            tc::split3x2(bq.x, bq.y, h.z, md.z, l.z);
-            tc::split3x2(bq.z, bq.w, h.w, md.w, l.w);
-            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(c, 8 * q, NB)) = h;
-            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(CT + c, 8 * q, NB)) = md;
-            *reinterpret_cast<uint4 *>(opb + tc::sw128_off(2 * CT + c, 8 * q, NB)) = l;
-        }
-        tc::fence_async_smem();
-        __syncthreads();
-        if (tid == 0 && !s_err) {
-            tc::fence_after_sync();
-            const uint32_t a0 = tc::smem_u32(opa), b0 = tc::smem_u32(opb);
-#pragma unroll
-            for (int kk = 0; kk < TC_KC / 16; ++kk) {
-                const uint32_t ka = (kk >> 2) * (TC_TM * 128) + (kk & 3) * 32;
-                const uint32_t kb = (kk >> 2) * (NB * 128) + (kk & 3) * 32;
-                tc::mma_bf16(tm, tc::desc_sw128(a0 + ka, 1024), tc::desc_sw128(b0 + kb, 1024), idesc,
-                             (s | kk) != 0 ? 1u : 0u);
+    if (warp == TC_WARP_TMA) {
+        if (lane == 0) {
+            tc::tma_prefetch_desc(&tm_codes);
+            tc::tma_prefetch_desc(&tm_r);
+            for (int s = 0; s < nck; ++s) {
+                const int buf = s % TC_NS;
+                // the buffer's previous stage has been converted
+                if (s >= TC_NS && !tc::mbar_wait(&s_empty[buf], ((s / TC_NS) - 1) & 1)) {
+                    s_err = 1;
+                    break;
+                }
+                unsigned char *rw = raw0 + (size_t)buf * T::RAW;
+                const int i0 = (c0 + s) * TC_KC;
+                tc::mbar_expect_tx(&s_full[buf], T::RAW);
+                tc::tma_load_2d(rw, &tm_codes, i0, ls + j0, &s_full[buf]);
+                tc::tma_load_2d(rw + T::RAW_A, &tm_r, i0, 0, &s_full[buf]);
             }
-            tc::mma_commit(&s_bar[ob]);
         }
-    }
-    __pipeline_wait_prior(0);
-    bool have = nck > 0;
-    if (have) {
-        const int last = nck - 1;
-        if (!tc::mbar_wait(&s_bar[last & 1], (last >> 1) & 1)) s_err = 1;
+    } else if (warp == TC_WARP_MMA) {
+        if (lane == 0 && nck > 0) {
+            const uint32_t idesc = tc::idesc_bf16(TC_TM, NB);
+            for (int s = 0; s < nck; ++s) {
+                const int ob = s & 1;
+                if (!tc::mbar_wait(&s_conv[ob], (s >> 1) & 1)) {
+                    s_err = 1;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t a0 = tc::smem_u32(op0 + ob * T::OP), b0 = a0 + T::OP_A;
+#pragma unroll
+                for (int kk = 0; kk < TC_KC / 16; ++kk) {
+                    const uint32_t ka = (kk >> 2) * (TC_TM * 128) + (kk & 3) * 32;
+                    const uint32_t kb = (kk >> 2) * (NB * 128) + (kk & 3) * 32;
+                    tc::mma_bf16(tm, tc::desc_sw128(a0 + ka, 1024), tc::desc_sw128(b0 + kb, 1024), idesc,
+                                 (s | kk) != 0 ? 1u : 0u);
+                }
+                tc::mma_commit(&s_opfree[ob]);
+            }
+            tc::mma_commit(&s_done);
+        }
+    } else {
+        // converters: raw stage -> bf16 operand tiles
+        for (int s = 0; s < nck; ++s) {
+            const int buf = s % TC_NS, ob = s & 1;
+            bool ok = tc::mbar_wait(&s_full[buf], (s / TC_NS) & 1);
+            // the operand buffer was last read by the MMAs of stage s-2
+            if (ok && s >= 2) ok = tc::mbar_wait(&s_opfree[ob], ((s - 2) >> 1) & 1);
+            if (!ok) {
+                s_err = 1;
+                break;
+            }
+            const unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
+            unsigned char *opa = op0 + ob * T::OP;
+            unsigned char *opb = opa + T::OP_A;
+            // codes: a warp converts 4 SNP rows x 8 chunks of 16 codes (conflict-free)
+#pragma unroll
+            for (int it = 0; it < TC_TM * 8 / TC_CONV; ++it) {
+                const int t = tid + TC_CONV * it;
+                const int m = t >> 3, ch = t & 7;
+                const uint4 w = *reinterpret_cast<const uint4 *>(ra_ + m * 128 + ((ch ^ (m & 7)) << 4));
+                uint4 lo, hi;
+                tc::codes_to_bf16x4(w.x, lo.x, lo.y);
+                tc::codes_to_bf16x4(w.y, lo.z, lo.w);
+                tc::codes_to_bf16x4(w.z, hi.x, hi.y);
+                tc::codes_to_bf16x4(w.w, hi.z, hi.w);
+                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(m, 16 * ch, TC_TM)) = lo;
+                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(m, 16 * ch + 8, TC_TM)) = hi;
+            }
+            // residuals -> three bf16 rows per chain
+            for (int t = tid; t < CT * (TC_KC / 8); t += TC_CONV) {
+                const int c = t / (TC_KC / 8), q = t % (TC_KC / 8);
+                const float4 a = *reinterpret_cast<const float4 *>(ra_ + T::RAW_A + c * 512 + q * 32);
+                const float4 bq = *reinterpret_cast<const float4 *>(ra_ + T::RAW_A + c * 512 + q * 32 + 16);
+                uint4 h, md, l;
+                tc::split3x2(a.x, a.y, h.x, md.x, l.x);
+                tc::split3x2(a.z, a.w, h.y, md.y, l.y);
+                tc::split3x2(bq.x, bq.y, h.z, md.z, l.z);
+                tc::split3x2(bq.z, bq.w, h.w, md.w, l.w);
+                *reinterpret_cast<uint4 *>(opb + tc::sw128_off(c, 8 * q, NB)) = h;
+                *reinterpret_cast<uint4 *>(opb + tc::sw128_off(CT + c, 8 * q, NB)) = md;
+                *reinterpret_cast<uint4 *>(opb + tc::sw128_off(2 * CT + c, 8 * q, NB)) = l;
+            }
+            tc::fence_async_smem();
+            tc::mbar_arrive(&s_conv[ob]);
+            tc::mbar_arrive(&s_empty[buf]);
+        }
+        if (nck > 0 && !tc::mbar_wait(&s_done, 0)) s_err = 1;
     }
     __syncthreads();
-    if (s_err) {
-        have = false;
-        if (tid == 0) flag_err(D, 4);
-    }
     tc::fence_after_sync();
+    const bool have = nck > 0 && !s_err;
+    if (s_err && tid == 0) flag_err(D, 4);
     // genotype partial sums: row m of the accumulator (tensor-memory lane m)
     if (warp < 4) {
         const int m = warp * 32 + lane, jk = j0 + m;
@@ -240,7 +261,7 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == TC_WARP_MMA) {
         tc::fence_after_sync();
         tc::tmem_dealloc(tm, 64);
     }
@@ -258,18 +279,18 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
     float *sU = reinterpret_cast<float *>(base);      // [TC_TM][TC_UWR]
     float *sRa = sU + TC_TM * TC_UWR;                 // [CT][TC_UWR]
     float *s_u = sRa + CT * TC_UWR;                   // [TC_TM][CT]
-    for (int t = tid; t < TC_TM * CT; t += 256) s_u[t] = 0.0f;
+    for (int t = tid; t < TC_TM * CT; t += TC_THREADS) s_u[t] = 0.0f;
     for (int w0 = l0; w0 < l1; w0 += TC_UWR) {
         const int len = min(TC_UWR, l1 - w0);        // a multiple of 8
         __syncthreads();
-        for (int t = tid; t < TC_TM * (len / 4); t += 256) {
+        for (int t = tid; t < TC_TM * (len / 4); t += TC_THREADS) {
             const int jj = t / (len / 4), q = t % (len / 4);
             const int jk = j0 + jj;
             float *dst = sU + jj * TC_UWR + 4 * q;
             if (jk < N) __pipeline_memcpy_async(dst, D.U32 + D.uoff[ls + jk] + w0 + 4 * q, 16);
             else *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        for (int t = tid; t < CT * (len / 4); t += 256) {
+        for (int t = tid; t < CT * (len / 4); t += TC_THREADS) {
             const int c = t / (len / 4), q = t % (len / 4);
             __pipeline_memcpy_async(sRa + c * TC_UWR + 4 * q, D.ra32 + (size_t)c * D.ldra + w0 + 4 * q, 16);
         }
@@ -277,7 +298,7 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
         __pipeline_wait_prior(0);
         __syncthreads();
 #pragma unroll 1
-        for (int g = 0; g < 4; ++g) {
+        for (int g = 0; g < (warp < 8 ? 4 : 0); ++g) {
             const int jq = warp * 16 + g * 4;
             float acc[4 * CT];
 #pragma unroll
@@ -306,7 +327,7 @@ __global__ void __launch_bounds__(256, 1) k_rhs_tc(Dev D, int b, int ksplit)
         }
     }
     __syncthreads();
-    for (int t = tid; t < TC_TM * CT; t += 256) {
+    for (int t = tid; t < TC_TM * CT; t += TC_THREADS) {
         const int m = t / CT, c = t % CT, jk = j0 + m;
         if (jk < N) D.rpu[((size_t)ks * CT + c) * D.bs + jk] = (double)s_u[t];
     }

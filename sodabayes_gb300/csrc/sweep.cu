@@ -776,7 +776,8 @@ struct ProfScope {
 // per SM), then the update (row tiles of r on the tensor cores, ra tiles on
 // the FP32 cores; two CTAs per SM).
 template <int CT>
-static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_count, cudaStream_t st, ProfHook *prof)
+static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_count, const TcMaps *maps,
+                                  cudaStream_t st, ProfHook *prof)
 {
     const int mtiles = (nblk_snps + TC_TM - 1) / TC_TM;
     const int nst = D.ldx / TC_KC;
@@ -785,7 +786,7 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
     ks = ks > nst ? nst : ks;
     {
         ProfScope ps(prof, st, PROF_RHS);
-        k_rhs_tc<CT><<<mtiles * ks, 256, RhsTc<CT>::SMEM, st>>>(D, b, ks);
+        k_rhs_tc<CT><<<mtiles * ks, TC_THREADS, RhsTc<CT>::SMEM, st>>>(maps->codes128, maps->r, D, b, ks);
     }
     {
         const int span = mtiles * TC_TM;
@@ -795,16 +796,18 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
     const int ra_tiles = (nblk_snps + 127) / 128;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
-        k_update_tc<CT><<<D.nr_ctas + ra_tiles * TU_RA_SPLIT, 256, UpdTc<CT>::SMEM, st>>>(D, b, TU_RA_SPLIT);
+        k_update_tc<CT><<<D.nr_ctas + ra_tiles * TU_RA_SPLIT, TC_THREADS, UpdTc<CT>::SMEM, st>>>(
+            maps->codes64, maps->d, D, b, TU_RA_SPLIT);
     }
     return cudaGetLastError();
 }
 
 template <int MODE, int CT>
-static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count, cudaStream_t st, ProfHook *prof)
+static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count, const TcMaps *maps, cudaStream_t st,
+                               ProfHook *prof)
 {
     if constexpr (MODE == SODAGPU_FP8 && CT >= 4) {
-        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, sm_count, st, prof);
+        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, sm_count, maps, st, prof);
     }
     constexpr int MTS = 8 * SptOf<CT>::v;
     const int mtiles = (nblk_snps + MTS - 1) / MTS;
@@ -830,14 +833,15 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
 }
 
 template <int MODE>
-static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int sm_count, cudaStream_t st, ProfHook *prof)
+static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int sm_count, const TcMaps *maps, cudaStream_t st,
+                                    ProfHook *prof)
 {
     switch (D.chains) {
-    case 1: return launch_block<MODE, 1>(D, b, nsnp, sm_count, st, prof);
-    case 2: return launch_block<MODE, 2>(D, b, nsnp, sm_count, st, prof);
-    case 4: return launch_block<MODE, 4>(D, b, nsnp, sm_count, st, prof);
-    case 8: return launch_block<MODE, 8>(D, b, nsnp, sm_count, st, prof);
-    case 16: return launch_block<MODE, 16>(D, b, nsnp, sm_count, st, prof);
+    case 1: return launch_block<MODE, 1>(D, b, nsnp, sm_count, maps, st, prof);
+    case 2: return launch_block<MODE, 2>(D, b, nsnp, sm_count, maps, st, prof);
+    case 4: return launch_block<MODE, 4>(D, b, nsnp, sm_count, maps, st, prof);
+    case 8: return launch_block<MODE, 8>(D, b, nsnp, sm_count, maps, st, prof);
+    case 16: return launch_block<MODE, 16>(D, b, nsnp, sm_count, maps, st, prof);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -919,9 +923,10 @@ cudaError_t sweep_prepare(int bs)
     return e;
 }
 
-cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, cudaStream_t st,
-                                    ProfHook *prof)
+cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, const TcMaps *maps,
+                                    cudaStream_t st, ProfHook *prof)
 {
+    if (D.tc && !maps) return cudaErrorInvalidValue;
     const int C = D.chains;
     {
         ProfScope ps(prof, st, PROF_MU);
@@ -932,9 +937,10 @@ cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_c
     for (int b = 0; b < D.nb; ++b) {
         const int nsnp = blk_sizes[b];
         cudaError_t e;
-        if (D.precision == SODAGPU_FP64) e = launch_block_mode<SODAGPU_FP64>(D, b, nsnp, sm_count, st, prof);
-        else if (D.precision == SODAGPU_FP32) e = launch_block_mode<SODAGPU_FP32>(D, b, nsnp, sm_count, st, prof);
-        else e = launch_block_mode<SODAGPU_FP8>(D, b, nsnp, sm_count, st, prof);
+        if (D.precision == SODAGPU_FP64) e = launch_block_mode<SODAGPU_FP64>(D, b, nsnp, sm_count, maps, st, prof);
+        else if (D.precision == SODAGPU_FP32)
+            e = launch_block_mode<SODAGPU_FP32>(D, b, nsnp, sm_count, maps, st, prof);
+        else e = launch_block_mode<SODAGPU_FP8>(D, b, nsnp, sm_count, maps, st, prof);
         if (e != cudaSuccess) return e;
     }
     {

@@ -1,5 +1,6 @@
 // sweep.cuh — host-side entry points of the sweep kernels (sweep.cu).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include "state.cuh"
 
@@ -22,10 +23,18 @@ struct ProfHook {
     int n, cap;
 };
 
+// TMA descriptors of the tensor-core sweep: genotype codes in 128 x 128 and
+// 128 x 64 (individuals x SNPs) boxes with 128-byte swizzle, the FP32
+// residuals of all chains in 128 x chains boxes, and the bf16 delta split in
+// 64 x rows boxes with 128-byte swizzle.
+struct TcMaps {
+    CUtensorMap codes128, codes64, r, d;
+};
+
 // Enqueues one Gibbs iteration of every chain on `st` (graph-capturable when
-// prof == nullptr).
-cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, cudaStream_t st,
-                                    ProfHook *prof = nullptr);
+// prof == nullptr).  `maps` is required when D.tc is set.
+cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, const TcMaps *maps,
+                                    cudaStream_t st, ProfHook *prof = nullptr);
 cudaError_t sweep_enqueue_init(const Dev &D, double vara0, double scale_va0, int sm_count, cudaStream_t st);
 cudaError_t sweep_enqueue_recal(const Dev &D, double unused, cudaStream_t st);
 

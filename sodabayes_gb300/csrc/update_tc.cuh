@@ -8,12 +8,16 @@
 // Row tiles of r (128 individuals, one CTA each) run on tcgen05: A = the
 // tile's codes of 64 subset positions per stage, transposed to individual-major
 // bf16 in shared memory, B = the three-way bf16 split of delta/sd written by
-// the draws (k_draw), D = 128 x 3*chains FP32 in tensor memory.  Stages
-// whose 64 positions have no non-zero delta in any chain are skipped.  The
-// centring term sum_j x0_j delta_j is added in FP64 from the per-CTA sums of
-// the draws.  The augmented rows ra (U_b is FP32, one tile of 128 rows per
-// ra_split CTAs over column ranges) run on the FP32 cores; the last CTA of a
-// row tile adds the split partial sums in split order (deterministic).
+// the draws (k_draw), D = 128 x 3*chains FP32 in tensor memory.  Stages whose
+// 64 positions have no non-zero delta in any chain are skipped.  The pipeline
+// is the one of k_rhs_tc: warp 8 loads each stage's code tile and delta-split
+// tile by TMA (both 128-byte swizzled; the MMA reads the delta split straight
+// from the raw buffer), warps 0-7 transpose and convert the codes, warp 9
+// issues the MMAs.  The centring term sum_j x0_j delta_j is added in FP64
+// from the per-CTA sums of the draws.  The augmented rows ra (U_b is FP32,
+// one tile of 128 rows per ra_split CTAs over column ranges) run on the FP32
+// cores; the last CTA of a row tile adds the split partial sums in split
+// order (deterministic).
 #pragma once
 
 namespace soda {
@@ -27,29 +31,29 @@ constexpr int TU_UNR = 4;          // U columns in flight per warp
 template <int CT>
 struct UpdTc {
     static constexpr int NB = RhsTc<CT>::NB;
-    static constexpr int RAW_A = TU_KC * 128;          // codes: 64 positions x 128 individuals
-    static constexpr int RAW_B = NB * TU_KC * 2;       // bf16 split of delta/sd
+    static constexpr int RAW_A = TU_KC * 128;          // codes: 64 positions x 128 individuals (TMA, swizzled)
+    static constexpr int RAW_B = NB * TU_KC * 2;       // bf16 split of delta/sd (TMA, swizzled; MMA operand B)
     static constexpr int RAW = RAW_A + RAW_B;
-    static constexpr int OP_A = 128 * TU_KC * 2;
-    static constexpr int OP_B = RAW_B;
-    static constexpr int OP = OP_A + OP_B;
+    static constexpr int OP = 128 * TU_KC * 2;         // bf16 codes, individual-major (MMA operand A)
     static constexpr int PIPE = 2 * OP + TU_NS * RAW;
-    static constexpr int RED = 8 * CT * 128 * 4;       // warp partials of the ra tiles
+    static constexpr int RED = 8 * 8 * 128 * 4;        // warp partials of the ra tiles (8 chains a pass)
     static constexpr size_t SMEM = 1024 + (size_t)(PIPE > RED ? PIPE : RED);
-    static_assert(OP % 1024 == 0 && RAW % 1024 == 0, "operand buffers must keep 1024-byte alignment");
+    static_assert(OP % 1024 == 0 && RAW % 1024 == 0 && RAW_A % 1024 == 0, "buffers must keep 1024-byte alignment");
 };
 
 template <int CT>
-__device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned char *base)
+__device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, const CUtensorMap *tm_d, const Dev &D,
+                                               int b, unsigned char *base)
 {
     using T = UpdTc<CT>;
     constexpr int NB = T::NB;
-    __shared__ uint64_t s_bar[2];
+    constexpr int NW = TC_THREADS / 32;
+    __shared__ uint64_t s_full[TU_NS], s_empty[TU_NS], s_conv[2], s_opfree[2], s_done;
     __shared__ uint32_t s_tmem;
-    __shared__ int s_err, s_nact, s_wcnt[9];
+    __shared__ int s_err, s_nact, s_wcnt[NW + 1];
     __shared__ int s_act[TU_MAXQ];
     __shared__ double s_k0[CT];
-    __shared__ double s_k0p[256];
+    __shared__ double s_k0p[TC_CONV];
     __shared__ double s_rsw[4][CT];
     unsigned char *op0 = base;
     unsigned char *raw0 = base + 2 * T::OP;
@@ -59,7 +63,7 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
     const int tile = blockIdx.x, t0 = tile * 128;
     const int nq = (N + TU_KC - 1) / TU_KC;
 
-    // stages with a non-zero delta, in subset order (nq <= 256 = blockDim)
+    // stages with a non-zero delta, in subset order (nq <= 256)
     {
         bool f = false;
         if (tid < nq) {
@@ -78,8 +82,8 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
         const unsigned m = __ballot_sync(0xffffffffu, f);
         if (lane == 0) s_wcnt[warp] = __popc(m);
         // the centring term: 256/CT threads per chain over interleaved draw CTAs, then in part order
-        constexpr int PARTS = 256 / CT;
-        {
+        constexpr int PARTS = TC_CONV / CT;
+        if (tid < TC_CONV) {
             const int c = tid / PARTS, part = tid % PARTS;
             const int ntl = (((N + TC_TM - 1) / TC_TM) * TC_TM * CT + 255) / 256;
             double a = 0.0;
@@ -89,7 +93,7 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
         __syncthreads();
         if (tid == 0) {
             int acc = 0;
-            for (int q = 0; q < 8; ++q) {
+            for (int q = 0; q < NW; ++q) {
                 const int t = s_wcnt[q];
                 s_wcnt[q] = acc;
                 acc += t;
@@ -109,59 +113,84 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
     if (nact == 0) return;   // nothing changed: r, r32 and rsum stay valid
 
     if (tid == 0) {
-        tc::mbar_init(&s_bar[0], 1);
-        tc::mbar_init(&s_bar[1], 1);
+        for (int i = 0; i < TU_NS; ++i) {
+            tc::mbar_init(&s_full[i], 1);
+            tc::mbar_init(&s_empty[i], TC_CONV + 1);   // converters + the MMAs reading the delta split
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&s_conv[i], TC_CONV);
+            tc::mbar_init(&s_opfree[i], 1);
+        }
+        tc::mbar_init(&s_done, 1);
         tc::mbar_fence_init();
         s_err = 0;
     }
-    if (warp == 0) tc::tmem_alloc(&s_tmem, 64);
+    if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 64);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tm = s_tmem;
 
-    auto issue = [&](int s, int buf) {
-        unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
-        const int k0 = s_act[s] * TU_KC;
-        for (int t = tid; t < TU_KC * 8; t += 256) {   // codes: 64 positions x 8 chunks of 16 individuals
-            const int kk = t >> 3, ch = t & 7;
-            unsigned char *dst = ra_ + kk * 128 + ((ch ^ ((kk >> 3) & 7)) << 4);
-            const int jk = k0 + kk;
-            if (jk < N) __pipeline_memcpy_async(dst, D.G + (size_t)(ls + jk) * D.ldx + t0 + ch * 16, 16);
-            else *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
+    if (warp == TC_WARP_TMA) {
+        if (lane == 0) {
+            tc::tma_prefetch_desc(tm_codes);
+            tc::tma_prefetch_desc(tm_d);
+            for (int s = 0; s < nact; ++s) {
+                const int buf = s % TU_NS;
+                if (s >= TU_NS && !tc::mbar_wait(&s_empty[buf], ((s / TU_NS) - 1) & 1)) {
+                    s_err = 1;
+                    break;
+                }
+                unsigned char *rw = raw0 + (size_t)buf * T::RAW;
+                const int k0 = s_act[s] * TU_KC;
+                tc::mbar_expect_tx(&s_full[buf], T::RAW);
+                tc::tma_load_2d(rw, tm_codes, t0, ls + k0, &s_full[buf]);
+                tc::tma_load_2d(rw + T::RAW_A, tm_d, k0, 0, &s_full[buf]);
+            }
         }
-        for (int t = tid; t < NB * 8; t += 256) {      // delta split: NB rows x 8 chunks of 8 positions
-            const int n = t >> 3, ch = t & 7;
-            __pipeline_memcpy_async(ra_ + T::RAW_A + tc::sw128_off(n, 8 * ch, NB),
-                                    D.dsplit + (size_t)n * D.ldd + k0 + 8 * ch, 16);
-        }
-        __pipeline_commit();
-    };
-
+    } else if (warp == TC_WARP_MMA) {
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, NB);
+            for (int s = 0; s < nact; ++s) {
+                const int ob = s & 1, buf = s % TU_NS;
+                if (!tc::mbar_wait(&s_conv[ob], (s >> 1) & 1)) {
+                    s_err = 1;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t a0 = tc::smem_u32(op0 + ob * T::OP);
+                const uint32_t b0 = tc::smem_u32(raw0 + (size_t)buf * T::RAW + T::RAW_A);
 #pragma unroll
-    for (int pp = 0; pp < TU_NS - 1; ++pp) {
-        if (pp < nact) issue(pp, pp);
-        else __pipeline_commit();
-    }
-    const uint32_t idesc = tc::idesc_bf16(128, NB);
-    const int iq_l = lane >> 3, kc = lane & 7;
-    const int rq = 4 * (4 * warp + iq_l);   // first of this thread's four individuals
-    for (int s = 0; s < nact; ++s) {
-        if (s + TU_NS - 1 < nact) issue(s + TU_NS - 1, (s + TU_NS - 1) % TU_NS);
-        else __pipeline_commit();
-        __pipeline_wait_prior(TU_NS - 1);
-        const int ob = s & 1;
-        if (s >= 2 && !tc::mbar_wait(&s_bar[ob], ((s - 2) >> 1) & 1)) s_err = 1;
-        __syncthreads();
-        const unsigned char *ra_ = raw0 + (size_t)(s % TU_NS) * T::RAW;
-        unsigned char *opa = op0 + ob * T::OP;
-        unsigned char *opb = opa + T::OP_A;
-        // transpose: positions 8kc..8kc+7 of individuals rq..rq+3 (a word per position)
-        {
+                for (int kk = 0; kk < TU_KC / 16; ++kk)
+                    tc::mma_bf16(tm, tc::desc_sw128(a0 + kk * 32, 1024), tc::desc_sw128(b0 + kk * 32, 1024), idesc,
+                                 (s | kk) != 0 ? 1u : 0u);
+                tc::mma_commit(&s_opfree[ob]);
+                tc::mma_commit(&s_empty[buf]);
+            }
+            tc::mma_commit(&s_done);
+        }
+    } else {
+        // converters: thread (a, bb) of warp w transposes individuals 16w+4a..+3 x positions 8bb..8bb+7.
+        // Reads rotate the position (slot e holds position (e+bb)&7) so that the 32 lanes hit 32 banks
+        // of the 128-byte-swizzled tile; a 64-bit rotation restores position order.
+        const int a = lane >> 3, bb = lane & 7;
+        const int rq = 16 * warp + 4 * a;
+        for (int s = 0; s < nact; ++s) {
+            const int buf = s % TU_NS, ob = s & 1;
+            bool ok = tc::mbar_wait(&s_full[buf], (s / TU_NS) & 1);
+            if (ok && s >= 2) ok = tc::mbar_wait(&s_opfree[ob], ((s - 2) >> 1) & 1);
+            if (!ok) {
+                s_err = 1;
+                break;
+            }
+            const unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
+            unsigned char *opa = op0 + ob * T::OP;
             uint32_t w[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e)
-                w[e] = *reinterpret_cast<const uint32_t *>(ra_ + (8 * kc + e) * 128 + ((warp ^ kc) << 4) + iq_l * 4);
+            for (int e = 0; e < 8; ++e) {
+                const int kk = 8 * bb + ((e + bb) & 7);
+                w[e] = *reinterpret_cast<const uint32_t *>(ra_ + kk * 128 + ((warp ^ (kk & 7)) << 4) + a * 4);
+            }
             uint32_t row[4][2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -174,32 +203,26 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
                 row[2][h] = __byte_perm(a2, a3, 0x5410u);
                 row[3][h] = __byte_perm(a2, a3, 0x7632u);
             }
+            const int sh = (bb & 3) * 8;
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
+                uint32_t lo = row[r][0], hi = row[r][1];
+                if (bb & 4) {
+                    const uint32_t t = lo;
+                    lo = hi;
+                    hi = t;
+                }
+                const uint32_t nlo = __funnelshift_l(hi, lo, sh), nhi = __funnelshift_l(lo, hi, sh);
                 uint4 v;
-                tc::codes_to_bf16x4(row[r][0], v.x, v.y);
-                tc::codes_to_bf16x4(row[r][1], v.z, v.w);
-                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(rq + r, 8 * kc, 128)) = v;
+                tc::codes_to_bf16x4(nlo, v.x, v.y);
+                tc::codes_to_bf16x4(nhi, v.z, v.w);
+                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(rq + r, 8 * bb, 128)) = v;
             }
+            tc::fence_async_smem();
+            tc::mbar_arrive(&s_conv[ob]);
+            tc::mbar_arrive(&s_empty[buf]);
         }
-        for (int t = tid; t < T::OP_B / 16; t += 256)
-            reinterpret_cast<uint4 *>(opb)[t] = reinterpret_cast<const uint4 *>(ra_ + T::RAW_A)[t];
-        tc::fence_async_smem();
-        __syncthreads();
-        if (tid == 0 && !s_err) {
-            tc::fence_after_sync();
-            const uint32_t a0 = tc::smem_u32(opa), b0 = tc::smem_u32(opb);
-#pragma unroll
-            for (int kk = 0; kk < TU_KC / 16; ++kk)
-                tc::mma_bf16(tm, tc::desc_sw128(a0 + kk * 32, 1024), tc::desc_sw128(b0 + kk * 32, 1024), idesc,
-                             (s | kk) != 0 ? 1u : 0u);
-            tc::mma_commit(&s_bar[ob]);
-        }
-    }
-    __pipeline_wait_prior(0);
-    {
-        const int last = nact - 1;
-        if (!tc::mbar_wait(&s_bar[last & 1], (last >> 1) & 1)) s_err = 1;
+        if (!tc::mbar_wait(&s_done, 0)) s_err = 1;
     }
     __syncthreads();
     const bool ok = !s_err;
@@ -207,33 +230,40 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
     tc::fence_after_sync();
     if (warp < 4) {
         const int i = t0 + warp * 32 + lane;
-        float acc[NB];
+        const bool row_ok = i < D.n;
+        double rv[CT];
 #pragma unroll
-        for (int g = 0; g < NB / 8; ++g) {
-            float v[8];
-            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + g * 8, v);
+        for (int c = 0; c < CT; ++c) rv[c] = row_ok ? D.r[(size_t)c * D.ldr + i] : 0.0;
+#pragma unroll
+        for (int g = 0; g < CT / 8 + (CT % 8 ? 1 : 0); ++g) {
+            // chains 8g .. 8g+7: their hi, mid and lo accumulator columns
+            float hi[8], md[8], lo[8];
+            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + 8 * g, hi);
+            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + CT + 8 * g, md);
+            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + 2 * CT + 8 * g, lo);
             tc::tmem_wait_ld();
 #pragma unroll
-            for (int e = 0; e < 8; ++e) acc[g * 8 + e] = v[e];
+            for (int e = 0; e < 8; ++e) {
+                const int c = 8 * g + e;
+                if (c < CT && ok && row_ok) rv[c] += (double)((hi[e] + md[e]) + lo[e]) + s_k0[c];
+            }
+        }
+        if (ok && row_ok) {
+#pragma unroll
+            for (int c = 0; c < CT; ++c) {
+                D.r[(size_t)c * D.ldr + i] = rv[c];
+                D.r32[(size_t)c * D.ldr + i] = (float)rv[c];
+            }
         }
 #pragma unroll
         for (int c = 0; c < CT; ++c) {
-            double v = 0.0;
-            if (ok && i < D.n) {
-                const size_t o = (size_t)c * D.ldr + i;
-                v = D.r[o] + ((double)((acc[c] + acc[CT + c]) + acc[2 * CT + c]) + s_k0[c]);
-                D.r[o] = v;
-                D.r32[o] = (float)v;
-            } else if (i < D.n) {
-                v = D.r[(size_t)c * D.ldr + i];
-            }
-            v = warp_sum(v);
+            const double v = warp_sum(rv[c]);
             if (lane == 0) s_rsw[warp][c] = v;
         }
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == TC_WARP_MMA) {
         tc::fence_after_sync();
         tc::tmem_dealloc(tm, 64);
     }
@@ -245,8 +275,9 @@ __device__ __forceinline__ void update_tc_rows(const Dev &D, int b, unsigned cha
 template <int CT>
 __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, unsigned char *base)
 {
+    constexpr int CP = CT < 8 ? CT : 8;   // chains per pass (keeps the accumulators in registers)
     __shared__ int s_last;
-    float *s_red = reinterpret_cast<float *>(base);   // [8][CT][128]
+    float *s_red = reinterpret_cast<float *>(base);   // [8 warps][CP][128]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
@@ -259,52 +290,58 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
     const int kb = kbeg + (int)(((long long)(N - kbeg) * (sp + 1)) / ra_split);
     const int ii = i0 + 4 * lane;
     const bool rows_ok = ii + 4 <= npad;
-    float acc[4][CT];
-#pragma unroll
-    for (int e = 0; e < 4; ++e)
-#pragma unroll
-        for (int c = 0; c < CT; ++c) acc[e][c] = 0.0f;
-    for (int k0 = ka + warp; k0 < kb; k0 += 8 * TU_UNR) {
-        float4 u[TU_UNR];
-        int kk[TU_UNR];
-#pragma unroll
-        for (int q = 0; q < TU_UNR; ++q) {
-            const int k = k0 + 8 * q;
-            kk[q] = (k < kb && D.nzflag[k]) ? k : -1;
-            u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (kk[q] >= 0 && rows_ok) u[q] = *reinterpret_cast<const float4 *>(D.U32 + D.uoff[ls + k] + ii);
-        }
-#pragma unroll
-        for (int q = 0; q < TU_UNR; ++q) {
-            if (kk[q] < 0) continue;
-            float dl[CT];
-#pragma unroll
-            for (int c = 0; c < CT; c += 4) {
-                const float4 v = *reinterpret_cast<const float4 *>(D.delta32 + (size_t)kk[q] * CT + c);
-                dl[c] = v.x; dl[c + 1] = v.y; dl[c + 2] = v.z; dl[c + 3] = v.w;
-            }
-#pragma unroll
-            for (int c = 0; c < CT; ++c) {
-                acc[0][c] = fmaf(u[q].x, dl[c], acc[0][c]);
-                acc[1][c] = fmaf(u[q].y, dl[c], acc[1][c]);
-                acc[2][c] = fmaf(u[q].z, dl[c], acc[2][c]);
-                acc[3][c] = fmaf(u[q].w, dl[c], acc[3][c]);
-            }
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < CT; ++c)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) s_red[(warp * CT + c) * 128 + 4 * lane + e] = acc[e][c];
-    __syncthreads();
     float *part = D.rapart + ((size_t)(tr * ra_split + sp) * CT) * 128;
-    if (tid < 128) {
-        for (int c = 0; c < CT; ++c) {
-            float s = 0.0f;
+    for (int cp0 = 0; cp0 < CT; cp0 += CP) {
+        float acc[4][CP];
 #pragma unroll
-            for (int w = 0; w < 8; ++w) s += s_red[(w * CT + c) * 128 + tid];
-            part[c * 128 + tid] = s;
+        for (int e = 0; e < 4; ++e)
+#pragma unroll
+            for (int c = 0; c < CP; ++c) acc[e][c] = 0.0f;
+        // warp w of 8 takes columns ka+w, ka+w+8, ...; the MMA/TMA warps idle here
+        for (int k0 = ka + warp; warp < 8 && k0 < kb; k0 += 8 * TU_UNR) {
+            float4 u[TU_UNR];
+            int kk[TU_UNR];
+#pragma unroll
+            for (int q = 0; q < TU_UNR; ++q) {
+                const int k = k0 + 8 * q;
+                kk[q] = (k < kb && D.nzflag[k]) ? k : -1;
+                u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (kk[q] >= 0 && rows_ok) u[q] = *reinterpret_cast<const float4 *>(D.U32 + D.uoff[ls + k] + ii);
+            }
+#pragma unroll
+            for (int q = 0; q < TU_UNR; ++q) {
+                if (kk[q] < 0) continue;
+                float dl[CP];
+#pragma unroll
+                for (int c = 0; c < CP; c += 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(D.delta32 + (size_t)kk[q] * CT + cp0 + c);
+                    dl[c] = v.x; dl[c + 1] = v.y; dl[c + 2] = v.z; dl[c + 3] = v.w;
+                }
+#pragma unroll
+                for (int c = 0; c < CP; ++c) {
+                    acc[0][c] = fmaf(u[q].x, dl[c], acc[0][c]);
+                    acc[1][c] = fmaf(u[q].y, dl[c], acc[1][c]);
+                    acc[2][c] = fmaf(u[q].z, dl[c], acc[2][c]);
+                    acc[3][c] = fmaf(u[q].w, dl[c], acc[3][c]);
+                }
+            }
         }
+        if (warp < 8) {
+#pragma unroll
+            for (int c = 0; c < CP; ++c)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) s_red[(warp * CP + c) * 128 + 4 * lane + e] = acc[e][c];
+        }
+        __syncthreads();
+        if (tid < 128) {
+            for (int c = 0; c < CP; ++c) {
+                float sum = 0.0f;
+#pragma unroll
+                for (int w = 0; w < 8; ++w) sum += s_red[(w * CP + c) * 128 + tid];
+                part[(cp0 + c) * 128 + tid] = sum;
+            }
+        }
+        __syncthreads();
     }
     __threadfence();
     __syncthreads();
@@ -312,13 +349,20 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    const int i = i0 + tid;
-    if (tid < 128 && i < D.bs) {
-        for (int c = 0; c < CT; ++c) {
-            float s = 0.0f;
-            for (int q = 0; q < ra_split; ++q) s += __ldcg(D.rapart + ((size_t)(tr * ra_split + q) * CT + c) * 128 + tid);
+    // the last CTA of the row tile: split partial sums in split order
+    const int i = i0 + (tid & 127);
+    if (tid < 256 && i < D.bs) {
+        for (int c = tid >> 7; c < CT; c += 2) {
+            float pv[TU_RA_SPLIT];
+#pragma unroll
+            for (int q = 0; q < TU_RA_SPLIT; ++q)
+                pv[q] = q < ra_split ? __ldcg(D.rapart + ((size_t)(tr * ra_split + q) * CT + c) * 128 + (tid & 127)) : 0.0f;
+            float sum = 0.0f;
+#pragma unroll
+            for (int q = 0; q < TU_RA_SPLIT; ++q)
+                if (q < ra_split) sum += pv[q];
             const size_t o = (size_t)c * D.ldra + i;
-            const double v = D.ra[o] + (double)s;
+            const double v = D.ra[o] + (double)sum;
             D.ra[o] = v;
             D.ra32[o] = (float)v;
         }
@@ -327,11 +371,13 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
 }
 
 template <int CT>
-__global__ void __launch_bounds__(256, 2) k_update_tc(Dev D, int b, int ra_split)
+__global__ void __launch_bounds__(TC_THREADS, 2)
+    k_update_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_d, Dev D, int b,
+                int ra_split)
 {
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
     unsigned char *base = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
-    if ((int)blockIdx.x < D.nr_ctas) update_tc_rows<CT>(D, b, base);
+    if ((int)blockIdx.x < D.nr_ctas) update_tc_rows<CT>(&tm_codes, &tm_d, D, b, base);
     else update_tc_ra<CT>(D, b, ra_split, base);
 }
 
