@@ -84,7 +84,7 @@ __device__ __forceinline__ float code_to_f32(uint32_t w, int k)
 // three-way split of delta/sd per chain (dsplit; pairs up to `span`, past the
 // subset's end, write zeros) and per-CTA sums of x0_j delta_j (k0part).
 template <int MODE, int CT, bool TC>
-__global__ void __launch_bounds__(256) k_draw(Dev D, int b, int ksplit, int span)
+__global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int span)
 {
     __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring)
     __shared__ double s_k[256];
@@ -95,9 +95,11 @@ __global__ void __launch_bounds__(256) k_draw(Dev D, int b, int ksplit, int span
     const int N = D.blk_ls[b + 1] - ls;
     const bool act = jl < N;
     const int k = ls + (act ? jl : 0);
+    // prologue, overlapping the rhs kernel: the SNP's metadata and state (not
+    // written by the rhs kernel)
     const int snp = act && !D.skip[k] ? D.perm[k] : -1;
     double inv = 0.0, x0 = 0.0, gold = 0.0;
-    int cl = 0;
+    int cl = 0, sg = 0;
     if (snp >= 0) {
         if (MODE == SODAGPU_FP8 || TC) {
             inv = D.xv[(size_t)k * 4 + 3];
@@ -106,29 +108,24 @@ __global__ void __launch_bounds__(256) k_draw(Dev D, int b, int ksplit, int span
         if (MODE != SODAGPU_FP64) {
             gold = D.g[(size_t)c * D.p + snp];
             cl = D.cls[(size_t)c * D.p + snp];
+            sg = D.grp[snp] - 1;
         }
     }
-    double xr = 0.0, ur = 0.0;
-    if (snp >= 0) {
-        double px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
+    tc::pdl_trigger();
+    tc::pdl_wait();
+    // the rhs partial sums of all splits (added in split order) and sum(r)
+    double px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
 #pragma unroll
-        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
-            if (sp < ksplit) {
-                const size_t o = ((size_t)sp * CT + c) * D.bs + jl;
-                px[sp] = __ldcg(D.rpx + o);
-                pu[sp] = __ldcg(D.rpu + o);
-            }
-        }
-#pragma unroll
-        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
-            if (sp < ksplit) {
-                xr += px[sp];
-                ur += pu[sp];
-            }
+    for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+        px[sp] = pu[sp] = 0.0;
+        if (act && sp < ksplit) {
+            const size_t o = ((size_t)sp * CT + c) * D.bs + jl;
+            px[sp] = __ldcg(D.rpx + o);
+            pu[sp] = __ldcg(D.rpu + o);
         }
     }
     if (MODE == SODAGPU_FP8) {
-        // sum(r) per chain: 256/CT threads per chain over interleaved row tiles, then in part order
+        // 256/CT threads per chain over interleaved row tiles, then in part order
         constexpr int PARTS = 256 / CT;
         const int cc = tid / PARTS, part = tid % PARTS;
         double a = 0.0;
@@ -137,7 +134,7 @@ __global__ void __launch_bounds__(256) k_draw(Dev D, int b, int ksplit, int span
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int q = q0 + u * PARTS;
-                v[u] = q < D.nr_ctas ? D.rsum[(size_t)cc * D.nr_ctas + q] : 0.0;
+                v[u] = q < D.nr_ctas ? __ldcg(D.rsum + (size_t)cc * D.nr_ctas + q) : 0.0;
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) a += v[u];
@@ -151,6 +148,14 @@ __global__ void __launch_bounds__(256) k_draw(Dev D, int b, int ksplit, int span
         }
         __syncthreads();
     }
+    double xr = 0.0, ur = 0.0;
+#pragma unroll
+    for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+        if (sp < ksplit) {
+            xr += px[sp];
+            ur += pu[sp];
+        }
+    }
     double delta = 0.0;
     if (snp >= 0) {
         if (MODE == SODAGPU_FP8) xr = xr * inv + x0 * s_rs[c];
@@ -162,7 +167,8 @@ __global__ void __launch_bounds__(256) k_draw(Dev D, int b, int ksplit, int span
         if (MODE == SODAGPU_FP64)
             delta = draw_snp(D, S, c, cur_rep(D), snp, xr + ur, zz, zz / S->vare, R, &err);
         else
-            delta = draw_snp_f(D, S, c, snp, (float)(xr + ur), (float)zz, (float)(zz / S->vare), R, &err, gold, cl);
+            delta = draw_snp_f(D, S, c, snp, (float)(xr + ur), (float)zz, (float)(zz / S->vare), R, &err, gold, cl,
+                               sg);
         if (err) flag_err(D, 1);
     }
     if (act) {
@@ -207,6 +213,8 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     extern __shared__ __align__(16) unsigned char smem[];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    tc::pdl_trigger();
+    tc::pdl_wait();
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
     const int mt = blockIdx.x / ksplit, ks = blockIdx.x % ksplit;

@@ -11,13 +11,16 @@
 // FP32-accurate products with FP32 accumulation in tensor memory.  A CTA owns
 // one M tile and one K split of 128-individual stages and runs a
 // warp-specialised pipeline synchronised by mbarriers:
-//   warp 8  (one thread) TMA: the stage's 128 x 128 code tile (hardware
+//   warp 16 (one thread) TMA: the stage's 128 x 128 code tile (hardware
 //           128-byte swizzle) and the chains' 128 residuals into a raw buffer
 //           (TC_NS buffers in flight);
-//   warps 0-7 convert the raw buffer into the double-buffered bf16 operand
+//   warps 0-15 convert the raw buffer into the double-buffered bf16 operand
 //           tiles (codes; residual hi/mid/lo rows) and release both;
-//   warp 9  (one thread) issues the eight K=16 MMAs of the stage and commits
+//   warp 17 (one thread) issues the eight K=16 MMAs of the stage and commits
 //           their completion, which frees the operand buffer.
+// With programmatic dependent launch the prologue (barriers, tensor memory,
+// the first code tiles) overlaps the previous kernel; residuals are read
+// after it completes.
 // The augmenting part u_j' ra_c (5% of the work) then runs on the FP32 cores
 // from staged windows of U.  Partial sums go to rpx/rpu, added and drawn by
 // k_draw.
@@ -30,9 +33,9 @@ constexpr int TC_TM = 128;       // SNPs per M tile
 constexpr int TC_KC = 128;       // individuals per stage
 constexpr int TC_NS = 4;         // raw stages in flight
 constexpr int TC_UWR = 256;      // augmented rows per staging window of the U part
-constexpr int TC_THREADS = 320;  // 8 converter warps, the TMA warp, the MMA warp
-constexpr int TC_CONV = 256;     // converter threads
-constexpr int TC_WARP_TMA = 8, TC_WARP_MMA = 9;
+constexpr int TC_THREADS = 576;  // 16 converter warps, the TMA warp, the MMA warp
+constexpr int TC_CONV = 512;     // converter threads
+constexpr int TC_WARP_TMA = 16, TC_WARP_MMA = 17;
 
 template <int CT>
 struct RhsTc {
@@ -139,6 +142,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         s_err = 0;
     }
     if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 64);
+    tc::pdl_trigger();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -148,10 +152,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (lane == 0) {
             tc::tma_prefetch_desc(&tm_codes);
             tc::tma_prefetch_desc(&tm_r);
-            for (int s = 0; s < nck; ++s) {
+            // the first code tiles do not depend on the previous kernel
+            const int pre = nck < TC_NS ? nck : TC_NS;
+            for (int s = 0; s < pre; ++s) {
+                tc::mbar_expect_tx(&s_full[s], T::RAW);
+                tc::tma_load_2d(raw0 + (size_t)s * T::RAW, &tm_codes, (c0 + s) * TC_KC, ls + j0, &s_full[s]);
+            }
+            tc::pdl_wait();
+            for (int s = 0; s < pre; ++s)
+                tc::tma_load_2d(raw0 + (size_t)s * T::RAW + T::RAW_A, &tm_r, (c0 + s) * TC_KC, 0, &s_full[s]);
+            for (int s = pre; s < nck; ++s) {
                 const int buf = s % TC_NS;
                 // the buffer's previous stage has been converted
-                if (s >= TC_NS && !tc::mbar_wait(&s_empty[buf], ((s / TC_NS) - 1) & 1)) {
+                if (!tc::mbar_wait(&s_empty[buf], ((s / TC_NS) - 1) & 1)) {
                     s_err = 1;
                     break;
                 }
@@ -161,8 +174,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 tc::tma_load_2d(rw, &tm_codes, i0, ls + j0, &s_full[buf]);
                 tc::tma_load_2d(rw + T::RAW_A, &tm_r, i0, 0, &s_full[buf]);
             }
+        } else {
+            tc::pdl_wait();
         }
     } else if (warp == TC_WARP_MMA) {
+        tc::pdl_wait();
         if (lane == 0 && nck > 0) {
             const uint32_t idesc = tc::idesc_bf16(TC_TM, NB);
             for (int s = 0; s < nck; ++s) {
@@ -185,6 +201,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc::mma_commit(&s_done);
         }
     } else {
+        tc::pdl_wait();
         // converters: raw stage -> bf16 operand tiles
         for (int s = 0; s < nck; ++s) {
             const int buf = s % TC_NS, ob = s & 1;
@@ -268,9 +285,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     // augmenting part on the FP32 cores: this split's share of the U rows of
     // the tile's columns (upper triangular: rows up to the tile's last
-    // column), staged by windows of TC_UWR rows with cp.async; warp w owns
-    // columns 16w..16w+15 (four at a time), lanes run over rows, and the
-    // 4 x CT lane sums are reduced by a transposing butterfly.
+    // column), staged by windows of TC_UWR rows with cp.async; converter warp
+    // w owns 8 columns (four at a time), lanes run over rows, and the 4 x CT
+    // lane sums are reduced by a transposing butterfly.
     const int npad = (N + 7) & ~7;
     const int rowsU = D.blk_pd[b] ? min(npad, j0 + TC_TM) : npad;
     const int nUc = (rowsU + 31) / 32;
@@ -298,8 +315,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         __pipeline_wait_prior(0);
         __syncthreads();
 #pragma unroll 1
-        for (int g = 0; g < (warp < 8 ? 4 : 0); ++g) {
-            const int jq = warp * 16 + g * 4;
+        for (int g = 0; g < (warp < TC_CONV / 32 ? TC_TM / (4 * (TC_CONV / 32)) : 0); ++g) {
+            const int jq = warp * (TC_TM / (TC_CONV / 32)) + g * 4;
             float acc[4 * CT];
 #pragma unroll
             for (int v = 0; v < 4 * CT; ++v) acc[v] = 0.0f;

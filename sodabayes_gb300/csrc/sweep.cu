@@ -62,7 +62,7 @@ __device__ __forceinline__ void flag_err(const Dev &D, int code)
 // Per-SNP conditional draw inside a subset.  Returns delta = g_old - g_new.
 // Restates models.f90:146-161 (BayesA), 211-255 (BayesB), 350-412 (C/Cpi/R/Rc).
 // ---------------------------------------------------------------------------
-__device__ double draw_snp(const Dev &D, const ChainScal *S, int c, int rep, int snploc,
+__device__ __forceinline__ double draw_snp(const Dev &D, const ChainScal *S, int c, int rep, int snploc,
                            double rhs, double zz, double zz_vare, CRng &R, int *err)
 {
     const size_t o = (size_t)c * D.p + snploc;
@@ -152,10 +152,10 @@ __device__ double draw_snp(const Dev &D, const ChainScal *S, int c, int rep, int
 // The same draw in FP32 arithmetic, for the FP32/FP8 sweeps: GB300 executes
 // FP64 at a small fraction of its FP32 rate, and the draws of a subset sit on
 // the critical path of every subset.  State stays FP64.
-// gold = g and cl = class of the SNP in this chain, loaded by the caller
-// ahead of the draw (they sit on the draw's critical path).
-__device__ double draw_snp_f(const Dev &D, const ChainScal *S, int c, int snploc, float rhs, float zz,
-                             float zz_vare, CRng &R, int *err, double gold, int cl)
+// gold = g and cl = class of the SNP in this chain, sg = its group - 1, all
+// loaded by the caller ahead of the draw (they sit on its critical path).
+__device__ __forceinline__ double draw_snp_f(const Dev &D, const ChainScal *S, int c, int snploc, float rhs, float zz,
+                             float zz_vare, CRng &R, int *err, double gold, int cl, int sg)
 {
     const size_t o = (size_t)c * D.p + snploc;
     const float vare = (float)S->vare;
@@ -203,7 +203,6 @@ __device__ double draw_snp_f(const Dev &D, const ChainScal *S, int c, int snploc
         return gold - gnew;
     }
     const int nm = D.nmix;
-    const int sg = D.grp[snploc] - 1;
     float sv[MAXDIST];
     sv[0] = (float)S->log_p[sg];
     for (int kk = 1; kk < nm; ++kk) {
@@ -772,6 +771,26 @@ struct ProfScope {
     }
 };
 
+// Launch with programmatic stream serialization: the kernel may start while
+// the previous one in the stream finishes; it calls griddepcontrol.wait before
+// reading that kernel's results.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // Tensor-core subset: rhs tiles of 128 SNPs x K splits (one wave of one CTA
 // per SM), then the update (row tiles of r on the tensor cores, ra tiles on
 // the FP32 cores; two CTAs per SM).
@@ -784,21 +803,26 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
     int ks = sm_count / mtiles;
     ks = ks < 1 ? 1 : (ks > RHS_KSPLIT_MAX ? RHS_KSPLIT_MAX : ks);
     ks = ks > nst ? nst : ks;
+    cudaError_t e;
     {
         ProfScope ps(prof, st, PROF_RHS);
-        k_rhs_tc<CT><<<mtiles * ks, TC_THREADS, RhsTc<CT>::SMEM, st>>>(maps->codes128, maps->r, D, b, ks);
+        e = launch_pdl(k_rhs_tc<CT>, dim3(mtiles * ks), dim3(TC_THREADS), RhsTc<CT>::SMEM, st, maps->codes128,
+                       maps->r, D, b, ks);
     }
+    if (e != cudaSuccess) return e;
     {
         const int span = mtiles * TC_TM;
         ProfScope ps(prof, st, PROF_DRAW);
-        k_draw<SODAGPU_FP8, CT, true><<<(span * CT + 255) / 256, 256, 0, st>>>(D, b, ks, span);
+        e = launch_pdl(k_draw<SODAGPU_FP8, CT, true>, dim3((span * CT + 255) / 256), dim3(256), 0, st, D, b, ks, span);
     }
+    if (e != cudaSuccess) return e;
     const int ra_tiles = (nblk_snps + 127) / 128;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
-        k_update_tc<CT><<<D.nr_ctas + ra_tiles * TU_RA_SPLIT, TC_THREADS, UpdTc<CT>::SMEM, st>>>(
-            maps->codes64, maps->d, D, b, TU_RA_SPLIT);
+        e = launch_pdl(k_update_tc<CT>, dim3(D.nr_ctas + ra_tiles * TU_RA_SPLIT), dim3(TU_THREADS), UpdTc<CT>::SMEM,
+                       st, maps->codes64, maps->d, D, b, TU_RA_SPLIT);
     }
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
@@ -816,20 +840,25 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
     int ks = sm_count / mtiles;
     ks = ks < 1 ? 1 : (ks > RHS_KSPLIT_MAX ? RHS_KSPLIT_MAX : ks);
     ks = ks > nst ? nst : ks;
+    cudaError_t e;
     {
         ProfScope ps(prof, st, PROF_RHS);
-        k_rhs<MODE, CT><<<mtiles * ks, 256, rhs_smem_bytes<MODE, CT>(), st>>>(D, b, ks);
+        e = launch_pdl(k_rhs<MODE, CT>, dim3(mtiles * ks), dim3(256), rhs_smem_bytes<MODE, CT>(), st, D, b, ks);
     }
+    if (e != cudaSuccess) return e;
     {
         ProfScope ps(prof, st, PROF_DRAW);
-        k_draw<MODE, CT, false><<<(nblk_snps * CT + 255) / 256, 256, 0, st>>>(D, b, ks, nblk_snps);
+        e = launch_pdl(k_draw<MODE, CT, false>, dim3((nblk_snps * CT + 255) / 256), dim3(256), 0, st, D, b, ks,
+                       nblk_snps);
     }
+    if (e != cudaSuccess) return e;
     const int ntile = D.nr_ctas + (D.bs + UT - 1) / UT;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
-        k_update<MODE, CT><<<ntile, 32 * UpdWarps<MODE, CT>::v, update_smem_bytes_ct<MODE, CT>(D.bs), st>>>(D, b);
+        e = launch_pdl(k_update<MODE, CT>, dim3(ntile), dim3(32 * UpdWarps<MODE, CT>::v),
+                       update_smem_bytes_ct<MODE, CT>(D.bs), st, D, b);
     }
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int MODE>

@@ -118,6 +118,19 @@ __device__ __forceinline__ void tma_prefetch_desc(const void *tmap)
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
 }
 
+// Programmatic dependent launch: wait for the preceding grid (no-op when the
+// kernel was launched without the attribute), and allow the next grid to
+// start its prologue.
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+__device__ __forceinline__ void pdl_trigger()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ void fence_async_smem()
 {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

@@ -42,6 +42,8 @@ __global__ void __launch_bounds__(32 * UpdWarps<MODE, CT>::v) k_update(Dev D, in
     __shared__ int s_n;
     __shared__ double sh[33];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    tc::pdl_trigger();
+    tc::pdl_wait();
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
     const int npad = (N + 7) & ~7;

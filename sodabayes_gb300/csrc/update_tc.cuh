@@ -26,7 +26,10 @@ constexpr int TU_KC = 64;          // subset positions per stage
 constexpr int TU_NS = 4;           // raw stages in flight
 constexpr int TU_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
 constexpr int TU_RA_SPLIT = 8;     // CTAs per 128-row tile of ra
-constexpr int TU_UNR = 4;          // U columns in flight per warp
+constexpr int TU_UNR = 8;          // U columns in flight per warp
+constexpr int TU_THREADS = 320;    // 8 converter warps, the TMA warp, the MMA warp
+constexpr int TU_CONV = 256;
+constexpr int TU_WARP_TMA = 8, TU_WARP_MMA = 9;
 
 template <int CT>
 struct UpdTc {
@@ -36,7 +39,7 @@ struct UpdTc {
     static constexpr int RAW = RAW_A + RAW_B;
     static constexpr int OP = 128 * TU_KC * 2;         // bf16 codes, individual-major (MMA operand A)
     static constexpr int PIPE = 2 * OP + TU_NS * RAW;
-    static constexpr int RED = 8 * 8 * 128 * 4;        // warp partials of the ra tiles (8 chains a pass)
+    static constexpr int RED = 4 * CT * 128 * 4;       // column-group partials of the ra tiles
     static constexpr size_t SMEM = 1024 + (size_t)(PIPE > RED ? PIPE : RED);
     static_assert(OP % 1024 == 0 && RAW % 1024 == 0 && RAW_A % 1024 == 0, "buffers must keep 1024-byte alignment");
 };
@@ -47,14 +50,14 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
 {
     using T = UpdTc<CT>;
     constexpr int NB = T::NB;
-    constexpr int NW = TC_THREADS / 32;
+    constexpr int NW = TU_THREADS / 32;
     __shared__ uint64_t s_full[TU_NS], s_empty[TU_NS], s_conv[2], s_opfree[2], s_done;
     __shared__ uint32_t s_tmem;
     __shared__ int s_err, s_nact, s_wcnt[NW + 1];
     __shared__ int s_act[TU_MAXQ];
     __shared__ double s_k0[CT];
-    __shared__ double s_k0p[TC_CONV];
-    __shared__ double s_rsw[4][CT];
+    __shared__ double s_k0p[TU_CONV];
+    __shared__ double s_rsw[8][CT];
     unsigned char *op0 = base;
     unsigned char *raw0 = base + 2 * T::OP;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -62,6 +65,8 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
     const int N = D.blk_ls[b + 1] - ls;
     const int tile = blockIdx.x, t0 = tile * 128;
     const int nq = (N + TU_KC - 1) / TU_KC;
+    tc::pdl_trigger();
+    tc::pdl_wait();   // the draws of this subset are complete
 
     // stages with a non-zero delta, in subset order (nq <= 256)
     {
@@ -82,12 +87,21 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
         const unsigned m = __ballot_sync(0xffffffffu, f);
         if (lane == 0) s_wcnt[warp] = __popc(m);
         // the centring term: 256/CT threads per chain over interleaved draw CTAs, then in part order
-        constexpr int PARTS = TC_CONV / CT;
-        if (tid < TC_CONV) {
+        constexpr int PARTS = TU_CONV / CT;
+        if (tid < TU_CONV) {
             const int c = tid / PARTS, part = tid % PARTS;
             const int ntl = (((N + TC_TM - 1) / TC_TM) * TC_TM * CT + 255) / 256;
             double a = 0.0;
-            for (int q = part; q < ntl; q += PARTS) a += D.k0part[(size_t)q * CT + c];
+            for (int q0 = part; q0 < ntl; q0 += 8 * PARTS) {
+                double v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int q = q0 + u * PARTS;
+                    v[u] = q < ntl ? D.k0part[(size_t)q * CT + c] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) a += v[u];
+            }
             s_k0p[tid] = a;
         }
         __syncthreads();
@@ -115,23 +129,23 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
     if (tid == 0) {
         for (int i = 0; i < TU_NS; ++i) {
             tc::mbar_init(&s_full[i], 1);
-            tc::mbar_init(&s_empty[i], TC_CONV + 1);   // converters + the MMAs reading the delta split
+            tc::mbar_init(&s_empty[i], TU_CONV + 1);   // converters + the MMAs reading the delta split
         }
         for (int i = 0; i < 2; ++i) {
-            tc::mbar_init(&s_conv[i], TC_CONV);
+            tc::mbar_init(&s_conv[i], TU_CONV);
             tc::mbar_init(&s_opfree[i], 1);
         }
         tc::mbar_init(&s_done, 1);
         tc::mbar_fence_init();
         s_err = 0;
     }
-    if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 64);
+    if (warp == TU_WARP_MMA) tc::tmem_alloc(&s_tmem, 64);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tm = s_tmem;
 
-    if (warp == TC_WARP_TMA) {
+    if (warp == TU_WARP_TMA) {
         if (lane == 0) {
             tc::tma_prefetch_desc(tm_codes);
             tc::tma_prefetch_desc(tm_d);
@@ -148,7 +162,7 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
                 tc::tma_load_2d(rw + T::RAW_A, tm_d, k0, 0, &s_full[buf]);
             }
         }
-    } else if (warp == TC_WARP_MMA) {
+    } else if (warp == TU_WARP_MMA) {
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_bf16(128, NB);
             for (int s = 0; s < nact; ++s) {
@@ -228,57 +242,65 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
     const bool ok = !s_err;
     if (!ok && tid == 0) flag_err(D, 4);
     tc::fence_after_sync();
-    if (warp < 4) {
-        const int i = t0 + warp * 32 + lane;
+    // epilogue: warps w and w+4 read the same 32 accumulator rows, each for half of the chains
+    constexpr int HALF = CT >= 8 ? CT / 2 : CT;
+    const int h = warp >> 2;
+    if (warp < 8 && h * HALF < CT) {
+        const int i = t0 + (warp & 3) * 32 + lane;
         const bool row_ok = i < D.n;
-        double rv[CT];
+        double rv[HALF];
 #pragma unroll
-        for (int c = 0; c < CT; ++c) rv[c] = row_ok ? D.r[(size_t)c * D.ldr + i] : 0.0;
+        for (int c = 0; c < HALF; ++c) rv[c] = row_ok ? D.r[(size_t)(h * HALF + c) * D.ldr + i] : 0.0;
 #pragma unroll
-        for (int g = 0; g < CT / 8 + (CT % 8 ? 1 : 0); ++g) {
-            // chains 8g .. 8g+7: their hi, mid and lo accumulator columns
+        for (int g = 0; g < (HALF + 7) / 8; ++g) {
+            // chains h*HALF + 8g ..: their hi, mid and lo accumulator columns
             float hi[8], md[8], lo[8];
-            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + 8 * g, hi);
-            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + CT + 8 * g, md);
-            tc::tmem_ld8(tm + ((uint32_t)(warp * 32) << 16) + 2 * CT + 8 * g, lo);
+            const uint32_t ta = tm + ((uint32_t)((warp & 3) * 32) << 16) + h * HALF + 8 * g;
+            tc::tmem_ld8(ta, hi);
+            tc::tmem_ld8(ta + CT, md);
+            tc::tmem_ld8(ta + 2 * CT, lo);
             tc::tmem_wait_ld();
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-                const int c = 8 * g + e;
-                if (c < CT && ok && row_ok) rv[c] += (double)((hi[e] + md[e]) + lo[e]) + s_k0[c];
+                const int cl = 8 * g + e;
+                if (cl < HALF && ok && row_ok) rv[cl] += (double)((hi[e] + md[e]) + lo[e]) + s_k0[h * HALF + cl];
             }
         }
         if (ok && row_ok) {
 #pragma unroll
-            for (int c = 0; c < CT; ++c) {
-                D.r[(size_t)c * D.ldr + i] = rv[c];
-                D.r32[(size_t)c * D.ldr + i] = (float)rv[c];
+            for (int c = 0; c < HALF; ++c) {
+                D.r[(size_t)(h * HALF + c) * D.ldr + i] = rv[c];
+                D.r32[(size_t)(h * HALF + c) * D.ldr + i] = (float)rv[c];
             }
         }
 #pragma unroll
-        for (int c = 0; c < CT; ++c) {
+        for (int c = 0; c < HALF; ++c) {
             const double v = warp_sum(rv[c]);
             if (lane == 0) s_rsw[warp][c] = v;
         }
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == TC_WARP_MMA) {
+    if (warp == TU_WARP_MMA) {
         tc::fence_after_sync();
         tc::tmem_dealloc(tm, 64);
     }
     // this tile's partial sum of r (the centring of the next subset)
-    if (tid < CT)
-        D.rsum[(size_t)tid * D.nr_ctas + tile] = ((s_rsw[0][tid] + s_rsw[1][tid]) + s_rsw[2][tid]) + s_rsw[3][tid];
+    if (tid < CT) {
+        const int hh = tid / HALF, cl = tid % HALF;
+        D.rsum[(size_t)tid * D.nr_ctas + tile] =
+            ((s_rsw[4 * hh][cl] + s_rsw[4 * hh + 1][cl]) + s_rsw[4 * hh + 2][cl]) + s_rsw[4 * hh + 3][cl];
+    }
 }
 
 template <int CT>
 __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, unsigned char *base)
 {
-    constexpr int CP = CT < 8 ? CT : 8;   // chains per pass (keeps the accumulators in registers)
     __shared__ int s_last;
-    float *s_red = reinterpret_cast<float *>(base);   // [8 warps][CP][128]
+    float *s_red = reinterpret_cast<float *>(base);   // [4 column groups][CT][128 rows]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    tc::pdl_trigger();
+    tc::pdl_wait();   // the draws of this subset are complete
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
     const int npad = (N + 7) & ~7;
@@ -288,60 +310,55 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
     const int kbeg = D.blk_pd[b] ? min(i0, N) : 0;   // upper triangular: rows i only meet columns k >= i
     const int ka = kbeg + (int)(((long long)(N - kbeg) * sp) / ra_split);
     const int kb = kbeg + (int)(((long long)(N - kbeg) * (sp + 1)) / ra_split);
-    const int ii = i0 + 4 * lane;
-    const bool rows_ok = ii + 4 <= npad;
+    // warp w of 8: rows i0 + 64*(w&1) + 2*lane (+1), columns ka + (w>>1) + 4q; the TMA/MMA warps idle here
+    const int rh = warp & 1, cg = warp >> 1;
+    const int ii = i0 + 64 * rh + 2 * lane;
+    const bool rows_ok = ii + 2 <= npad;
+    float acc[2][CT];
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[e][c] = 0.0f;
+    for (int k0 = ka + cg; warp < 8 && k0 < kb; k0 += 4 * TU_UNR) {
+        float2 u[TU_UNR];
+        int kk[TU_UNR];
+#pragma unroll
+        for (int q = 0; q < TU_UNR; ++q) {
+            const int k = k0 + 4 * q;
+            kk[q] = (k < kb && D.nzflag[k]) ? k : -1;
+            u[q] = make_float2(0.f, 0.f);
+            if (kk[q] >= 0 && rows_ok) u[q] = *reinterpret_cast<const float2 *>(D.U32 + D.uoff[ls + k] + ii);
+        }
+#pragma unroll
+        for (int q = 0; q < TU_UNR; ++q) {
+            if (kk[q] < 0) continue;
+#pragma unroll
+            for (int c = 0; c < CT; c += 4) {
+                const float4 v = *reinterpret_cast<const float4 *>(D.delta32 + (size_t)kk[q] * CT + c);
+                acc[0][c] = fmaf(u[q].x, v.x, acc[0][c]);
+                acc[1][c] = fmaf(u[q].y, v.x, acc[1][c]);
+                acc[0][c + 1] = fmaf(u[q].x, v.y, acc[0][c + 1]);
+                acc[1][c + 1] = fmaf(u[q].y, v.y, acc[1][c + 1]);
+                acc[0][c + 2] = fmaf(u[q].x, v.z, acc[0][c + 2]);
+                acc[1][c + 2] = fmaf(u[q].y, v.z, acc[1][c + 2]);
+                acc[0][c + 3] = fmaf(u[q].x, v.w, acc[0][c + 3]);
+                acc[1][c + 3] = fmaf(u[q].y, v.w, acc[1][c + 3]);
+            }
+        }
+    }
+    if (warp < 8) {
+#pragma unroll
+        for (int c = 0; c < CT; ++c) {
+            s_red[(cg * CT + c) * 128 + 64 * rh + 2 * lane] = acc[0][c];
+            s_red[(cg * CT + c) * 128 + 64 * rh + 2 * lane + 1] = acc[1][c];
+        }
+    }
+    __syncthreads();
     float *part = D.rapart + ((size_t)(tr * ra_split + sp) * CT) * 128;
-    for (int cp0 = 0; cp0 < CT; cp0 += CP) {
-        float acc[4][CP];
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-#pragma unroll
-            for (int c = 0; c < CP; ++c) acc[e][c] = 0.0f;
-        // warp w of 8 takes columns ka+w, ka+w+8, ...; the MMA/TMA warps idle here
-        for (int k0 = ka + warp; warp < 8 && k0 < kb; k0 += 8 * TU_UNR) {
-            float4 u[TU_UNR];
-            int kk[TU_UNR];
-#pragma unroll
-            for (int q = 0; q < TU_UNR; ++q) {
-                const int k = k0 + 8 * q;
-                kk[q] = (k < kb && D.nzflag[k]) ? k : -1;
-                u[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (kk[q] >= 0 && rows_ok) u[q] = *reinterpret_cast<const float4 *>(D.U32 + D.uoff[ls + k] + ii);
-            }
-#pragma unroll
-            for (int q = 0; q < TU_UNR; ++q) {
-                if (kk[q] < 0) continue;
-                float dl[CP];
-#pragma unroll
-                for (int c = 0; c < CP; c += 4) {
-                    const float4 v = *reinterpret_cast<const float4 *>(D.delta32 + (size_t)kk[q] * CT + cp0 + c);
-                    dl[c] = v.x; dl[c + 1] = v.y; dl[c + 2] = v.z; dl[c + 3] = v.w;
-                }
-#pragma unroll
-                for (int c = 0; c < CP; ++c) {
-                    acc[0][c] = fmaf(u[q].x, dl[c], acc[0][c]);
-                    acc[1][c] = fmaf(u[q].y, dl[c], acc[1][c]);
-                    acc[2][c] = fmaf(u[q].z, dl[c], acc[2][c]);
-                    acc[3][c] = fmaf(u[q].w, dl[c], acc[3][c]);
-                }
-            }
-        }
-        if (warp < 8) {
-#pragma unroll
-            for (int c = 0; c < CP; ++c)
-#pragma unroll
-                for (int e = 0; e < 4; ++e) s_red[(warp * CP + c) * 128 + 4 * lane + e] = acc[e][c];
-        }
-        __syncthreads();
-        if (tid < 128) {
-            for (int c = 0; c < CP; ++c) {
-                float sum = 0.0f;
-#pragma unroll
-                for (int w = 0; w < 8; ++w) sum += s_red[(w * CP + c) * 128 + tid];
-                part[(cp0 + c) * 128 + tid] = sum;
-            }
-        }
-        __syncthreads();
+    for (int t = tid; t < CT * 128; t += TU_THREADS) {
+        const int c = t >> 7, rl = t & 127;
+        part[c * 128 + rl] = ((s_red[(0 * CT + c) * 128 + rl] + s_red[(1 * CT + c) * 128 + rl]) +
+                              s_red[(2 * CT + c) * 128 + rl]) + s_red[(3 * CT + c) * 128 + rl];
     }
     __threadfence();
     __syncthreads();
@@ -350,28 +367,27 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
     if (!s_last) return;
     __threadfence();
     // the last CTA of the row tile: split partial sums in split order
-    const int i = i0 + (tid & 127);
-    if (tid < 256 && i < D.bs) {
-        for (int c = tid >> 7; c < CT; c += 2) {
-            float pv[TU_RA_SPLIT];
+    for (int t = tid; t < CT * 128; t += TU_THREADS) {
+        const int c = t >> 7, rl = t & 127, i = i0 + rl;
+        if (i >= D.bs) continue;
+        float pv[TU_RA_SPLIT];
 #pragma unroll
-            for (int q = 0; q < TU_RA_SPLIT; ++q)
-                pv[q] = q < ra_split ? __ldcg(D.rapart + ((size_t)(tr * ra_split + q) * CT + c) * 128 + (tid & 127)) : 0.0f;
-            float sum = 0.0f;
+        for (int q = 0; q < TU_RA_SPLIT; ++q)
+            pv[q] = q < ra_split ? __ldcg(D.rapart + ((size_t)(tr * ra_split + q) * CT + c) * 128 + rl) : 0.0f;
+        float sum = 0.0f;
 #pragma unroll
-            for (int q = 0; q < TU_RA_SPLIT; ++q)
-                if (q < ra_split) sum += pv[q];
-            const size_t o = (size_t)c * D.ldra + i;
-            const double v = D.ra[o] + (double)sum;
-            D.ra[o] = v;
-            D.ra32[o] = (float)v;
-        }
+        for (int q = 0; q < TU_RA_SPLIT; ++q)
+            if (q < ra_split) sum += pv[q];
+        const size_t o = (size_t)c * D.ldra + i;
+        const double v = D.ra[o] + (double)sum;
+        D.ra[o] = v;
+        D.ra32[o] = (float)v;
     }
     if (tid == 0) D.raticket[tr] = 0;
 }
 
 template <int CT>
-__global__ void __launch_bounds__(TC_THREADS, 2)
+__global__ void __launch_bounds__(TU_THREADS, 2)
     k_update_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_d, Dev D, int b,
                 int ra_split)
 {
