@@ -157,6 +157,8 @@ struct sodagpu_ctx {
     float *rapart = nullptr;
     int32_t *raticket = nullptr;
     TcMaps maps{};
+    std::vector<int32_t> h_rtab, h_atab;   // work tables of the tensor-core sweep
+    int32_t *rtab = nullptr, *atab = nullptr;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
     cudaGraphExec_t graph = nullptr;
@@ -752,6 +754,9 @@ int build_dev(sodagpu_ctx *c)
     D.k0part = c->k0part;
     D.rapart = c->rapart;
     D.raticket = c->raticket;
+    D.rtab = c->rtab;
+    D.atab = c->atab;
+    D.tstride = sweep_tc_table_stride(c->bs);
     return 0;
 }
 
@@ -793,8 +798,19 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             c->ldd = (int)round_up((size_t)c->bs, 128);
             TRY(c->alloc(&c->dsplit, (size_t)sweep_tc_rows(C) * c->ldd));
             TRY(c->alloc(&c->k0part, (((size_t)c->ldd * C + 255) / 256) * C));
-            TRY(c->alloc(&c->rapart, (size_t)mt * sweep_tc_ra_split() * C * 128));
+            TRY(c->alloc(&c->rapart, (size_t)mt * (sweep_tc_ra_split() + 1) * C * 128));
             TRY(c->alloc(&c->raticket, mt));
+            const int ts = sweep_tc_table_stride(c->bs);
+            c->h_rtab.assign((size_t)c->nb * ts, 0);
+            c->h_atab.assign((size_t)c->nb * ts, 0);
+            sweep_tc_tables(c->blk_sizes.data(), c->nb, c->bs, c->ldx, c->sm_count, c->h_rtab.data(),
+                            c->h_atab.data());
+            TRY(c->alloc(&c->rtab, c->h_rtab.size(), false));
+            TRY(c->alloc(&c->atab, c->h_atab.size(), false));
+            CUDA_TRY(cudaMemcpyAsync(c->rtab, c->h_rtab.data(), c->h_rtab.size() * 4, cudaMemcpyHostToDevice, c->st));
+            CUDA_TRY(cudaMemcpyAsync(c->atab, c->h_atab.data(), c->h_atab.size() * 4, cudaMemcpyHostToDevice, c->st));
+            c->maps.h_rtab = c->h_rtab.data();
+            c->maps.h_atab = c->h_atab.data();
         }
     }
     build_dev(c);

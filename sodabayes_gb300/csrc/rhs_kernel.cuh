@@ -80,7 +80,8 @@ __device__ __forceinline__ float code_to_f32(uint32_t w, int k)
 // (SNP, chain) pair, chains of a SNP in consecutive lanes (CT divides 32).
 // Every load a draw needs is issued up front: the SNP's metadata and state,
 // and the partial sums of all splits at once (added in split order).  With
-// TC the kernel also writes what the tensor-core update reads: the bf16
+// TC the kernel also writes what the tensor-core update reads (and takes the
+// split count of each SNP's tile from D.rtab): the bf16
 // three-way split of delta/sd per chain (dsplit; pairs up to `span`, past the
 // subset's end, write zeros) and per-CTA sums of x0_j delta_j (k0part).
 template <int MODE, int CT, bool TC>
@@ -110,6 +111,10 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
             cl = D.cls[(size_t)c * D.p + snp];
             sg = D.grp[snp] - 1;
         }
+    }
+    if (TC && act) {   // the tensor-core rhs gives each 128-SNP tile its own number of splits
+        const int32_t *rt = D.rtab + (size_t)b * D.tstride + jl / 128;
+        ksplit = rt[1] - rt[0];
     }
     tc::pdl_trigger();
     tc::pdl_wait();

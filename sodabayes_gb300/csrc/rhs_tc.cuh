@@ -14,8 +14,9 @@
 //   warp 16 (one thread) TMA: the stage's 128 x 128 code tile (hardware
 //           128-byte swizzle) and the chains' 128 residuals into a raw buffer
 //           (TC_NS buffers in flight);
-//   warps 0-15 convert the raw buffer into the double-buffered bf16 operand
-//           tiles (codes; residual hi/mid/lo rows) and release both;
+//   warps 0-15 convert the raw buffer into the double-buffered bf16 operands
+//           (codes: tensor memory, lane = SNP, written with tcgen05.st;
+//           residual hi/mid/lo rows: shared memory) and release both;
 //   warp 17 (one thread) issues the eight K=16 MMAs of the stage and commits
 //           their completion, which frees the operand buffer.
 // With programmatic dependent launch the prologue (barriers, tensor memory,
@@ -31,8 +32,7 @@ namespace soda {
 
 constexpr int TC_TM = 128;       // SNPs per M tile
 constexpr int TC_KC = 128;       // individuals per stage
-constexpr int TC_NS = 4;         // raw stages in flight
-constexpr int TC_UWR = 256;      // augmented rows per staging window of the U part
+constexpr int TC_NS = 6;         // raw stages in flight
 constexpr int TC_THREADS = 576;  // 16 converter warps, the TMA warp, the MMA warp
 constexpr int TC_CONV = 512;     // converter threads
 constexpr int TC_WARP_TMA = 16, TC_WARP_MMA = 17;
@@ -43,14 +43,15 @@ struct RhsTc {
     static constexpr int RAW_A = TC_TM * TC_KC;            // codes (TMA box 128 x 128, 128-byte swizzle)
     static constexpr int RAW_B = CT * TC_KC * 4;           // FP32 residuals (TMA box 128 x CT)
     static constexpr int RAW = RAW_A + RAW_B;
-    static constexpr int OP_A = TC_TM * TC_KC * 2;         // bf16 codes, two 64-wide K regions
-    static constexpr int OP_B = NB * TC_KC * 2;
-    static constexpr int OP = OP_A + OP_B;
+    static constexpr int OP_B = NB * TC_KC * 2;            // bf16 residual split, two 64-wide K regions
+    static constexpr int OP = OP_B;                        // (the codes operand lives in tensor memory)
     static constexpr size_t SMEM = 1024 + 2 * (size_t)OP + (size_t)TC_NS * RAW;
     static_assert(OP % 1024 == 0 && RAW % 1024 == 0, "operand and raw buffers must keep 1024-byte alignment");
-    // U part: a window of the tile's 128 U columns and the chains' ra, plus the partial sums
-    static constexpr size_t UPART = (size_t)(TC_TM + CT) * TC_UWR * 4 + (size_t)TC_TM * CT * 4;
-    static_assert(UPART <= 2 * (size_t)OP + (size_t)TC_NS * RAW, "U window must fit the pipeline buffers");
+    // U part: a window of UWR rows of the tile's 128 U columns and the chains' ra, plus the partial sums
+    static constexpr size_t PIPE = 2 * (size_t)OP + (size_t)TC_NS * RAW;
+    static constexpr size_t upart(int rows) { return (size_t)(TC_TM + CT) * rows * 4 + (size_t)TC_TM * CT * 4; }
+    static constexpr int UWR = upart(256) <= PIPE ? 256 : (upart(192) <= PIPE ? 192 : 128);
+    static_assert(upart(UWR) <= PIPE, "U window must fit the pipeline buffers");
 };
 
 // Transposing butterfly: V values per lane summed over the warp's 32 lanes.
@@ -96,8 +97,7 @@ __device__ __forceinline__ int xreduce_base(int lane)
 
 template <int CT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_rhs_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_r, Dev D, int b,
-             int ksplit)
+    k_rhs_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_r, Dev D, int b)
 {
     using T = RhsTc<CT>;
     constexpr int NB = T::NB;
@@ -112,9 +112,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
-    const int mt = blockIdx.x / ksplit, ks = blockIdx.x % ksplit;
+    // this CTA's SNP tile and K split (tiles get splits in proportion to their work)
+    const int32_t *rt = D.rtab + (size_t)b * D.tstride;
+    const int mtiles = (N + TC_TM - 1) / TC_TM;
+    int mt = 0;
+    while (mt + 1 < mtiles && rt[mt + 1] <= (int)blockIdx.x) ++mt;
+    const int ksplit = rt[mt + 1] - rt[mt], ks = (int)blockIdx.x - rt[mt];
     const int j0 = mt * TC_TM;
-    if (j0 >= N) return;
+    if (j0 >= N || ks >= ksplit) return;
     const int nG = D.ldx / TC_KC;
     const int c0 = (int)(((long long)nG * ks) / ksplit), c1 = (int)(((long long)nG * (ks + 1)) / ksplit);
     const int nck = c1 - c0;
@@ -124,8 +129,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int t = tid; t < 2 * (NB - 3 * CT) * (TC_KC / 8); t += TC_THREADS) {
             const int ob = t / ((NB - 3 * CT) * (TC_KC / 8)), r = t % ((NB - 3 * CT) * (TC_KC / 8));
             const int n = 3 * CT + r / (TC_KC / 8), q = r % (TC_KC / 8);
-            *reinterpret_cast<uint4 *>(op0 + ob * T::OP + T::OP_A + tc::sw128_off(n, 8 * q, NB)) =
-                make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4 *>(op0 + ob * T::OP + tc::sw128_off(n, 8 * q, NB)) = make_uint4(0, 0, 0, 0);
         }
     }
     if (tid == 0) {
@@ -141,7 +145,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc::mbar_fence_init();
         s_err = 0;
     }
-    if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 64);
+    if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 256);   // accumulator 0-63, codes operand 64-191
     tc::pdl_trigger();
     tc::fence_before_sync();
     __syncthreads();
@@ -188,13 +192,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t a0 = tc::smem_u32(op0 + ob * T::OP), b0 = a0 + T::OP_A;
+                const uint32_t ta = tm + 64 + 64 * ob, b0 = tc::smem_u32(op0 + ob * T::OP);
 #pragma unroll
                 for (int kk = 0; kk < TC_KC / 16; ++kk) {
-                    const uint32_t ka = (kk >> 2) * (TC_TM * 128) + (kk & 3) * 32;
                     const uint32_t kb = (kk >> 2) * (NB * 128) + (kk & 3) * 32;
-                    tc::mma_bf16(tm, tc::desc_sw128(a0 + ka, 1024), tc::desc_sw128(b0 + kb, 1024), idesc,
-                                 (s | kk) != 0 ? 1u : 0u);
+                    tc::mma_bf16_ta(tm, ta + 8 * kk, tc::desc_sw128(b0 + kb, 1024), idesc, (s | kk) != 0 ? 1u : 0u);
                 }
                 tc::mma_commit(&s_opfree[ob]);
             }
@@ -213,21 +215,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 break;
             }
             const unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
-            unsigned char *opa = op0 + ob * T::OP;
-            unsigned char *opb = opa + T::OP_A;
-            // codes: a warp converts 4 SNP rows x 8 chunks of 16 codes (conflict-free)
-#pragma unroll
-            for (int it = 0; it < TC_TM * 8 / TC_CONV; ++it) {
-                const int t = tid + TC_CONV * it;
-                const int m = t >> 3, ch = t & 7;
-                const uint4 w = *reinterpret_cast<const uint4 *>(ra_ + m * 128 + ((ch ^ (m & 7)) << 4));
-                uint4 lo, hi;
-                tc::codes_to_bf16x4(w.x, lo.x, lo.y);
-                tc::codes_to_bf16x4(w.y, lo.z, lo.w);
-                tc::codes_to_bf16x4(w.z, hi.x, hi.y);
-                tc::codes_to_bf16x4(w.w, hi.z, hi.w);
-                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(m, 16 * ch, TC_TM)) = lo;
-                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(m, 16 * ch + 8, TC_TM)) = hi;
+            unsigned char *opb = op0 + ob * T::OP;
+            // codes -> tensor memory: warp w writes lanes 32*(w%4).. (SNP rows), 32 codes of K
+            // (columns 16*(w/4) .. +15 of the stage's operand block)
+            {
+                const int m = 32 * (warp & 3) + lane, s4 = warp >> 2;
+                const uint4 wa = *reinterpret_cast<const uint4 *>(ra_ + m * 128 + (((2 * s4) ^ (m & 7)) << 4));
+                const uint4 wb = *reinterpret_cast<const uint4 *>(ra_ + m * 128 + (((2 * s4 + 1) ^ (m & 7)) << 4));
+                uint32_t v[16];
+                tc::codes_to_bf16x4(wa.x, v[0], v[1]);
+                tc::codes_to_bf16x4(wa.y, v[2], v[3]);
+                tc::codes_to_bf16x4(wa.z, v[4], v[5]);
+                tc::codes_to_bf16x4(wa.w, v[6], v[7]);
+                tc::codes_to_bf16x4(wb.x, v[8], v[9]);
+                tc::codes_to_bf16x4(wb.y, v[10], v[11]);
+                tc::codes_to_bf16x4(wb.z, v[12], v[13]);
+                tc::codes_to_bf16x4(wb.w, v[14], v[15]);
+                tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 64 * ob + 16 * s4, v);
             }
             // residuals -> three bf16 rows per chain
             for (int t = tid; t < CT * (TC_KC / 8); t += TC_CONV) {
@@ -243,7 +247,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 *reinterpret_cast<uint4 *>(opb + tc::sw128_off(CT + c, 8 * q, NB)) = md;
                 *reinterpret_cast<uint4 *>(opb + tc::sw128_off(2 * CT + c, 8 * q, NB)) = l;
             }
+            tc::tmem_wait_st();
             tc::fence_async_smem();
+            tc::fence_before_sync();
             tc::mbar_arrive(&s_conv[ob]);
             tc::mbar_arrive(&s_empty[buf]);
         }
@@ -280,12 +286,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     if (warp == TC_WARP_MMA) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tm, 64);
+        tc::tmem_dealloc(tm, 256);
     }
 
     // augmenting part on the FP32 cores: this split's share of the U rows of
     // the tile's columns (upper triangular: rows up to the tile's last
-    // column), staged by windows of TC_UWR rows with cp.async; converter warp
+    // column), staged by windows of UWR rows with cp.async; converter warp
     // w owns 8 columns (four at a time), lanes run over rows, and the 4 x CT
     // lane sums are reduced by a transposing butterfly.
     const int npad = (N + 7) & ~7;
@@ -293,23 +299,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int nUc = (rowsU + 31) / 32;
     const int l0 = 32 * (int)(((long long)nUc * ks) / ksplit);
     const int l1 = min(rowsU, 32 * (int)(((long long)nUc * (ks + 1)) / ksplit));
-    float *sU = reinterpret_cast<float *>(base);      // [TC_TM][TC_UWR]
-    float *sRa = sU + TC_TM * TC_UWR;                 // [CT][TC_UWR]
-    float *s_u = sRa + CT * TC_UWR;                   // [TC_TM][CT]
+    float *sU = reinterpret_cast<float *>(base);      // [TC_TM][T::UWR]
+    float *sRa = sU + TC_TM * T::UWR;                 // [CT][T::UWR]
+    float *s_u = sRa + CT * T::UWR;                   // [TC_TM][CT]
     for (int t = tid; t < TC_TM * CT; t += TC_THREADS) s_u[t] = 0.0f;
-    for (int w0 = l0; w0 < l1; w0 += TC_UWR) {
-        const int len = min(TC_UWR, l1 - w0);        // a multiple of 8
+    for (int w0 = l0; w0 < l1; w0 += T::UWR) {
+        const int len = min(T::UWR, l1 - w0);        // a multiple of 8
         __syncthreads();
         for (int t = tid; t < TC_TM * (len / 4); t += TC_THREADS) {
             const int jj = t / (len / 4), q = t % (len / 4);
             const int jk = j0 + jj;
-            float *dst = sU + jj * TC_UWR + 4 * q;
+            float *dst = sU + jj * T::UWR + 4 * q;
             if (jk < N) __pipeline_memcpy_async(dst, D.U32 + D.uoff[ls + jk] + w0 + 4 * q, 16);
             else *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         for (int t = tid; t < CT * (len / 4); t += TC_THREADS) {
             const int c = t / (len / 4), q = t % (len / 4);
-            __pipeline_memcpy_async(sRa + c * TC_UWR + 4 * q, D.ra32 + (size_t)c * D.ldra + w0 + 4 * q, 16);
+            __pipeline_memcpy_async(sRa + c * T::UWR + 4 * q, D.ra32 + (size_t)c * D.ldra + w0 + 4 * q, 16);
         }
         __pipeline_commit();
         __pipeline_wait_prior(0);
@@ -323,10 +329,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (int l = lane; l < len; l += 32) {
                 float u[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) u[q] = sU[(jq + q) * TC_UWR + l];
+                for (int q = 0; q < 4; ++q) u[q] = sU[(jq + q) * T::UWR + l];
 #pragma unroll
                 for (int c = 0; c < CT; ++c) {
-                    const float rv = sRa[c * TC_UWR + l];
+                    const float rv = sRa[c * T::UWR + l];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) acc[q * CT + c] = fmaf(u[q], rv, acc[q * CT + c]);
                 }

@@ -113,6 +113,9 @@ struct Dev {
     double *k0part;            // [draw CTAs][C] per-CTA sums of x0_j delta_j
     float *rapart;             // [ra tiles][TU_RA_SPLIT][C][128] ra update partial sums
     int32_t *raticket;         // [ra tiles] ra update tickets (self-resetting)
+    const int32_t *rtab;       // [nb][tstride] first rhs CTA of each 128-SNP tile, then the total
+    const int32_t *atab;       // [nb][tstride] first ra-update CTA of each 128-row tile, then the total
+    int tstride;
 };
 
 constexpr int RHS_KSPLIT_MAX = 16;

@@ -18,6 +18,7 @@
 #include "state.cuh"
 #include "sweep.cuh"
 #include "tc.cuh"
+#include <algorithm>
 
 namespace soda {
 
@@ -795,32 +796,28 @@ static cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
 // per SM), then the update (row tiles of r on the tensor cores, ra tiles on
 // the FP32 cores; two CTAs per SM).
 template <int CT>
-static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_count, const TcMaps *maps,
-                                  cudaStream_t st, ProfHook *prof)
+static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, const TcMaps *maps, cudaStream_t st,
+                                  ProfHook *prof)
 {
     const int mtiles = (nblk_snps + TC_TM - 1) / TC_TM;
-    const int nst = D.ldx / TC_KC;
-    int ks = sm_count / mtiles;
-    ks = ks < 1 ? 1 : (ks > RHS_KSPLIT_MAX ? RHS_KSPLIT_MAX : ks);
-    ks = ks > nst ? nst : ks;
+    const int nrhs = maps->h_rtab[(size_t)b * D.tstride + mtiles];
+    const int nra = maps->h_atab[(size_t)b * D.tstride + mtiles];
     cudaError_t e;
     {
         ProfScope ps(prof, st, PROF_RHS);
-        e = launch_pdl(k_rhs_tc<CT>, dim3(mtiles * ks), dim3(TC_THREADS), RhsTc<CT>::SMEM, st, maps->codes128,
-                       maps->r, D, b, ks);
+        e = launch_pdl(k_rhs_tc<CT>, dim3(nrhs), dim3(TC_THREADS), RhsTc<CT>::SMEM, st, maps->codes128, maps->r, D, b);
     }
     if (e != cudaSuccess) return e;
     {
         const int span = mtiles * TC_TM;
         ProfScope ps(prof, st, PROF_DRAW);
-        e = launch_pdl(k_draw<SODAGPU_FP8, CT, true>, dim3((span * CT + 255) / 256), dim3(256), 0, st, D, b, ks, span);
+        e = launch_pdl(k_draw<SODAGPU_FP8, CT, true>, dim3((span * CT + 255) / 256), dim3(256), 0, st, D, b, 0, span);
     }
     if (e != cudaSuccess) return e;
-    const int ra_tiles = (nblk_snps + 127) / 128;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
-        e = launch_pdl(k_update_tc<CT>, dim3(D.nr_ctas + ra_tiles * TU_RA_SPLIT), dim3(TU_THREADS), UpdTc<CT>::SMEM,
-                       st, maps->codes64, maps->d, D, b, TU_RA_SPLIT);
+        e = launch_pdl(k_update_tc<CT>, dim3(D.nr_ctas + nra), dim3(TU_THREADS), UpdTc<CT>::SMEM, st, maps->codes64,
+                       maps->d, D, b);
     }
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
@@ -831,7 +828,7 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
                                ProfHook *prof)
 {
     if constexpr (MODE == SODAGPU_FP8 && CT >= 4) {
-        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, sm_count, maps, st, prof);
+        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, maps, st, prof);
     }
     constexpr int MTS = 8 * SptOf<CT>::v;
     const int mtiles = (nblk_snps + MTS - 1) / MTS;
@@ -877,11 +874,54 @@ static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int sm_count
 
 int sweep_chain_count_supported(int c) { return c == 1 || c == 2 || c == 4 || c == 8 || c == 16; }
 
+// Every kernel of an iteration asks for the largest shared-memory carveout,
+// so that consecutive kernels never wait for the SMs to repartition L1 and
+// shared memory (microseconds per kernel boundary otherwise).
+template <typename K>
+static cudaError_t max_carveout(K *kern)
+{
+    return cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared);
+}
+
+template <int MODE, bool TC>
+static cudaError_t carve_draw()
+{
+    cudaError_t e = cudaSuccess;
+    if constexpr (!TC) {
+        e = max_carveout(k_draw<MODE, 1, false>);
+        if (e == cudaSuccess) e = max_carveout(k_draw<MODE, 2, false>);
+    }
+    if (e == cudaSuccess) e = max_carveout(k_draw<MODE, 4, TC>);
+    if (e == cudaSuccess) e = max_carveout(k_draw<MODE, 8, TC>);
+    if (e == cudaSuccess) e = max_carveout(k_draw<MODE, 16, TC>);
+    return e;
+}
+
+static cudaError_t carve_all()
+{
+    cudaError_t e = carve_draw<SODAGPU_FP64, false>();
+    if (e == cudaSuccess) e = carve_draw<SODAGPU_FP32, false>();
+    if (e == cudaSuccess) e = carve_draw<SODAGPU_FP8, false>();
+    if (e == cudaSuccess) e = carve_draw<SODAGPU_FP8, true>();
+    if (e == cudaSuccess) e = max_carveout(k_iter_begin);
+    if (e == cudaSuccess) e = max_carveout(k_mu_partial);
+    if (e == cudaSuccess) e = max_carveout(k_mu_apply);
+    if (e == cudaSuccess) e = max_carveout(k_skipped);
+    if (e == cudaSuccess) e = max_carveout(k_stats);
+    if (e == cudaSuccess) e = max_carveout(k_hyper);
+    if (e == cudaSuccess) e = max_carveout(k_post);
+    if (e == cudaSuccess) e = max_carveout(k_recal_partial);
+    if (e == cudaSuccess) e = max_carveout(k_recal_apply);
+    return e;
+}
+
 template <int MODE, int CT>
 static cudaError_t set_update_smem(int bs)
 {
-    return cudaFuncSetAttribute(k_update<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)update_smem_bytes_ct<MODE, CT>(bs));
+    cudaError_t e = cudaFuncSetAttribute(k_update<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)update_smem_bytes_ct<MODE, CT>(bs));
+    return e == cudaSuccess ? max_carveout(k_update<MODE, CT>) : e;
 }
 
 template <int MODE>
@@ -898,8 +938,9 @@ static cudaError_t set_update_smem_mode(int bs)
 template <int MODE, int CT>
 static cudaError_t set_rhs_smem()
 {
-    return cudaFuncSetAttribute(k_rhs<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)rhs_smem_bytes<MODE, CT>());
+    cudaError_t e = cudaFuncSetAttribute(k_rhs<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)rhs_smem_bytes<MODE, CT>());
+    return e == cudaSuccess ? max_carveout(k_rhs<MODE, CT>) : e;
 }
 
 template <int MODE>
@@ -920,6 +961,8 @@ static cudaError_t set_tc_smem()
                                          (int)RhsTc<CT>::SMEM);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_update_tc<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UpdTc<CT>::SMEM);
+    if (e == cudaSuccess) e = max_carveout(k_rhs_tc<CT>);
+    if (e == cudaSuccess) e = max_carveout(k_update_tc<CT>);
     return e;
 }
 
@@ -932,11 +975,49 @@ int sweep_tc_rows(int chains) { return ((3 * chains + 15) / 16) * 16; }
 
 int sweep_tc_ra_split() { return TU_RA_SPLIT; }
 
+int sweep_tc_table_stride(int bs) { return (bs + TC_TM - 1) / TC_TM + 1; }
+
+void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab, int32_t *atab)
+{
+    const int stride = sweep_tc_table_stride(bs);
+    const int nst = ldx / TC_KC;
+    for (int b = 0; b < nb; ++b) {
+        const int N = blk_sizes[b], tiles = (N + TC_TM - 1) / TC_TM, npad = (N + 7) & ~7;
+        int32_t *rt = rtab + (size_t)b * stride, *at = atab + (size_t)b * stride;
+        // rhs: weight of tile m = genotype bytes / 1024 + U rows (an FP32 U row of 128 columns
+        // costs about twice its 512 bytes on the FP32 cores)
+        long long W = 0;
+        for (int m = 0; m < tiles; ++m) W += ldx / 8 + std::min(npad, TC_TM * (m + 1));
+        int acc = 0;
+        for (int m = 0; m < tiles; ++m) {
+            const long long w = ldx / 8 + std::min(npad, TC_TM * (m + 1));
+            int ks = (int)(((long long)sm_count * w) / W);
+            ks = std::max(1, std::min(ks, std::min(RHS_KSPLIT_MAX, nst)));
+            rt[m] = acc;
+            acc += ks;
+        }
+        rt[tiles] = acc;
+        // ra update: tile t meets the columns k >= 128 t of the upper-triangular factor
+        long long Wa = 0;
+        for (int t = 0; t < tiles; ++t) Wa += N - TC_TM * t;
+        const int total = TU_RA_SPLIT * tiles;
+        acc = 0;
+        for (int t = 0; t < tiles; ++t) {
+            int sp = (int)(((long long)total * (N - TC_TM * t)) / Wa);
+            sp = std::max(1, std::min(sp, 64));
+            at[t] = acc;
+            acc += sp;
+        }
+        at[tiles] = acc;
+    }
+}
+
 // Raises the dynamic shared-memory limits of the rhs and update kernels.
 cudaError_t sweep_prepare(int bs)
 {
     {
-        cudaError_t e = set_tc_smem<4>();
+        cudaError_t e = carve_all();
+        if (e == cudaSuccess) e = set_tc_smem<4>();
         if (e == cudaSuccess) e = set_tc_smem<8>();
         if (e == cudaSuccess) e = set_tc_smem<16>();
         if (e != cudaSuccess) return e;

@@ -13,6 +13,13 @@ cudaError_t sweep_prepare(int bs);
 int sweep_tc_supported(int precision, int chains, int bs);
 int sweep_tc_rows(int chains);
 int sweep_tc_ra_split();
+// Work tables of the tensor-core sweep (host side), per subset b of blk_sizes:
+// rtab[b*stride + m] = first rhs CTA of 128-SNP tile m, rtab[b*stride + tiles]
+// = rhs CTAs; tiles get K splits in proportion to their bytes (genotypes plus
+// the upper-triangular U rows).  atab likewise for the ra update: 128-row
+// tiles get column splits in proportion to their triangular width.
+int sweep_tc_table_stride(int bs);
+void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab, int32_t *atab);
 // Optional per-launch event recording (eager profiling, never inside a graph):
 // before/after every launch an event pair is recorded and its kernel class
 // stored.  Classes: 0 rhs, 1 residual update, 2 mu, 3 everything else, 4 draws.
@@ -26,9 +33,11 @@ struct ProfHook {
 // TMA descriptors of the tensor-core sweep: genotype codes in 128 x 128 and
 // 128 x 64 (individuals x SNPs) boxes with 128-byte swizzle, the FP32
 // residuals of all chains in 128 x chains boxes, and the bf16 delta split in
-// 64 x rows boxes with 128-byte swizzle.
+// 64 x rows boxes with 128-byte swizzle; and the host copies of the work
+// tables.
 struct TcMaps {
     CUtensorMap codes128, codes64, r, d;
+    const int32_t *h_rtab, *h_atab;   // host copies of D.rtab / D.atab
 };
 
 // Enqueues one Gibbs iteration of every chain on `st` (graph-capturable when

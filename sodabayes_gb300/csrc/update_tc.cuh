@@ -7,25 +7,26 @@
 //
 // Row tiles of r (128 individuals, one CTA each) run on tcgen05: A = the
 // tile's codes of 64 subset positions per stage, transposed to individual-major
-// bf16 in shared memory, B = the three-way bf16 split of delta/sd written by
-// the draws (k_draw), D = 128 x 3*chains FP32 in tensor memory.  Stages whose
-// 64 positions have no non-zero delta in any chain are skipped.  The pipeline
-// is the one of k_rhs_tc: warp 8 loads each stage's code tile and delta-split
-// tile by TMA (both 128-byte swizzled; the MMA reads the delta split straight
-// from the raw buffer), warps 0-7 transpose and convert the codes, warp 9
-// issues the MMAs.  The centring term sum_j x0_j delta_j is added in FP64
-// from the per-CTA sums of the draws.  The augmented rows ra (U_b is FP32,
-// one tile of 128 rows per ra_split CTAs over column ranges) run on the FP32
-// cores; the last CTA of a row tile adds the split partial sums in split
-// order (deterministic).
+// bf16 in tensor memory (lane = individual, written with tcgen05.st), B = the
+// three-way bf16 split of delta/sd written by the draws (k_draw), D = 128 x
+// 3*chains FP32 in tensor memory.  Stages whose 64 positions have no
+// non-zero delta in any chain are skipped.  The pipeline is the one of
+// k_rhs_tc: warp 8 loads each stage's code tile and delta-split tile by TMA
+// (both 128-byte swizzled; the MMA reads the delta split straight from the
+// raw buffer), warps 0-7 gather and convert the codes, warp 9 issues the
+// MMAs.  The centring term sum_j x0_j delta_j is added in FP64 from the
+// per-CTA sums of the draws.  The augmented rows ra (U_b is FP32; a tile of
+// 128 rows is split over column ranges, D.atab giving wider tiles more CTAs)
+// run on the FP32 cores; the last CTA of a row tile adds the split partial
+// sums in split order (deterministic).
 #pragma once
 
 namespace soda {
 
 constexpr int TU_KC = 64;          // subset positions per stage
-constexpr int TU_NS = 4;           // raw stages in flight
+constexpr int TU_NS = 6;           // raw stages in flight
 constexpr int TU_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
-constexpr int TU_RA_SPLIT = 8;     // CTAs per 128-row tile of ra
+constexpr int TU_RA_SPLIT = 8;     // ra-update CTAs per 128-row tile, on average
 constexpr int TU_UNR = 8;          // U columns in flight per warp
 constexpr int TU_THREADS = 320;    // 8 converter warps, the TMA warp, the MMA warp
 constexpr int TU_CONV = 256;
@@ -37,11 +38,10 @@ struct UpdTc {
     static constexpr int RAW_A = TU_KC * 128;          // codes: 64 positions x 128 individuals (TMA, swizzled)
     static constexpr int RAW_B = NB * TU_KC * 2;       // bf16 split of delta/sd (TMA, swizzled; MMA operand B)
     static constexpr int RAW = RAW_A + RAW_B;
-    static constexpr int OP = 128 * TU_KC * 2;         // bf16 codes, individual-major (MMA operand A)
-    static constexpr int PIPE = 2 * OP + TU_NS * RAW;
+    static constexpr int PIPE = TU_NS * RAW;           // (the codes operand lives in tensor memory)
     static constexpr int RED = 4 * CT * 128 * 4;       // column-group partials of the ra tiles
     static constexpr size_t SMEM = 1024 + (size_t)(PIPE > RED ? PIPE : RED);
-    static_assert(OP % 1024 == 0 && RAW % 1024 == 0 && RAW_A % 1024 == 0, "buffers must keep 1024-byte alignment");
+    static_assert(RAW % 1024 == 0 && RAW_A % 1024 == 0, "buffers must keep 1024-byte alignment");
 };
 
 template <int CT>
@@ -58,8 +58,7 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
     __shared__ double s_k0[CT];
     __shared__ double s_k0p[TU_CONV];
     __shared__ double s_rsw[8][CT];
-    unsigned char *op0 = base;
-    unsigned char *raw0 = base + 2 * T::OP;
+    unsigned char *raw0 = base;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
@@ -139,7 +138,7 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
         tc::mbar_fence_init();
         s_err = 0;
     }
-    if (warp == TU_WARP_MMA) tc::tmem_alloc(&s_tmem, 64);
+    if (warp == TU_WARP_MMA) tc::tmem_alloc(&s_tmem, 128);   // accumulator 0-63, codes operand 64-127
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -172,23 +171,21 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t a0 = tc::smem_u32(op0 + ob * T::OP);
+                const uint32_t ta = tm + 64 + 32 * ob;
                 const uint32_t b0 = tc::smem_u32(raw0 + (size_t)buf * T::RAW + T::RAW_A);
 #pragma unroll
                 for (int kk = 0; kk < TU_KC / 16; ++kk)
-                    tc::mma_bf16(tm, tc::desc_sw128(a0 + kk * 32, 1024), tc::desc_sw128(b0 + kk * 32, 1024), idesc,
-                                 (s | kk) != 0 ? 1u : 0u);
+                    tc::mma_bf16_ta(tm, ta + 8 * kk, tc::desc_sw128(b0 + kk * 32, 1024), idesc, (s | kk) != 0 ? 1u : 0u);
                 tc::mma_commit(&s_opfree[ob]);
                 tc::mma_commit(&s_empty[buf]);
             }
             tc::mma_commit(&s_done);
         }
     } else {
-        // converters: thread (a, bb) of warp w transposes individuals 16w+4a..+3 x positions 8bb..8bb+7.
-        // Reads rotate the position (slot e holds position (e+bb)&7) so that the 32 lanes hit 32 banks
-        // of the 128-byte-swizzled tile; a 64-bit rotation restores position order.
-        const int a = lane >> 3, bb = lane & 7;
-        const int rq = 16 * warp + 4 * a;
+        // converters: warp w writes tensor-memory lanes 32*(w%4).. (individuals), positions 32*(w/4) ..
+        // +31 of the stage (16 columns): a thread gathers its individual's byte from 32 rows of the
+        // 128-byte-swizzled code tile (a warp reads 32 consecutive bytes of one row at a time)
+        const int ind = 32 * (warp & 3) + lane, kh = warp >> 2;
         for (int s = 0; s < nact; ++s) {
             const int buf = s % TU_NS, ob = s & 1;
             bool ok = tc::mbar_wait(&s_full[buf], (s / TU_NS) & 1);
@@ -198,41 +195,17 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
                 break;
             }
             const unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
-            unsigned char *opa = op0 + ob * T::OP;
-            uint32_t w[8];
+            uint32_t v[16];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int kk = 8 * bb + ((e + bb) & 7);
-                w[e] = *reinterpret_cast<const uint32_t *>(ra_ + kk * 128 + ((warp ^ (kk & 7)) << 4) + a * 4);
+            for (int j = 0; j < 16; ++j) {
+                const int k = 32 * kh + 2 * j;
+                const uint32_t c0 = ra_[k * 128 + ((((ind >> 4) ^ (k & 7))) << 4) + (ind & 15)];
+                const uint32_t c1 = ra_[(k + 1) * 128 + ((((ind >> 4) ^ ((k + 1) & 7))) << 4) + (ind & 15)];
+                v[j] = tc::bf16x2_sub128(c0 | (c1 << 16) | 0x43004300u);
             }
-            uint32_t row[4][2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const uint32_t a0 = __byte_perm(w[4 * h + 0], w[4 * h + 1], 0x5140u);
-                const uint32_t a1 = __byte_perm(w[4 * h + 2], w[4 * h + 3], 0x5140u);
-                const uint32_t a2 = __byte_perm(w[4 * h + 0], w[4 * h + 1], 0x7362u);
-                const uint32_t a3 = __byte_perm(w[4 * h + 2], w[4 * h + 3], 0x7362u);
-                row[0][h] = __byte_perm(a0, a1, 0x5410u);
-                row[1][h] = __byte_perm(a0, a1, 0x7632u);
-                row[2][h] = __byte_perm(a2, a3, 0x5410u);
-                row[3][h] = __byte_perm(a2, a3, 0x7632u);
-            }
-            const int sh = (bb & 3) * 8;
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                uint32_t lo = row[r][0], hi = row[r][1];
-                if (bb & 4) {
-                    const uint32_t t = lo;
-                    lo = hi;
-                    hi = t;
-                }
-                const uint32_t nlo = __funnelshift_l(hi, lo, sh), nhi = __funnelshift_l(lo, hi, sh);
-                uint4 v;
-                tc::codes_to_bf16x4(nlo, v.x, v.y);
-                tc::codes_to_bf16x4(nhi, v.z, v.w);
-                *reinterpret_cast<uint4 *>(opa + tc::sw128_off(rq + r, 8 * bb, 128)) = v;
-            }
-            tc::fence_async_smem();
+            tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 32 * ob + 16 * kh, v);
+            tc::tmem_wait_st();
+            tc::fence_before_sync();
             tc::mbar_arrive(&s_conv[ob]);
             tc::mbar_arrive(&s_empty[buf]);
         }
@@ -283,7 +256,7 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
     __syncthreads();
     if (warp == TU_WARP_MMA) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tm, 64);
+        tc::tmem_dealloc(tm, 128);
     }
     // this tile's partial sum of r (the centring of the next subset)
     if (tid < CT) {
@@ -294,7 +267,7 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
 }
 
 template <int CT>
-__device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, unsigned char *base)
+__device__ __forceinline__ void update_tc_ra(const Dev &D, int b, unsigned char *base)
 {
     __shared__ int s_last;
     float *s_red = reinterpret_cast<float *>(base);   // [4 column groups][CT][128 rows]
@@ -304,8 +277,13 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
     const int npad = (N + 7) & ~7;
+    // this CTA's row tile and column split (tiles get splits in proportion to their width)
     const int idx = blockIdx.x - D.nr_ctas;
-    const int tr = idx / ra_split, sp = idx % ra_split;
+    const int32_t *at = D.atab + (size_t)b * D.tstride;
+    const int ntr = (N + 127) / 128;
+    int tr = 0;
+    while (tr + 1 < ntr && at[tr + 1] <= idx) ++tr;
+    const int ra_split = at[tr + 1] - at[tr], sp = idx - at[tr];
     const int i0 = tr * 128;
     const int kbeg = D.blk_pd[b] ? min(i0, N) : 0;   // upper triangular: rows i only meet columns k >= i
     const int ka = kbeg + (int)(((long long)(N - kbeg) * sp) / ra_split);
@@ -354,7 +332,7 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
         }
     }
     __syncthreads();
-    float *part = D.rapart + ((size_t)(tr * ra_split + sp) * CT) * 128;
+    float *part = D.rapart + ((size_t)idx * CT) * 128;
     for (int t = tid; t < CT * 128; t += TU_THREADS) {
         const int c = t >> 7, rl = t & 127;
         part[c * 128 + rl] = ((s_red[(0 * CT + c) * 128 + rl] + s_red[(1 * CT + c) * 128 + rl]) +
@@ -367,17 +345,20 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
     if (!s_last) return;
     __threadfence();
     // the last CTA of the row tile: split partial sums in split order
+    const float *p0 = D.rapart + ((size_t)at[tr] * CT) * 128;
     for (int t = tid; t < CT * 128; t += TU_THREADS) {
         const int c = t >> 7, rl = t & 127, i = i0 + rl;
         if (i >= D.bs) continue;
-        float pv[TU_RA_SPLIT];
-#pragma unroll
-        for (int q = 0; q < TU_RA_SPLIT; ++q)
-            pv[q] = q < ra_split ? __ldcg(D.rapart + ((size_t)(tr * ra_split + q) * CT + c) * 128 + rl) : 0.0f;
         float sum = 0.0f;
+        for (int q0 = 0; q0 < ra_split; q0 += 8) {
+            float pv[8];
 #pragma unroll
-        for (int q = 0; q < TU_RA_SPLIT; ++q)
-            if (q < ra_split) sum += pv[q];
+            for (int q = 0; q < 8; ++q)
+                pv[q] = q0 + q < ra_split ? __ldcg(p0 + ((size_t)(q0 + q) * CT + c) * 128 + rl) : 0.0f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q0 + q < ra_split) sum += pv[q];
+        }
         const size_t o = (size_t)c * D.ldra + i;
         const double v = D.ra[o] + (double)sum;
         D.ra[o] = v;
@@ -388,13 +369,12 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, int ra_split, 
 
 template <int CT>
 __global__ void __launch_bounds__(TU_THREADS, 2)
-    k_update_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_d, Dev D, int b,
-                int ra_split)
+    k_update_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_d, Dev D, int b)
 {
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
     unsigned char *base = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
     if ((int)blockIdx.x < D.nr_ctas) update_tc_rows<CT>(&tm_codes, &tm_d, D, b, base);
-    else update_tc_ra<CT>(D, b, ra_split, base);
+    else update_tc_ra<CT>(D, b, base);
 }
 
 }  // namespace soda
