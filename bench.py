@@ -20,6 +20,10 @@ restatement of its algorithm (oracle/) on the host cores.
 
 Multi-GPU: the path does not shard (one chain's subsets are sequential);
 --gpus N runs N independent replicas, one per rank.
+
+--profile-case: a small case with the same per-subset shape (n=20,000,
+p=20,000, 10 subsets of 2,000) for ncu captures of single kernel launches;
+it runs --steps iterations and prints the library timings.
 """
 from __future__ import annotations
 
@@ -221,7 +225,10 @@ def bench_ours(args, rank, ws):
     bytes_rhs = _rhs_bytes(spec.n, BLOCKSIZE, C, "fp8")
     achieved = bytes_rhs / (rhs_ms / 1000.0) / 1e9
     res["roofline"] = {"bound": "hbm", "kernel": "k_rhs_tc<%d>" % C, "achieved": round(achieved, 1),
-                       "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "traffic": None,
+                       "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                       "traffic": _measured_traffic("k_rhs_tc%d_n20000_s2000.md" % C),
+                       "traffic_source": "ncu --set full of one launch of the same kernel at the same subset shape "
+                                         "(profiles/k_rhs_tc%d_n20000_s2000.md)" % C,
                        "peak_source": peak_kind, "bytes_per_launch": bytes_rhs,
                        "launch_ms": round(rhs_ms, 5),
                        "kernel_ms_per_iter": {k: round(v[0] / 2, 4) for k, v in prof.items()}}
@@ -326,6 +333,43 @@ def cpu_sample(args, steps=1, warmup=0):
             "seconds_per_iteration": t_iter}
 
 
+def profile_case(args):
+    """Small case for kernel captures: same per-subset shape as the workload."""
+    import torch
+    from sodabayes_gb300 import SodaJob, make_config, synth
+    spec = synth.SynthSpec(n=20000, p=20000, maf_lo=0.01, maf_hi=0.5, ld_block=50, rho=0.7, ncausal=80, h2=0.5,
+                           seed=5)
+    codes, y, _ = synth.make_device(spec)
+    with SodaJob(make_config(spec.n, spec.p, _opts(args.precision, args.chains, 77, 1000))) as job:
+        job.load_genotypes(device_ptr=codes.data_ptr())
+        job.load_pheno(y)
+        job.build_z()
+        job.init_chains()
+        job.run(args.steps)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": {"n": spec.n, "p": spec.p, "chains": args.chains,
+                                            "precision": args.precision, "iterations": args.steps,
+                                            "included": job.state()["included"], "timings": job.timings()}}))
+
+
+def _measured_traffic(kernel_file: str):
+    """dram bytes read + written per launch from a committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", kernel_file)
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    vals = {}
+    for key in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+        for line in txt.splitlines():
+            if line.startswith("| " + key + " |"):
+                tok = line.split("|")[2].split()
+                vals[key] = float(tok[0]) * {"MB": 1e6, "KB": 1e3, "GB": 1e9}.get(tok[1], 1.0)
+    if len(vals) != 2:
+        return None
+    return vals["dram__bytes_read.sum"] + vals["dram__bytes_write.sum"]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -337,7 +381,13 @@ def main():
     ap.add_argument("--error-iters", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--cpu-blocks", type=int, default=4)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="n=20000, p=20000 case of the same subset shape, for ncu captures")
+    ap.add_argument("--precision", default="fp8", choices=["fp64", "fp32", "fp8"], help="--profile-case only")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     rank, ws = _dist_init()
