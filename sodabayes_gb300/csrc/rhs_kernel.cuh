@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     const int snp = act && !D.skip[k] ? D.perm[k] : -1;
     double inv = 0.0, x0 = 0.0, gold = 0.0;
     int cl = 0, sg = 0;
+    DrawPre pre{};
     if (snp >= 0) {
         if (MODE == SODAGPU_FP8 || TC) {
             inv = D.xv[(size_t)k * 4 + 3];
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
             gold = D.g[(size_t)c * D.p + snp];
             cl = D.cls[(size_t)c * D.p + snp];
             sg = D.grp[snp] - 1;
+            draw_prefetch(D, &D.scal[c], c, snp, sg, pre);   // chain state: fixed within an iteration
         }
     }
     if (TC && act) {   // the tensor-core rhs gives each 128-SNP tile its own number of splits
@@ -129,20 +131,21 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
             pu[sp] = __ldcg(D.rpu + o);
         }
     }
-    if (MODE == SODAGPU_FP8) {
-        // 256/CT threads per chain over interleaved row tiles, then in part order
+    if (MODE == SODAGPU_FP8 || TC) {
+        // sum(r) per chain from the row-tile partial sums: 256/CT threads per chain take
+        // interleaved tiles, loaded 16 at a time in one batch, then added in part order
         constexpr int PARTS = 256 / CT;
         const int cc = tid / PARTS, part = tid % PARTS;
         double a = 0.0;
-        for (int q0 = part; q0 < D.nr_ctas; q0 += 4 * PARTS) {
-            double v[4];
+        for (int q0 = part; q0 < D.nr_ctas; q0 += 16 * PARTS) {
+            double v[16];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 16; ++u) {
                 const int q = q0 + u * PARTS;
                 v[u] = q < D.nr_ctas ? __ldcg(D.rsum + (size_t)cc * D.nr_ctas + q) : 0.0;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) a += v[u];
+            for (int u = 0; u < 16; ++u) a += v[u];
         }
         s_k[tid] = a;
         __syncthreads();
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     }
     double delta = 0.0;
     if (snp >= 0) {
-        if (MODE == SODAGPU_FP8) xr = xr * inv + x0 * s_rs[c];
+        if (MODE == SODAGPU_FP8 || TC) xr = xr * inv + x0 * s_rs[c];
         const ChainScal *S = &D.scal[c];
         const double zz = D.xxd[b];
         CRng R;
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
             delta = draw_snp(D, S, c, cur_rep(D), snp, xr + ur, zz, zz / S->vare, R, &err);
         else
             delta = draw_snp_f(D, S, c, snp, (float)(xr + ur), (float)zz, (float)(zz / S->vare), R, &err, gold, cl,
-                               sg);
+                               sg, pre);
         if (err) flag_err(D, 1);
     }
     if (act) {

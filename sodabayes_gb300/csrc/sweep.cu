@@ -153,19 +153,48 @@ __device__ __forceinline__ double draw_snp(const Dev &D, const ChainScal *S, int
 // The same draw in FP32 arithmetic, for the FP32/FP8 sweeps: GB300 executes
 // FP64 at a small fraction of its FP32 rate, and the draws of a subset sit on
 // the critical path of every subset.  State stays FP64.
+// Chain state a draw reads, loaded by the caller ahead of the draw (for up
+// to DRAW_PRE mixture classes; the state changes only between iterations):
+// the residual variance, the prior scale, the SNP's locus variance (BayesA/B)
+// and, per class k, log pi of the SNP's group, gamma_k sigma2_g and
+// sigma2_e / (gamma_k sigma2_g).
+constexpr int DRAW_PRE = 4;
+struct DrawPre {
+    float vare, scale_va, vs;
+    float logp[DRAW_PRE], gp[DRAW_PRE], vgp[DRAW_PRE];
+};
+
+__device__ __forceinline__ void draw_prefetch(const Dev &D, const ChainScal *S, int c, int snploc, int sg, DrawPre &q)
+{
+    q.vare = (float)S->vare;
+    q.scale_va = (float)S->scale_va;
+    q.vs = (D.method == SODAGPU_BAYES_A || D.method == SODAGPU_BAYES_B) ? (float)D.vara_s[(size_t)c * D.p + snploc]
+                                                                          : 0.0f;
+#pragma unroll
+    for (int k = 0; k < DRAW_PRE; ++k) {
+        const bool in = k < D.nmix;
+        q.logp[k] = in ? (float)S->log_p[sg + k * D.ngroup] : 0.0f;
+        q.gp[k] = in ? (float)S->gp[k] : 0.0f;
+        q.vgp[k] = in ? (float)S->vare_gp[k] : 0.0f;
+    }
+}
+
 // gold = g and cl = class of the SNP in this chain, sg = its group - 1, all
-// loaded by the caller ahead of the draw (they sit on its critical path).
+// loaded by the caller ahead of the draw (they sit on its critical path);
+// pre: the prefetched chain state (used when nmix <= DRAW_PRE).
 __device__ __forceinline__ double draw_snp_f(const Dev &D, const ChainScal *S, int c, int snploc, float rhs, float zz,
-                             float zz_vare, CRng &R, int *err, double gold, int cl, int sg)
+                                             float zz_vare, CRng &R, int *err, double gold, int cl, int sg,
+                                             const DrawPre &pre)
 {
     const size_t o = (size_t)c * D.p + snploc;
-    const float vare = (float)S->vare;
+    const bool use_pre = D.nmix <= DRAW_PRE;
+    const float vare = pre.vare;
     float gk = (float)gold;
     const int m = D.method;
-    const float df_va = (float)D.df_va, scale_va = (float)S->scale_va;
+    const float df_va = (float)D.df_va, scale_va = pre.scale_va;
     if (m == SODAGPU_BAYES_A) {
         rhs = rhs + zz * gk;
-        const float vs = (float)D.vara_s[o];
+        const float vs = pre.vs;
         const float v1 = zz + vare / vs;
         gk = d_rnorm_f(rhs / v1, sqrtf(vare / v1), R);
         D.g[o] = (double)gk;
@@ -176,11 +205,11 @@ __device__ __forceinline__ double draw_snp_f(const Dev &D, const ChainScal *S, i
     if (cl > 1) rhs = rhs + zz * gk;
     const int ng = D.ngroup;
     if (m == SODAGPU_BAYES_B) {
-        const float vs = (float)D.vara_s[o];
-        const float s1 = (float)S->log_p[0];
+        const float vs = pre.vs;
+        const float s1 = pre.logp[0];
         const float logdetV = logf(vs * zz_vare + 1.0f);
         const float uhat = rhs / (zz + vare / vs);
-        const float s2 = -0.5f * (logdetV - (rhs * uhat / vare)) + (float)S->log_p[ng];
+        const float s2 = -0.5f * (logdetV - (rhs * uhat / vare)) + pre.logp[1];
         const float clike = s1 - s2;
         float sk;
         if (clike > 700.0f) sk = 0.0f;
@@ -204,33 +233,75 @@ __device__ __forceinline__ double draw_snp_f(const Dev &D, const ChainScal *S, i
         return gold - gnew;
     }
     const int nm = D.nmix;
-    float sv[MAXDIST];
-    sv[0] = (float)S->log_p[sg];
-    for (int kk = 1; kk < nm; ++kk) {
-        const float logdetV = logf((float)S->gp[kk] * zz_vare + 1.0f);
-        const float uhat = rhs / (zz + (float)S->vare_gp[kk]);
-        sv[kk] = -0.5f * (logdetV - (rhs * uhat / vare)) + (float)S->log_p[sg + kk * ng];
-    }
-    const float u = crng_unit_f(R);
-    float ssculm = 0.0f;
     int flag = 1;
-    for (int kk = 0; kk < nm; ++kk) {
-        const float skk = sv[kk];
-        float sk = 0.0f;
-        bool overflow = false;
-        for (int j = 0; j < nm; ++j) {
-            if (j == kk) continue;
-            const float clike = sv[j] - skk;
-            if (clike < -700.0f) continue;
-            if (clike > 700.0f) { overflow = true; break; }
-            sk = sk + expf(clike);
+    if (use_pre) {
+        // up to DRAW_PRE classes with every loop unrolled: the scores stay in registers
+        float sv[DRAW_PRE];
+        sv[0] = pre.logp[0];
+#pragma unroll
+        for (int kk = 1; kk < DRAW_PRE; ++kk) {
+            sv[kk] = 0.0f;
+            if (kk < nm) {
+                const float logdetV = logf(pre.gp[kk] * zz_vare + 1.0f);
+                const float uhat = rhs / (zz + pre.vgp[kk]);
+                sv[kk] = -0.5f * (logdetV - (rhs * uhat / vare)) + pre.logp[kk];
+            }
         }
-        ssculm = ssculm + (overflow ? 0.0f : 1.0f / (1.0f + sk));
-        if (u < ssculm) { flag = kk + 1; break; }
+        const float u = crng_unit_f(R);
+        float ssculm = 0.0f;
+        bool done = false;
+#pragma unroll
+        for (int kk = 0; kk < DRAW_PRE; ++kk) {
+            if (kk < nm && !done) {
+                float sk = 0.0f;
+                bool overflow = false;
+#pragma unroll
+                for (int j = 0; j < DRAW_PRE; ++j) {
+                    if (j < nm && j != kk && !overflow) {
+                        const float clike = sv[j] - sv[kk];
+                        if (clike > 700.0f) overflow = true;
+                        else if (clike >= -700.0f) sk = sk + expf(clike);
+                    }
+                }
+                ssculm = ssculm + (overflow ? 0.0f : 1.0f / (1.0f + sk));
+                if (u < ssculm) {
+                    flag = kk + 1;
+                    done = true;
+                }
+            }
+        }
+    } else {
+        float sv[MAXDIST];
+        sv[0] = (float)S->log_p[sg];
+        for (int kk = 1; kk < nm; ++kk) {
+            const float logdetV = logf((float)S->gp[kk] * zz_vare + 1.0f);
+            const float uhat = rhs / (zz + (float)S->vare_gp[kk]);
+            sv[kk] = -0.5f * (logdetV - (rhs * uhat / vare)) + (float)S->log_p[sg + kk * ng];
+        }
+        const float u = crng_unit_f(R);
+        float ssculm = 0.0f;
+        for (int kk = 0; kk < nm; ++kk) {
+            const float skk = sv[kk];
+            float sk = 0.0f;
+            bool overflow = false;
+            for (int j = 0; j < nm; ++j) {
+                if (j == kk) continue;
+                const float clike = sv[j] - skk;
+                if (clike < -700.0f) continue;
+                if (clike > 700.0f) { overflow = true; break; }
+                sk = sk + expf(clike);
+            }
+            ssculm = ssculm + (overflow ? 0.0f : 1.0f / (1.0f + sk));
+            if (u < ssculm) { flag = kk + 1; break; }
+        }
     }
     double gnew = 0.0;
     if (flag != 1) {
-        const float v1 = zz + vare / (float)S->gp[flag - 1];
+        float gsel = 0.0f;
+#pragma unroll
+        for (int k = 0; k < DRAW_PRE; ++k)
+            if (k == flag - 1) gsel = pre.gp[k];
+        const float v1 = zz + vare / (use_pre ? gsel : (float)S->gp[flag - 1]);
         gnew = (double)d_rnorm_f(rhs / v1, sqrtf(vare / v1), R);
     }
     D.cls[o] = flag;
