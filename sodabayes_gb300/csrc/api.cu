@@ -1095,7 +1095,7 @@ int sodagpu_profile_kernels(sodagpu_ctx *c, int32_t iters, double *ms, int32_t *
     h.trace_cap = 0;
     h.trace_iter = 0;
     CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
-    const int cap = 2 * c->nb + 8;
+    const int cap = 4 * c->nb + 16;   // rhs, draws and update per subset, plus the iteration kernels
     std::vector<cudaEvent_t> ev(2 * cap);
     std::vector<int> cls(cap);
     for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));

@@ -93,3 +93,20 @@ def test_tensor_sweep_pivoted_fallback(gpu_lib, data):
         assert rel <= 1e-4, (c, rel)
         ya, yr = tcs[c]["yaadj"], ref[c]["yaadj"]
         assert np.max(np.abs(ya - yr)) <= 1e-4 * max(1e-300, np.max(np.abs(yr)))
+
+
+def test_profile_counts_every_subset_kernel(gpu_lib, data):
+    """sodagpu_profile_kernels records every launch of an iteration (rhs,
+    draws and update of every subset)."""
+    G, y, _ = data
+    cfg = make_config(N, P, _opts(chains=16))
+    with SodaJob(cfg) as job:
+        job.load_genotypes(G)
+        job.load_pheno(y)
+        job.build_z()
+        job.init_chains()
+        prof = job.profile_kernels(2)
+    nb = cfg.nblocks
+    assert prof["rhs"][1] == 2 * nb and prof["update"][1] == 2 * nb and prof["draw"][1] == 2 * nb
+    assert prof["mu"][1] == 2 and prof["other"][1] == 2
+    assert all(v[0] > 0.0 for v in prof.values())
