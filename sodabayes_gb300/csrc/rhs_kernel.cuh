@@ -89,6 +89,8 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
 {
     __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring)
     __shared__ double s_k[256];
+    __shared__ DrawPre s_pre[CT];   // chain constants in FP32 (the FP64 pipe is narrow)
+    __shared__ float s_zzv[CT];
     const int tid = threadIdx.x, lane = tid & 31;
     const int t = blockIdx.x * 256 + tid;
     const int jl = t / CT, c = t % CT;
@@ -96,22 +98,30 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     const int N = D.blk_ls[b + 1] - ls;
     const bool act = jl < N;
     const int k = ls + (act ? jl : 0);
-    // prologue, overlapping the rhs kernel: the SNP's metadata and state (not
-    // written by the rhs kernel)
+    const double zz = D.xxd[b];
+    // prologue, overlapping the rhs kernel: chain constants (fixed within an
+    // iteration), the SNP's metadata and state (not written by the rhs kernel)
+    if (MODE != SODAGPU_FP64 && tid < CT) {
+        draw_prefetch(D, &D.scal[tid], tid, 0, 0, s_pre[tid]);
+        s_zzv[tid] = (float)(zz / D.scal[tid].vare);
+    }
     const int snp = act && !D.skip[k] ? D.perm[k] : -1;
     double inv = 0.0, x0 = 0.0, gold = 0.0;
+    float inv32 = 0.0f;
     int cl = 0, sg = 0;
-    DrawPre pre{};
+    float vs = 0.0f;
     if (snp >= 0) {
         if (MODE == SODAGPU_FP8 || TC) {
             inv = D.xv[(size_t)k * 4 + 3];
             x0 = D.xv[(size_t)k * 4 + 0];
+            inv32 = D.xv32[(size_t)k * 4 + 3];
         }
         if (MODE != SODAGPU_FP64) {
             gold = D.g[(size_t)c * D.p + snp];
             cl = D.cls[(size_t)c * D.p + snp];
             sg = D.grp[snp] - 1;
-            draw_prefetch(D, &D.scal[c], c, snp, sg, pre);   // chain state: fixed within an iteration
+            if (D.method == SODAGPU_BAYES_A || D.method == SODAGPU_BAYES_B)
+                vs = (float)D.vara_s[(size_t)c * D.p + snp];
         }
     }
     if (TC && act) {   // the tensor-core rhs gives each 128-SNP tile its own number of splits
@@ -120,15 +130,45 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     }
     tc::pdl_trigger();
     tc::pdl_wait();
-    // the rhs partial sums of all splits (added in split order) and sum(r)
-    double px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
+    // the rhs partial sums of all splits (added in split order; FP32 from the tensor-core rhs)
+    double xr = 0.0, ur = 0.0;
+    if (TC) {
+        const float *px32 = reinterpret_cast<const float *>(D.rpx), *pu32 = reinterpret_cast<const float *>(D.rpu);
+        float px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
 #pragma unroll
-    for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
-        px[sp] = pu[sp] = 0.0;
-        if (act && sp < ksplit) {
-            const size_t o = ((size_t)sp * CT + c) * D.bs + jl;
-            px[sp] = __ldcg(D.rpx + o);
-            pu[sp] = __ldcg(D.rpu + o);
+        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+            px[sp] = pu[sp] = 0.0f;
+            if (act && sp < ksplit) {
+                const size_t o = ((size_t)sp * CT + c) * D.bs + jl;
+                px[sp] = __ldcg(px32 + o);
+                pu[sp] = __ldcg(pu32 + o);
+            }
+        }
+        float xs = 0.0f, us = 0.0f;
+#pragma unroll
+        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+            xs += px[sp];
+            us += pu[sp];
+        }
+        xr = xs;
+        ur = us;
+    } else {
+        double px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
+#pragma unroll
+        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+            px[sp] = pu[sp] = 0.0;
+            if (act && sp < ksplit) {
+                const size_t o = ((size_t)sp * CT + c) * D.bs + jl;
+                px[sp] = __ldcg(D.rpx + o);
+                pu[sp] = __ldcg(D.rpu + o);
+            }
+        }
+#pragma unroll
+        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
+            if (sp < ksplit) {
+                xr += px[sp];
+                ur += pu[sp];
+            }
         }
     }
     if (MODE == SODAGPU_FP8 || TC) {
@@ -148,45 +188,46 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
             for (int u = 0; u < 16; ++u) a += v[u];
         }
         s_k[tid] = a;
-        __syncthreads();
-        if (tid < CT) {
-            double tt = 0.0;
-            for (int q = 0; q < PARTS; ++q) tt += s_k[tid * PARTS + q];
-            s_rs[tid] = tt;
-        }
-        __syncthreads();
     }
-    double xr = 0.0, ur = 0.0;
-#pragma unroll
-    for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
-        if (sp < ksplit) {
-            xr += px[sp];
-            ur += pu[sp];
-        }
+    __syncthreads();
+    if ((MODE == SODAGPU_FP8 || TC) && tid < CT) {
+        constexpr int PARTS = 256 / CT;
+        double tt = 0.0;
+        for (int q = 0; q < PARTS; ++q) tt += s_k[tid * PARTS + q];
+        s_rs[tid] = tt;
     }
+    __syncthreads();
     double delta = 0.0;
     if (snp >= 0) {
         if (MODE == SODAGPU_FP8 || TC) xr = xr * inv + x0 * s_rs[c];
         const ChainScal *S = &D.scal[c];
-        const double zz = D.xxd[b];
         CRng R;
         crng_init(R, D.seed, c, cur_rep(D), snp, P_SNP);
         int err = 0;
-        if (MODE == SODAGPU_FP64)
+        if (MODE == SODAGPU_FP64) {
             delta = draw_snp(D, S, c, cur_rep(D), snp, xr + ur, zz, zz / S->vare, R, &err);
-        else
-            delta = draw_snp_f(D, S, c, snp, (float)(xr + ur), (float)zz, (float)(zz / S->vare), R, &err, gold, cl,
-                               sg, pre);
+        } else {
+            DrawPre pre = s_pre[c];
+            pre.vs = vs;
+            if (D.ngroup > 1) {
+#pragma unroll
+                for (int q = 0; q < DRAW_PRE; ++q)
+                    pre.logp[q] = q < D.nmix ? (float)S->log_p[sg + q * D.ngroup] : 0.0f;
+            }
+            delta = draw_snp_f(D, S, c, snp, (float)(xr + ur), (float)zz, s_zzv[c], R, &err, gold, cl, sg, pre);
+        }
         if (err) flag_err(D, 1);
     }
+    float delta32 = 0.0f;
     if (act) {
+        delta32 = (float)delta;
         D.delta[(size_t)c * D.bs + jl] = delta;
-        if (MODE != SODAGPU_FP64) D.delta32[(size_t)jl * CT + c] = (float)delta;   // chain-contiguous
+        if (MODE != SODAGPU_FP64) D.delta32[(size_t)jl * CT + c] = delta32;   // chain-contiguous
     }
     if (TC) {
         if (jl < span) {
             uint32_t hi = 0, mid = 0, lo = 0;
-            if (delta != 0.0) tc::split3((float)(delta * inv), hi, mid, lo);
+            if (delta32 != 0.0f) tc::split3(delta32 * inv32, hi, mid, lo);
             D.dsplit[(size_t)c * D.ldd + jl] = (uint16_t)hi;
             D.dsplit[(size_t)(CT + c) * D.ldd + jl] = (uint16_t)mid;
             D.dsplit[(size_t)(2 * CT + c) * D.ldd + jl] = (uint16_t)lo;

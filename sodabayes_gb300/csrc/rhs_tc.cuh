@@ -23,8 +23,8 @@
 // the first code tiles) overlaps the previous kernel; residuals are read
 // after it completes.
 // The augmenting part u_j' ra_c (5% of the work) then runs on the FP32 cores
-// from staged windows of U.  Partial sums go to rpx/rpu, added and drawn by
-// k_draw.
+// from staged windows of U.  Partial sums go to rpx/rpu (as FP32), added and
+// drawn by k_draw.
 #pragma once
 #include <cuda.h>
 
@@ -276,10 +276,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
             for (int e = 0; e < 8; ++e) acc[g * 8 + e] = v[e];
         }
-        if (jk < N) {
+        if (jk < N) {   // FP32 partial sums (the accumulators are FP32)
+            float *px32 = reinterpret_cast<float *>(D.rpx);
 #pragma unroll
-            for (int c = 0; c < CT; ++c)
-                D.rpx[((size_t)ks * CT + c) * D.bs + jk] = (double)((acc[c] + acc[CT + c]) + acc[2 * CT + c]);
+            for (int c = 0; c < CT; ++c) px32[((size_t)ks * CT + c) * D.bs + jk] = (acc[c] + acc[CT + c]) + acc[2 * CT + c];
         }
     }
     tc::fence_before_sync();
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     for (int t = tid; t < TC_TM * CT; t += TC_THREADS) {
         const int m = t / CT, c = t % CT, jk = j0 + m;
-        if (jk < N) D.rpu[((size_t)ks * CT + c) * D.bs + jk] = (double)s_u[t];
+        if (jk < N) reinterpret_cast<float *>(D.rpu)[((size_t)ks * CT + c) * D.bs + jk] = s_u[t];
     }
 }
 
