@@ -177,9 +177,13 @@ def _make_job(spec, codes_dev, y, prec, chains, seed, numit=100000):
     return job
 
 
-def _rhs_bytes(n, N, chains, prec):
+def _rhs_bytes(n, N, chains, prec, tc=False):
     """Algorithmic bytes of one rhs launch: the subset's genotype columns and
-    augmenting columns once, plus each chain's residual copies."""
+    augmenting columns once, plus each chain's residual copies.  The
+    tensor-core rhs reads the upper triangle of U as three bf16 terms and the
+    residuals r and ra as their three-term bf16 splits."""
+    if tc:
+        return n * N + N * (N + 1) // 2 * 6 + chains * (n + N) * 6
     ex = {"fp8": 1, "fp32": 4, "fp64": 1}[prec]
     eu = {"fp8": 4, "fp32": 4, "fp64": 8}[prec]
     er = {"fp8": 4, "fp32": 4, "fp64": 8}[prec]
@@ -222,7 +226,7 @@ def bench_ours(args, rank, ws):
     nb = spec.p // BLOCKSIZE
     rhs_ms = prof["rhs"][0] / prof["rhs"][1]
     hbm, peak_kind = _peaks()
-    bytes_rhs = _rhs_bytes(spec.n, BLOCKSIZE, C, "fp8")
+    bytes_rhs = _rhs_bytes(spec.n, BLOCKSIZE, C, "fp8", tc=True)
     achieved = bytes_rhs / (rhs_ms / 1000.0) / 1e9
     res["roofline"] = {"bound": "hbm", "kernel": "k_rhs_tc<%d>" % C, "achieved": round(achieved, 1),
                        "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),

@@ -153,6 +153,9 @@ struct sodagpu_ctx {
     uint8_t *nzflag = nullptr;
     int tc = 0, ldd = 0;                 // tensor-core sweep
     uint16_t *dsplit = nullptr;
+    uint16_t *rsp = nullptr, *rasp = nullptr, *usp = nullptr;   // tensor-core rhs operands
+    int ldu = 0;
+    bool usp_ready = false;
     double *k0part = nullptr;
     float *rapart = nullptr;
     int32_t *raticket = nullptr;
@@ -757,6 +760,10 @@ int build_dev(sodagpu_ctx *c)
     D.rtab = c->rtab;
     D.atab = c->atab;
     D.tstride = sweep_tc_table_stride(c->bs);
+    D.rsp = c->rsp;
+    D.rasp = c->rasp;
+    D.usp = c->usp;
+    D.ldu = c->ldu;
     return 0;
 }
 
@@ -800,6 +807,11 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             TRY(c->alloc(&c->k0part, (((size_t)c->ldd * C + 255) / 256) * C));
             TRY(c->alloc(&c->rapart, (size_t)mt * (sweep_tc_ra_split() + 1) * C * 128));
             TRY(c->alloc(&c->raticket, mt));
+            const int NB = sweep_tc_rows(C);
+            c->ldu = (int)round_up((size_t)c->bs, 8);
+            TRY(c->alloc(&c->rsp, (size_t)NB * c->ldr));
+            TRY(c->alloc(&c->rasp, (size_t)NB * c->ldra));
+            TRY(c->alloc(&c->usp, (size_t)3 * p * c->ldu, false));
             const int ts = sweep_tc_table_stride(c->bs);
             c->h_rtab.assign((size_t)c->nb * ts, 0);
             c->h_atab.assign((size_t)c->nb * ts, 0);
@@ -822,12 +834,22 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             r = make_tmap_2d(&c->maps.codes64, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 128, 64,
                              CU_TENSOR_MAP_SWIZZLE_128B);
         if (r == CUDA_SUCCESS)
-            r = make_tmap_2d(&c->maps.r, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, c->r32, c->ldr, C, (uint64_t)c->ldr * 4, 128,
-                             C, CU_TENSOR_MAP_SWIZZLE_NONE);
+            r = make_tmap_2d(&c->maps.rsp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->rsp, c->ldr, NB, (uint64_t)c->ldr * 2,
+                             64, NB, CU_TENSOR_MAP_SWIZZLE_128B);
+        if (r == CUDA_SUCCESS)
+            r = make_tmap_2d(&c->maps.rasp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->rasp, c->ldra, NB,
+                             (uint64_t)c->ldra * 2, 64, NB, CU_TENSOR_MAP_SWIZZLE_128B);
+        if (r == CUDA_SUCCESS)
+            r = make_tmap_2d(&c->maps.usp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->usp, c->ldu, (uint64_t)3 * p,
+                             (uint64_t)c->ldu * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
         if (r == CUDA_SUCCESS)
             r = make_tmap_2d(&c->maps.d, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->dsplit, c->ldd, NB, (uint64_t)c->ldd * 2,
                              64, NB, CU_TENSOR_MAP_SWIZZLE_128B);
         if (r != CUDA_SUCCESS) return fail(SODAGPU_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        if (!c->usp_ready) {
+            CUDA_TRY(sweep_tc_prepare(c->G, c->D, c->st));
+            c->usp_ready = true;
+        }
     }
     RunCtl h{};
     CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));

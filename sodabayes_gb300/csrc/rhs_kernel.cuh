@@ -130,28 +130,21 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     }
     tc::pdl_trigger();
     tc::pdl_wait();
-    // the rhs partial sums of all splits (added in split order; FP32 from the tensor-core rhs)
+    // the rhs partial sums of all splits, added in split order (the tensor-core rhs
+    // gives one FP32 sum per split: codes' r + (sd u)' ra)
     double xr = 0.0, ur = 0.0;
     if (TC) {
-        const float *px32 = reinterpret_cast<const float *>(D.rpx), *pu32 = reinterpret_cast<const float *>(D.rpu);
-        float px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
+        const float *px32 = reinterpret_cast<const float *>(D.rpx);
+        float px[RHS_KSPLIT_MAX];
 #pragma unroll
         for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
-            px[sp] = pu[sp] = 0.0f;
-            if (act && sp < ksplit) {
-                const size_t o = ((size_t)sp * CT + c) * D.bs + jl;
-                px[sp] = __ldcg(px32 + o);
-                pu[sp] = __ldcg(pu32 + o);
-            }
+            px[sp] = 0.0f;
+            if (act && sp < ksplit) px[sp] = __ldcg(px32 + ((size_t)sp * CT + c) * D.bs + jl);
         }
-        float xs = 0.0f, us = 0.0f;
+        float xs = 0.0f;
 #pragma unroll
-        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) {
-            xs += px[sp];
-            us += pu[sp];
-        }
+        for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) xs += px[sp];
         xr = xs;
-        ur = us;
     } else {
         double px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
 #pragma unroll
@@ -199,7 +192,8 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     __syncthreads();
     double delta = 0.0;
     if (snp >= 0) {
-        if (MODE == SODAGPU_FP8 || TC) xr = xr * inv + x0 * s_rs[c];
+        if (TC) xr = xr * (inv != 0.0 ? inv : 1.0) + x0 * s_rs[c];   // columns with sd = 0 carry U unscaled
+        else if (MODE == SODAGPU_FP8) xr = xr * inv + x0 * s_rs[c];
         const ChainScal *S = &D.scal[c];
         CRng R;
         crng_init(R, D.seed, c, cur_rep(D), snp, P_SNP);

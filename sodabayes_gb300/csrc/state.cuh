@@ -15,6 +15,8 @@
 //   r32    float  [C][ldr]       FP32 copy read by the FP32/FP8 dot products
 //   ra     double [C][ldra]      augmented residual yAadj (ra32: FP32 copy)
 //   g, vara_s double [C][nloci], cls int32 [C][nloci] (by SNP id)
+//   tensor-core sweep only: rsp / rasp, the bf16 hi/mid/lo split of r32 /
+//   ra32 (written with them), and usp, the same split of U scaled by sd_k
 #pragma once
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -116,6 +118,10 @@ struct Dev {
     const int32_t *rtab;       // [nb][tstride] first rhs CTA of each 128-SNP tile, then the total
     const int32_t *atab;       // [nb][tstride] first ra-update CTA of each 128-row tile, then the total
     int tstride;
+    uint16_t *rsp;             // [round_up(3C,16)][ldr] bf16 hi/mid/lo of r32 (rows c, C+c, 2C+c), or null
+    uint16_t *rasp;            // [round_up(3C,16)][ldra] the same split of ra32, or null
+    const uint16_t *usp;       // [3][nloci][ldu] bf16 hi/mid/lo of U column k times sd_k (1 if sd_k = 0)
+    int ldu;                   // row stride of usp (bs rounded up to 8)
 };
 
 constexpr int RHS_KSPLIT_MAX = 16;

@@ -54,6 +54,31 @@ __device__ double block_sum(double v, double *sh /* >= 33 doubles */)
 
 __device__ __forceinline__ int cur_rep(const Dev &D) { return *((volatile int32_t *)&D.ctl->rep); }
 
+// Residual stores: the FP64 master, its FP32 copy and, when the tensor-core
+// rhs runs, the bf16 hi/mid/lo split of the FP32 copy that it loads by TMA.
+__device__ __forceinline__ void split_store(uint16_t *sp, size_t o, size_t part, float f)
+{
+    uint32_t h, m, l;
+    tc::split3(f, h, m, l);
+    sp[o] = (uint16_t)h;
+    sp[o + part] = (uint16_t)m;
+    sp[o + 2 * part] = (uint16_t)l;
+}
+__device__ __forceinline__ void store_r(const Dev &D, int c, int i, double v)
+{
+    const size_t o = (size_t)c * D.ldr + i;
+    D.r[o] = v;
+    D.r32[o] = (float)v;
+    if (D.rsp) split_store(D.rsp, o, (size_t)D.chains * D.ldr, (float)v);
+}
+__device__ __forceinline__ void store_ra(const Dev &D, int c, int i, double v)
+{
+    const size_t o = (size_t)c * D.ldra + i;
+    D.ra[o] = v;
+    D.ra32[o] = (float)v;
+    if (D.rasp) split_store(D.rasp, o, (size_t)D.chains * D.ldra, (float)v);
+}
+
 __device__ __forceinline__ void flag_err(const Dev &D, int code)
 {
     atomicExch(&D.ctl->err, code);
@@ -365,10 +390,8 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
     for (int q = 0; q < ROWS_PER_THREAD; ++q) {
         const int i = blockIdx.x * ROW_TILE + q * ROW_THREADS + threadIdx.x;
         if (i < D.n) {
-            const size_t o = (size_t)c * D.ldr + i;
-            const double v = (D.r[o] + mu_old) - mu;
-            D.r[o] = v;
-            D.r32[o] = (float)v;
+            const double v = (D.r[(size_t)c * D.ldr + i] + mu_old) - mu;
+            store_r(D, c, i, v);
             vs += v;
         }
     }
@@ -656,9 +679,7 @@ __global__ void __launch_bounds__(256) k_post(Dev D)
     for (int i = t0; i < D.naind; i += stride) {
         CRng R;
         crng_init(R, D.seed, c, rep, i, P_RA);
-        const double v = d_rnorm(0.0, sd, R);
-        D.ra[(size_t)c * D.ldra + i] = v;
-        D.ra32[(size_t)c * D.ldra + i] = (float)v;
+        store_ra(D, c, i, d_rnorm(0.0, sd, R));
     }
     if (!S->keep) return;
     const int m = D.method;
@@ -701,9 +722,7 @@ __global__ void __launch_bounds__(256) k_recal_apply(Dev D, int force, int mu_sl
     double d = 0.0;
     for (int s = 0; s < RECAL_SPLIT; ++s) d = d + D.recal_part[((size_t)c * RECAL_SPLIT + s) * D.ldr + i];
     const int slot = mu_slot >= 0 ? mu_slot : (rep & 1);
-    const double v = D.y[i] - d - D.scal[c].mu[slot];
-    D.r[(size_t)c * D.ldr + i] = v;
-    D.r32[(size_t)c * D.ldr + i] = (float)v;
+    store_r(D, c, i, D.y[i] - d - D.scal[c].mu[slot]);
 }
 
 // ---------------------------------------------------------------------------
@@ -722,8 +741,7 @@ __global__ void __launch_bounds__(256) k_init_chain(Dev D, double vara0, double 
     double rr = 0.0, vy = 0.0;
     for (int i = threadIdx.x; i < D.n; i += blockDim.x) {
         const double v = (D.y[i] - 0.0) - mu;
-        D.r[(size_t)c * D.ldr + i] = v;
-        D.r32[(size_t)c * D.ldr + i] = (float)v;
+        store_r(D, c, i, v);
         rr += v * v;
         vy += (D.y[i] - mu) * (D.y[i] - mu);
     }
@@ -801,8 +819,7 @@ __global__ void __launch_bounds__(256) k_init_chain(Dev D, double vara0, double 
             crng_init(R, D.seed, c, 0, i, P_RA);
             v = d_rnorm(0.0, sd, R);
         }
-        D.ra[(size_t)c * D.ldra + i] = v;
-        D.ra32[(size_t)c * D.ldra + i] = (float)v;
+        store_ra(D, c, i, v);
     }
 }
 
@@ -876,7 +893,8 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, const TcM
     cudaError_t e;
     {
         ProfScope ps(prof, st, PROF_RHS);
-        e = launch_pdl(k_rhs_tc<CT>, dim3(nrhs), dim3(TC_THREADS), RhsTc<CT>::SMEM, st, maps->codes128, maps->r, D, b);
+        e = launch_pdl(k_rhs_tc<CT>, dim3(nrhs), dim3(TC_THREADS), RhsTc<CT>::SMEM, st, maps->codes128, maps->rsp,
+                       maps->usp, maps->rasp, D, b);
     }
     if (e != cudaSuccess) return e;
     {
@@ -1044,6 +1062,35 @@ int sweep_tc_supported(int precision, int chains, int bs)
 
 int sweep_tc_rows(int chains) { return ((3 * chains + 15) / 16) * 16; }
 
+__global__ void __launch_bounds__(256) k_tc_prepare(int8_t *G, Dev D, uint16_t *usp)
+{
+    for (int k = blockIdx.x; k < D.p; k += gridDim.x) {
+        const double inv = D.xv[(size_t)k * 4 + 3];
+        const double sc = inv != 0.0 ? 1.0 / inv : 1.0;
+        const int len = D.ulen[k];
+        const int64_t off = D.uoff[k];
+        for (int i = threadIdx.x; i < D.ldu; i += blockDim.x) {
+            const double v = i < len ? D.U64[off + i] * sc : 0.0;
+            const __nv_bfloat16 h = __double2bfloat16(v);
+            const double r1 = v - (double)__bfloat162float(h);
+            const __nv_bfloat16 m = __double2bfloat16(r1);
+            const __nv_bfloat16 l = __double2bfloat16(r1 - (double)__bfloat162float(m));
+            usp[(size_t)k * D.ldu + i] = __bfloat16_as_ushort(h);
+            usp[((size_t)D.p + k) * D.ldu + i] = __bfloat16_as_ushort(m);
+            usp[((size_t)2 * D.p + k) * D.ldu + i] = __bfloat16_as_ushort(l);
+        }
+        if (inv == 0.0)
+            for (int i = threadIdx.x; i < D.ldx; i += blockDim.x) G[(size_t)k * D.ldx + i] = 0;
+    }
+}
+
+cudaError_t sweep_tc_prepare(int8_t *G, const Dev &D, cudaStream_t st)
+{
+    if (!D.usp || D.ldu <= 0) return cudaErrorInvalidValue;
+    k_tc_prepare<<<std::min(D.p, 4096), 256, 0, st>>>(G, D, const_cast<uint16_t *>(D.usp));
+    return cudaGetLastError();
+}
+
 int sweep_tc_ra_split() { return TU_RA_SPLIT; }
 
 int sweep_tc_table_stride(int bs) { return (bs + TC_TM - 1) / TC_TM + 1; }
@@ -1053,15 +1100,14 @@ void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count
     const int stride = sweep_tc_table_stride(bs);
     const int nst = ldx / TC_KC;
     for (int b = 0; b < nb; ++b) {
-        const int N = blk_sizes[b], tiles = (N + TC_TM - 1) / TC_TM, npad = (N + 7) & ~7;
+        const int N = blk_sizes[b], tiles = (N + TC_TM - 1) / TC_TM;
         int32_t *rt = rtab + (size_t)b * stride, *at = atab + (size_t)b * stride;
-        // rhs: weight of tile m = genotype bytes / 1024 + U rows (an FP32 U row of 128 columns
-        // costs about twice its 512 bytes on the FP32 cores)
+        // rhs: weight of tile m = its pipeline stages (genotype and U stages alike)
         long long W = 0;
-        for (int m = 0; m < tiles; ++m) W += ldx / 8 + std::min(npad, TC_TM * (m + 1));
+        for (int m = 0; m < tiles; ++m) W += rhs_tc_stages(nst, N, m, true, nullptr);
         int acc = 0;
         for (int m = 0; m < tiles; ++m) {
-            const long long w = ldx / 8 + std::min(npad, TC_TM * (m + 1));
+            const long long w = rhs_tc_stages(nst, N, m, true, nullptr);
             int ks = (int)(((long long)sm_count * w) / W);
             ks = std::max(1, std::min(ks, std::min(RHS_KSPLIT_MAX, nst)));
             rt[m] = acc;

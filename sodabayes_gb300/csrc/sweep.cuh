@@ -15,11 +15,16 @@ int sweep_tc_rows(int chains);
 int sweep_tc_ra_split();
 // Work tables of the tensor-core sweep (host side), per subset b of blk_sizes:
 // rtab[b*stride + m] = first rhs CTA of 128-SNP tile m, rtab[b*stride + tiles]
-// = rhs CTAs; tiles get K splits in proportion to their bytes (genotypes plus
-// the upper-triangular U rows).  atab likewise for the ra update: 128-row
+// = rhs CTAs; tiles get K splits in proportion to their pipeline stages
+// (genotype stages plus the U stages of the upper-triangular factor).  atab likewise for the ra update: 128-row
 // tiles get column splits in proportion to their triangular width.
 int sweep_tc_table_stride(int bs);
 void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab, int32_t *atab);
+// Set-up of the tensor-core rhs, once per job after the Z build: writes the
+// bf16 hi/mid/lo split of every U column k times sd_k into D.usp ([3][p][ldu];
+// sd_k = 1 where 1/sd_k is 0) and zeroes the codes of those columns in G (their
+// x values are all 0, so no product changes).
+cudaError_t sweep_tc_prepare(int8_t *G, const Dev &D, cudaStream_t st);
 // Optional per-launch event recording (eager profiling, never inside a graph):
 // before/after every launch an event pair is recorded and its kernel class
 // stored.  Classes: 0 rhs, 1 residual update, 2 mu, 3 everything else, 4 draws.
@@ -30,13 +35,13 @@ struct ProfHook {
     int n, cap;
 };
 
-// TMA descriptors of the tensor-core sweep: genotype codes in 128 x 128 and
-// 128 x 64 (individuals x SNPs) boxes with 128-byte swizzle, the FP32
-// residuals of all chains in 128 x chains boxes, and the bf16 delta split in
-// 64 x rows boxes with 128-byte swizzle; and the host copies of the work
-// tables.
+// TMA descriptors of the tensor-core sweep, all with 128-byte swizzle:
+// genotype codes in 128 x 128 and 128 x 64 (individuals x SNPs) boxes; the
+// bf16 splits of delta, r and ra in 64 x rows boxes; the bf16 U terms in
+// 64 x 128 (U rows x SNPs) boxes; and the host copies of the work tables.
 struct TcMaps {
-    CUtensorMap codes128, codes64, r, d;
+    CUtensorMap codes128, codes64, d;   // codes (128 x 128 and 64 x 128 boxes), delta split
+    CUtensorMap rsp, usp, rasp;         // residual split, U-term split, ra split
     const int32_t *h_rtab, *h_atab;   // host copies of D.rtab / D.atab
 };
 

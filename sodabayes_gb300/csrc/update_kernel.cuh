@@ -171,15 +171,10 @@ __global__ void __launch_bounds__(32 * UpdWarps<MODE, CT>::v) k_update(Dev D, in
             for (int ww = 0; ww < NW; ++ww) dsum += s_red[((size_t)ww * CT + c) * UT + rl];
             const double d = (double)dsum;
             if (rows) {
-                const size_t o = (size_t)c * D.ldr + i;
-                v = D.r[o] + d;
-                D.r[o] = v;
-                D.r32[o] = (float)v;
+                v = D.r[(size_t)c * D.ldr + i] + d;
+                store_r(D, c, i, v);
             } else {
-                const size_t o = (size_t)c * D.ldra + i;
-                const double va = D.ra[o] + d;
-                D.ra[o] = va;
-                D.ra32[o] = (float)va;
+                store_ra(D, c, i, D.ra[(size_t)c * D.ldra + i] + d);
             }
         }
         if (MODE == SODAGPU_FP8 && rows) {

@@ -241,10 +241,7 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
         }
         if (ok && row_ok) {
 #pragma unroll
-            for (int c = 0; c < HALF; ++c) {
-                D.r[(size_t)(h * HALF + c) * D.ldr + i] = rv[c];
-                D.r32[(size_t)(h * HALF + c) * D.ldr + i] = (float)rv[c];
-            }
+            for (int c = 0; c < HALF; ++c) store_r(D, h * HALF + c, i, rv[c]);
         }
 #pragma unroll
         for (int c = 0; c < HALF; ++c) {
@@ -359,10 +356,7 @@ __device__ __forceinline__ void update_tc_ra(const Dev &D, int b, unsigned char 
             for (int q = 0; q < 8; ++q)
                 if (q0 + q < ra_split) sum += pv[q];
         }
-        const size_t o = (size_t)c * D.ldra + i;
-        const double v = D.ra[o] + (double)sum;
-        D.ra[o] = v;
-        D.ra32[o] = (float)v;
+        store_ra(D, c, i, D.ra[(size_t)c * D.ldra + i] + (double)sum);
     }
     if (tid == 0) D.raticket[tr] = 0;
 }
