@@ -157,11 +157,11 @@ struct sodagpu_ctx {
     int ldu = 0;
     bool usp_ready = false;
     double *k0part = nullptr;
-    float *rapart = nullptr;
-    int32_t *raticket = nullptr;
+    float *vpart = nullptr;              // residual-update partial sums
+    unsigned long long *ugrid = nullptr;
     TcMaps maps{};
-    std::vector<int32_t> h_rtab, h_atab;   // work tables of the tensor-core sweep
-    int32_t *rtab = nullptr, *atab = nullptr;
+    std::vector<int32_t> h_rtab;         // work table of the tensor-core rhs
+    int32_t *rtab = nullptr;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
     cudaGraphExec_t graph = nullptr;
@@ -755,10 +755,10 @@ int build_dev(sodagpu_ctx *c)
     D.ldd = c->ldd;
     D.dsplit = c->dsplit;
     D.k0part = c->k0part;
-    D.rapart = c->rapart;
-    D.raticket = c->raticket;
+    D.vpart = c->vpart;
+    D.ugrid = c->ugrid;
+    D.nvt = sweep_tc_update_tiles(c->n);
     D.rtab = c->rtab;
-    D.atab = c->atab;
     D.tstride = sweep_tc_table_stride(c->bs);
     D.rsp = c->rsp;
     D.rasp = c->rasp;
@@ -801,12 +801,11 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         TRY(c->alloc(&c->rpu, (size_t)RHS_KSPLIT_MAX * C * c->bs));
         c->tc = c->cfg.kernels == SODAGPU_KERNELS_AUTO && sweep_tc_supported(c->cfg.precision, C, c->bs);
         if (c->tc) {
-            const int mt = (c->bs + 127) / 128;
             c->ldd = (int)round_up((size_t)c->bs, 128);
             TRY(c->alloc(&c->dsplit, (size_t)sweep_tc_rows(C) * c->ldd));
             TRY(c->alloc(&c->k0part, (((size_t)c->ldd * C + 255) / 256) * C));
-            TRY(c->alloc(&c->rapart, (size_t)mt * (sweep_tc_ra_split() + 1) * C * 128));
-            TRY(c->alloc(&c->raticket, mt));
+            TRY(c->alloc(&c->vpart, sweep_tc_vpart_floats(c->n, c->bs, C, c->sm_count), false));
+            TRY(c->alloc(&c->ugrid, 1));
             const int NB = sweep_tc_rows(C);
             c->ldu = (int)round_up((size_t)c->bs, 8);
             TRY(c->alloc(&c->rsp, (size_t)NB * c->ldr));
@@ -814,15 +813,10 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             TRY(c->alloc(&c->usp, (size_t)3 * p * c->ldu, false));
             const int ts = sweep_tc_table_stride(c->bs);
             c->h_rtab.assign((size_t)c->nb * ts, 0);
-            c->h_atab.assign((size_t)c->nb * ts, 0);
-            sweep_tc_tables(c->blk_sizes.data(), c->nb, c->bs, c->ldx, c->sm_count, c->h_rtab.data(),
-                            c->h_atab.data());
+            sweep_tc_tables(c->blk_sizes.data(), c->nb, c->bs, c->ldx, c->sm_count, c->h_rtab.data());
             TRY(c->alloc(&c->rtab, c->h_rtab.size(), false));
-            TRY(c->alloc(&c->atab, c->h_atab.size(), false));
             CUDA_TRY(cudaMemcpyAsync(c->rtab, c->h_rtab.data(), c->h_rtab.size() * 4, cudaMemcpyHostToDevice, c->st));
-            CUDA_TRY(cudaMemcpyAsync(c->atab, c->h_atab.data(), c->h_atab.size() * 4, cudaMemcpyHostToDevice, c->st));
             c->maps.h_rtab = c->h_rtab.data();
-            c->maps.h_atab = c->h_atab.data();
         }
     }
     build_dev(c);
@@ -831,8 +825,8 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         CUresult r = make_tmap_2d(&c->maps.codes128, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 128,
                                   128, CU_TENSOR_MAP_SWIZZLE_128B);
         if (r == CUDA_SUCCESS)
-            r = make_tmap_2d(&c->maps.codes64, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 128, 64,
-                             CU_TENSOR_MAP_SWIZZLE_128B);
+            r = make_tmap_2d(&c->maps.codes256, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 256, 64,
+                             CU_TENSOR_MAP_SWIZZLE_NONE);
         if (r == CUDA_SUCCESS)
             r = make_tmap_2d(&c->maps.rsp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->rsp, c->ldr, NB, (uint64_t)c->ldr * 2,
                              64, NB, CU_TENSOR_MAP_SWIZZLE_128B);
@@ -842,6 +836,9 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         if (r == CUDA_SUCCESS)
             r = make_tmap_2d(&c->maps.usp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->usp, c->ldu, (uint64_t)3 * p,
                              (uint64_t)c->ldu * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+        if (r == CUDA_SUCCESS)
+            r = make_tmap_2d(&c->maps.usp64, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->usp, c->ldu, (uint64_t)3 * p,
+                             (uint64_t)c->ldu * 2, 64, 64, CU_TENSOR_MAP_SWIZZLE_128B);
         if (r == CUDA_SUCCESS)
             r = make_tmap_2d(&c->maps.d, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->dsplit, c->ldd, NB, (uint64_t)c->ldd * 2,
                              64, NB, CU_TENSOR_MAP_SWIZZLE_128B);

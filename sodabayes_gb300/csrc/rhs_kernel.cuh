@@ -77,7 +77,9 @@ __device__ __forceinline__ float code_to_f32(uint32_t w, int k)
 
 // Per-SNP draws of one subset (models.f90:146-162, 211-256, 350-413) after
 // the rhs kernel left its split partial sums in rpx/rpu: one thread per
-// (SNP, chain) pair, chains of a SNP in consecutive lanes (CT divides 32).
+// (SNP, chain) pair; a CTA takes 256/CT consecutive SNPs, its threads
+// SNP-fastest so that the chain-major arrays (partial sums, g, class, delta
+// and its split) are read and written in contiguous runs.
 // Every load a draw needs is issued up front: the SNP's metadata and state,
 // and the partial sums of all splits at once (added in split order).  With
 // TC the kernel also writes what the tensor-core update reads (and takes the
@@ -91,9 +93,13 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     __shared__ double s_k[256];
     __shared__ DrawPre s_pre[CT];   // chain constants in FP32 (the FP64 pipe is narrow)
     __shared__ float s_zzv[CT];
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int t = blockIdx.x * 256 + tid;
-    const int jl = t / CT, c = t % CT;
+    __shared__ float s_d32[256];
+    __shared__ int s_nzf[256 / CT];
+    constexpr int SPC = 256 / CT;   // SNPs per CTA
+    const int tid = threadIdx.x;
+    const int jloc = tid % SPC, c = tid / SPC;
+    const int jl = blockIdx.x * SPC + jloc;
+    if (tid < SPC) s_nzf[tid] = 0;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
     const bool act = jl < N;
@@ -215,30 +221,36 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     float delta32 = 0.0f;
     if (act) {
         delta32 = (float)delta;
-        D.delta[(size_t)c * D.bs + jl] = delta;
-        if (MODE != SODAGPU_FP64) D.delta32[(size_t)jl * CT + c] = delta32;   // chain-contiguous
+        if (!TC) D.delta[(size_t)c * D.bs + jl] = delta;
+        if (delta != 0.0) s_nzf[jloc] = 1;
     }
+    s_d32[jloc * CT + c] = delta32;
     if (TC) {
         if (jl < span) {
             uint32_t hi = 0, mid = 0, lo = 0;
-            if (delta32 != 0.0f) tc::split3(delta32 * inv32, hi, mid, lo);
+            // delta / sd; columns with sd = 0 (zero codes) carry delta for the unscaled U
+            if (delta32 != 0.0f) tc::split3(delta32 * (inv32 != 0.0f ? inv32 : 1.0f), hi, mid, lo);
             D.dsplit[(size_t)c * D.ldd + jl] = (uint16_t)hi;
             D.dsplit[(size_t)(CT + c) * D.ldd + jl] = (uint16_t)mid;
             D.dsplit[(size_t)(2 * CT + c) * D.ldd + jl] = (uint16_t)lo;
         }
         // this CTA's sum of x0_j delta_j per chain, SNPs in order
         __syncthreads();
-        s_k[tid] = x0 * delta;
-        __syncthreads();
-        if (tid < CT) {
-            double tt = 0.0;
-            for (int q = 0; q < 256 / CT; ++q) tt += s_k[q * CT + tid];
-            D.k0part[(size_t)blockIdx.x * CT + tid] = tt;
-        }
+        s_k[jloc * CT + c] = x0 * delta;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, act && delta != 0.0);
-    const unsigned grp = CT >= 32 ? 0xffffffffu : (((1u << CT) - 1u) << ((lane / CT) * CT));
-    if (act && c == 0) D.nzflag[jl] = (m & grp) != 0u;
+    __syncthreads();
+    if (TC && tid < CT) {
+        double tt = 0.0;
+        for (int q = 0; q < SPC; ++q) tt += s_k[q * CT + tid];
+        D.k0part[(size_t)blockIdx.x * CT + tid] = tt;
+    }
+    // delta32 chain-contiguous per SNP (the CTA's block of 256 values), and the flags of SNPs whose
+    // delta is non-zero in some chain
+    if (MODE != SODAGPU_FP64) {
+        const int j = blockIdx.x * SPC + tid / CT;
+        if (j < N) D.delta32[(size_t)blockIdx.x * 256 + tid] = s_d32[tid];
+    }
+    if (tid < SPC && blockIdx.x * SPC + tid < N) D.nzflag[blockIdx.x * SPC + tid] = s_nzf[tid];
 }
 
 template <int MODE, int CT>

@@ -19,8 +19,8 @@
 //   warp 16 (one thread) TMA: each stage's A tile (codes: 128 x 128 bytes;
 //           U terms: 128 x 64 bf16) and B tile, all 128-byte swizzled, into a
 //           raw buffer (NS buffers in flight);
-//   warps 0-15 convert a genotype stage's codes into the double-buffered bf16
-//           operand in tensor memory (lane = SNP, tcgen05.st);
+//   warps 0-15 convert a genotype stage's codes into one of four bf16
+//           operands in tensor memory (lane = SNP, tcgen05.st);
 //   warp 17 (one thread) issues the stage's MMAs (A from tensor memory or,
 //           for U stages, from the raw buffer; B always from the raw buffer)
 //           and commits their completion, which frees the buffers.
@@ -38,6 +38,7 @@ constexpr int TC_KC = 128;       // individuals per genotype stage
 constexpr int TC_KU = 64;        // U rows per augmenting stage
 constexpr int TC_THREADS = 576;  // 16 converter warps, the TMA warp, the MMA warp
 constexpr int TC_CONV = 512;     // converter threads
+constexpr int TC_NOB = 4;        // bf16 codes operands in tensor memory (converters run up to 4 stages ahead)
 constexpr int TC_WARP_TMA = 16, TC_WARP_MMA = 17;
 
 template <int CT>
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     using T = RhsTc<CT>;
     constexpr int NB = T::NB, NS = T::NS;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
-    __shared__ uint64_t s_full[NS], s_empty[NS], s_conv[2], s_opfree[2], s_done;
+    __shared__ uint64_t s_full[NS], s_empty[NS], s_conv[TC_NOB], s_opfree[TC_NOB], s_done;
     __shared__ uint32_t s_tmem;
     __shared__ int s_err;
     unsigned char *raw0 = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc::mbar_init(&s_full[i], 1);
             tc::mbar_init(&s_empty[i], TC_CONV + 1);    // converters + the MMAs reading B (and U's A)
         }
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < TC_NOB; ++i) {
             tc::mbar_init(&s_conv[i], TC_CONV);
             tc::mbar_init(&s_opfree[i], 1);
         }
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc::mbar_fence_init();
         s_err = 0;
     }
-    if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 256);   // accumulator 0-63, codes operand 64-191
+    if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 512);   // accumulator 0-63, codes operands 64-319
     tc::pdl_trigger();
     tc::fence_before_sync();
     __syncthreads();
@@ -172,8 +173,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const int buf = s % NS;
                 const uint32_t rb = tc::smem_u32(raw0 + (size_t)buf * T::RAW);
                 if (s < nck) {
-                    const int ob = s & 1;
-                    if (!tc::mbar_wait(&s_conv[ob], (s >> 1) & 1)) {
+                    const int ob = s % TC_NOB;
+                    if (!tc::mbar_wait(&s_conv[ob], (s / TC_NOB) & 1)) {
                         s_err = 1;
                         break;
                     }
@@ -206,11 +207,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // converters: genotype stages -> bf16 codes in tensor memory; augmenting stages
         // need no conversion (they only release the buffer after its TMA completed)
         for (int s = 0; s < ns; ++s) {
-            const int buf = s % NS, ob = s & 1;
+            const int buf = s % NS, ob = s % TC_NOB;
             bool ok = tc::mbar_wait(&s_full[buf], (s / NS) & 1);
             if (s < nck) {
-                // the operand buffer was last read by the MMAs of stage s-2
-                if (ok && s >= 2) ok = tc::mbar_wait(&s_opfree[ob], ((s - 2) >> 1) & 1);
+                // the operand buffer was last read by the MMAs of stage s - TC_NOB
+                if (ok && s >= TC_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
                 if (!ok) {
                     s_err = 1;
                     break;
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     if (warp == TC_WARP_MMA) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tm, 256);
+        tc::tmem_dealloc(tm, 512);
     }
 }
 

@@ -113,10 +113,10 @@ struct Dev {
     int ldd;                   // row stride of dsplit (bs rounded up to 128)
     uint16_t *dsplit;          // [round_up(3C,16)][ldd] bf16 hi/mid/lo of delta/sd per chain
     double *k0part;            // [draw CTAs][C] per-CTA sums of x0_j delta_j
-    float *rapart;             // [ra tiles][TU_RA_SPLIT][C][128] ra update partial sums
-    int32_t *raticket;         // [ra tiles] ra update tickets (self-resetting)
+    float *vpart;              // [tiles + update CTAs][C][256] update partial sums, one slot per segment
+    unsigned long long *ugrid; // grid-barrier counter of the update (each launch adds its CTA count)
+    int nvt;                   // row tiles of 256 individuals of the update
     const int32_t *rtab;       // [nb][tstride] first rhs CTA of each 128-SNP tile, then the total
-    const int32_t *atab;       // [nb][tstride] first ra-update CTA of each 128-row tile, then the total
     int tstride;
     uint16_t *rsp;             // [round_up(3C,16)][ldr] bf16 hi/mid/lo of r32 (rows c, C+c, 2C+c), or null
     uint16_t *rasp;            // [round_up(3C,16)][ldra] the same split of ra32, or null

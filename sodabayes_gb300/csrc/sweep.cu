@@ -54,8 +54,9 @@ __device__ double block_sum(double v, double *sh /* >= 33 doubles */)
 
 __device__ __forceinline__ int cur_rep(const Dev &D) { return *((volatile int32_t *)&D.ctl->rep); }
 
-// Residual stores: the FP64 master, its FP32 copy and, when the tensor-core
-// rhs runs, the bf16 hi/mid/lo split of the FP32 copy that it loads by TMA.
+// Residual stores: the FP64 master and, for the FP32-core rhs, its FP32 copy,
+// or, when the tensor-core rhs runs, the bf16 hi/mid/lo split of the FP32
+// value that it loads by TMA.
 __device__ __forceinline__ void split_store(uint16_t *sp, size_t o, size_t part, float f)
 {
     uint32_t h, m, l;
@@ -68,7 +69,7 @@ __device__ __forceinline__ void store_r(const Dev &D, int c, int i, double v)
 {
     const size_t o = (size_t)c * D.ldr + i;
     D.r[o] = v;
-    D.r32[o] = (float)v;
+    if (!D.tc) D.r32[o] = (float)v;   // read only by the FP32-core dot products
     if (D.rsp) split_store(D.rsp, o, (size_t)D.chains * D.ldr, (float)v);
 }
 __device__ __forceinline__ void store_ra(const Dev &D, int c, int i, double v)
@@ -884,12 +885,11 @@ static cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
 // per SM), then the update (row tiles of r on the tensor cores, ra tiles on
 // the FP32 cores; two CTAs per SM).
 template <int CT>
-static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, const TcMaps *maps, cudaStream_t st,
-                                  ProfHook *prof)
+static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_count, const TcMaps *maps,
+                                   cudaStream_t st, ProfHook *prof)
 {
     const int mtiles = (nblk_snps + TC_TM - 1) / TC_TM;
     const int nrhs = maps->h_rtab[(size_t)b * D.tstride + mtiles];
-    const int nra = maps->h_atab[(size_t)b * D.tstride + mtiles];
     cudaError_t e;
     {
         ProfScope ps(prof, st, PROF_RHS);
@@ -905,8 +905,9 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, const TcM
     if (e != cudaSuccess) return e;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
-        e = launch_pdl(k_update_tc<CT>, dim3(D.nr_ctas + nra), dim3(TU_THREADS), UpdTc<CT>::SMEM, st, maps->codes64,
-                       maps->d, D, b);
+        e = launch_pdl(k_update_tc<CT>, dim3(std::min(sm_count, TV_MAXG)), dim3(TV_THREADS), UpdTc<CT>::SMEM, st,
+                       maps->codes256, maps->d, maps->usp64, D, b);
+
     }
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
@@ -917,7 +918,7 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
                                ProfHook *prof)
 {
     if constexpr (MODE == SODAGPU_FP8 && CT >= 4) {
-        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, maps, st, prof);
+        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, sm_count, maps, st, prof);
     }
     constexpr int MTS = 8 * SptOf<CT>::v;
     const int mtiles = (nblk_snps + MTS - 1) / MTS;
@@ -1052,12 +1053,21 @@ static cudaError_t set_tc_smem()
         e = cudaFuncSetAttribute(k_update_tc<CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UpdTc<CT>::SMEM);
     if (e == cudaSuccess) e = max_carveout(k_rhs_tc<CT>);
     if (e == cudaSuccess) e = max_carveout(k_update_tc<CT>);
+
     return e;
 }
 
 int sweep_tc_supported(int precision, int chains, int bs)
 {
-    return precision == SODAGPU_FP8 && (chains == 4 || chains == 8 || chains == 16) && bs <= TU_MAXQ * TU_KC;
+    return precision == SODAGPU_FP8 && (chains == 4 || chains == 8 || chains == 16) && bs <= TV_MAXQ * TV_K;
+}
+
+int sweep_tc_update_tiles(int n) { return (n + TV_N - 1) / TV_N; }
+
+size_t sweep_tc_vpart_floats(int n, int bs, int chains, int sm_count)
+{
+    const size_t slots = (size_t)sweep_tc_update_tiles(n) + (size_t)((bs + TV_N - 1) / TV_N) + (size_t)sm_count;
+    return slots * (size_t)chains * TV_N;
 }
 
 int sweep_tc_rows(int chains) { return ((3 * chains + 15) / 16) * 16; }
@@ -1091,17 +1101,15 @@ cudaError_t sweep_tc_prepare(int8_t *G, const Dev &D, cudaStream_t st)
     return cudaGetLastError();
 }
 
-int sweep_tc_ra_split() { return TU_RA_SPLIT; }
-
 int sweep_tc_table_stride(int bs) { return (bs + TC_TM - 1) / TC_TM + 1; }
 
-void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab, int32_t *atab)
+void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab)
 {
     const int stride = sweep_tc_table_stride(bs);
     const int nst = ldx / TC_KC;
     for (int b = 0; b < nb; ++b) {
         const int N = blk_sizes[b], tiles = (N + TC_TM - 1) / TC_TM;
-        int32_t *rt = rtab + (size_t)b * stride, *at = atab + (size_t)b * stride;
+        int32_t *rt = rtab + (size_t)b * stride;
         // rhs: weight of tile m = its pipeline stages (genotype and U stages alike)
         long long W = 0;
         for (int m = 0; m < tiles; ++m) W += rhs_tc_stages(nst, N, m, true, nullptr);
@@ -1114,18 +1122,6 @@ void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count
             acc += ks;
         }
         rt[tiles] = acc;
-        // ra update: tile t meets the columns k >= 128 t of the upper-triangular factor
-        long long Wa = 0;
-        for (int t = 0; t < tiles; ++t) Wa += N - TC_TM * t;
-        const int total = TU_RA_SPLIT * tiles;
-        acc = 0;
-        for (int t = 0; t < tiles; ++t) {
-            int sp = (int)(((long long)total * (N - TC_TM * t)) / Wa);
-            sp = std::max(1, std::min(sp, 64));
-            at[t] = acc;
-            acc += sp;
-        }
-        at[tiles] = acc;
     }
 }
 

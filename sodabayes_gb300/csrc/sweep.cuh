@@ -8,18 +8,20 @@ namespace soda {
 
 int sweep_chain_count_supported(int chains);
 cudaError_t sweep_prepare(int bs);
-// Tensor-core sweep: whether it applies, the rows of its delta split
-// (3 * chains rounded up to 16) and the CTAs per 128-row tile of ra.
+// Tensor-core sweep: whether it applies and the rows of its delta split
+// (3 * chains rounded up to 16).
 int sweep_tc_supported(int precision, int chains, int bs);
 int sweep_tc_rows(int chains);
-int sweep_tc_ra_split();
-// Work tables of the tensor-core sweep (host side), per subset b of blk_sizes:
+// The residual update's row tiles (256 individuals) and the floats of its
+// partial-sum slots (one per tile segment: tiles + CTAs slots of 3C x 256).
+int sweep_tc_update_tiles(int n);
+size_t sweep_tc_vpart_floats(int n, int bs, int chains, int sm_count);
+// Work tables of the tensor-core rhs (host side), per subset b of blk_sizes:
 // rtab[b*stride + m] = first rhs CTA of 128-SNP tile m, rtab[b*stride + tiles]
 // = rhs CTAs; tiles get K splits in proportion to their pipeline stages
-// (genotype stages plus the U stages of the upper-triangular factor).  atab likewise for the ra update: 128-row
-// tiles get column splits in proportion to their triangular width.
+// (genotype stages plus the U stages of the upper-triangular factor).
 int sweep_tc_table_stride(int bs);
-void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab, int32_t *atab);
+void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab);
 // Set-up of the tensor-core rhs, once per job after the Z build: writes the
 // bf16 hi/mid/lo split of every U column k times sd_k into D.usp ([3][p][ldu];
 // sd_k = 1 where 1/sd_k is 0) and zeroes the codes of those columns in G (their
@@ -35,14 +37,15 @@ struct ProfHook {
     int n, cap;
 };
 
-// TMA descriptors of the tensor-core sweep, all with 128-byte swizzle:
-// genotype codes in 128 x 128 and 128 x 64 (individuals x SNPs) boxes; the
+// TMA descriptors of the tensor-core sweep: genotype codes in 128 x 128
+// (individuals x SNPs, 128-byte swizzle) and 256 x 64 (unswizzled) boxes; the
 // bf16 splits of delta, r and ra in 64 x rows boxes; the bf16 U terms in
-// 64 x 128 (U rows x SNPs) boxes; and the host copies of the work tables.
+// 64 x 128 and 64 x 64 (U rows x SNPs) boxes (all 128-byte swizzle); and the
+// host copy of the rhs work table.
 struct TcMaps {
-    CUtensorMap codes128, codes64, d;   // codes (128 x 128 and 64 x 128 boxes), delta split
-    CUtensorMap rsp, usp, rasp;         // residual split, U-term split, ra split
-    const int32_t *h_rtab, *h_atab;   // host copies of D.rtab / D.atab
+    CUtensorMap codes128, codes256, d;  // codes (128 x 128 and 256 x 64 boxes), delta split
+    CUtensorMap rsp, usp, usp64, rasp;  // residual split, U-term split (two box heights), ra split
+    const int32_t *h_rtab;              // host copy of D.rtab
 };
 
 // Enqueues one Gibbs iteration of every chain on `st` (graph-capturable when

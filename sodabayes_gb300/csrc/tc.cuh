@@ -32,12 +32,29 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr, uint32_t sbo_byte
     return d;
 }
 
+// Descriptor of an MN-major operand with 128-byte swizzle: 1024-byte atoms of
+// 64 bf16 along M/N by 8 rows of K; lbo = byte stride between atoms along
+// M/N, sbo = byte stride between 8-row groups of K.
+__device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo_bytes >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= (uint64_t)2u << 61;
+    return d;
+}
+
 // Instruction descriptor for kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, shape M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+
+// The same with B MN-major (N contiguous in shared memory).
+__host__ __device__ constexpr uint32_t idesc_bf16_bmn(int M, int N) { return idesc_bf16(M, N) | (1u << 16); }
 
 // byte offset of the 16-byte chunk holding (row, k..k+7) in a K-major SW128
 // tile with `rows` rows (k a multiple of 8)

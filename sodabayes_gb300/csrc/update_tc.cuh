@@ -3,76 +3,294 @@
 // sweep.cu after rhs_tc.cuh.
 //
 //   r  += X_b delta = sum_j x0_j delta_j + G_b (delta / sd)
-//   ra += U_b delta
+//   ra += U_b delta = (U_b sd) (delta / sd)
 //
-// Row tiles of r (128 individuals, one CTA each) run on tcgen05: A = the
-// tile's codes of 64 subset positions per stage, transposed to individual-major
-// bf16 in tensor memory (lane = individual, written with tcgen05.st), B = the
-// three-way bf16 split of delta/sd written by the draws (k_draw), D = 128 x
-// 3*chains FP32 in tensor memory.  Stages whose 64 positions have no
-// non-zero delta in any chain are skipped.  The pipeline is the one of
-// k_rhs_tc: warp 8 loads each stage's code tile and delta-split tile by TMA
-// (both 128-byte swizzled; the MMA reads the delta split straight from the
-// raw buffer), warps 0-7 gather and convert the codes, warp 9 issues the
-// MMAs.  The centring term sum_j x0_j delta_j is added in FP64 from the
-// per-CTA sums of the draws.  The augmented rows ra (U_b is FP32; a tile of
-// 128 rows is split over column ranges, D.atab giving wider tiles more CTAs)
-// run on the FP32 cores; the last CTA of a row tile adds the split partial
-// sums in split order (deterministic).
+// Both products run on tcgen05 as transposed products D = S B' with
+//   S (operand A, K-major, TMA) = the bf16 hi/mid/lo split of delta/sd written
+//     by the draws (delta itself for columns with sd = 0, whose codes are
+//     zero): rows term * chains + c (3 * chains of the M = 128 rows are
+//     used), K = subset positions, 64 per stage;
+//   B (N = 256) = for r, the genotype codes of 256 individuals, loaded by TMA
+//     as they are stored (64 positions x 256 bytes) and widened to bf16 by
+//     the converter warps into an MN-major operand (individuals contiguous);
+//     for ra, one bf16 term of sd * U (256 rows of U), loaded by TMA straight
+//     into an MN-major operand (the factor is stored column by column);
+//   D = 128 x 256 FP32 in tensor memory, double-buffered.
+// A tcgen05.mma costs about the same for any N up to 256, so the codes sit on
+// the N = 256 side: one instruction consumes 4 KB of codes.
+//
+// Work units: (row tile of 256 individuals, active stage) and, for ra,
+// (tile of 256 rows of U, active stage, U term); stages whose 64 positions
+// have no non-zero delta in any chain are inactive, and an upper-triangular
+// factor meets a row tile only from its first row on.  The units are laid
+// out row tiles first and split evenly over the CTAs (one per SM); a CTA's
+// consecutive units of one tile form a segment, whose accumulator rows go to
+// vpart as FP32 partial sums.  After a grid-wide barrier (one CTA per SM, all
+// resident; the wait is bounded) every CTA takes an equal share of the
+// (128-element half tile, chain) pairs: it adds the pair's segments in
+// segment order (deterministic) and applies hi + mid + lo and the centring
+// term sum_j x0_j delta_j (FP64) to the FP64 residuals.
+//
+// Warp roles (mbarrier hand-offs, every wait bounded): warp 8 issues the TMA
+// loads, warps 0-7 widen the codes, warp 9 issues the MMAs, warps 10-13
+// reduce the centring term and move finished accumulators to vpart; all
+// warps then take part in the reductions.
 #pragma once
 
 namespace soda {
 
-constexpr int TU_KC = 64;          // subset positions per stage
-constexpr int TU_NS = 6;           // raw stages in flight
-constexpr int TU_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
-constexpr int TU_RA_SPLIT = 8;     // ra-update CTAs per 128-row tile, on average
-constexpr int TU_UNR = 8;          // U columns in flight per warp
-constexpr int TU_THREADS = 320;    // 8 converter warps, the TMA warp, the MMA warp
-constexpr int TU_CONV = 256;
-constexpr int TU_WARP_TMA = 8, TU_WARP_MMA = 9;
+constexpr int TV_N = 256;          // individuals per row tile / rows of U per ra tile (MMA N)
+constexpr int TV_K = 64;           // subset positions per stage
+constexpr int TV_NA = 4;           // delta-split tiles (operand A) in flight
+constexpr int TV_NC = 4;           // code tiles in flight
+constexpr int TV_NOB = 2;          // B operands
+constexpr int TV_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
+constexpr int TV_MAXRA = 64;       // ra tiles per subset
+constexpr int TV_THREADS = 448;    // 8 converter warps, TMA, MMA, 4 epilogue warps
+constexpr int TV_MAXG = 512;       // CTAs (one per SM)
+constexpr int TV_WROW = 1, TV_WRA = 1;   // unit weights of the split (row / ra units)
+constexpr int TV_CONV = 256;
+constexpr int TV_WARP_TMA = 8, TV_WARP_MMA = 9, TV_WARP_EPI = 10;
 
 template <int CT>
 struct UpdTc {
     static constexpr int NB = RhsTc<CT>::NB;
-    static constexpr int RAW_A = TU_KC * 128;          // codes: 64 positions x 128 individuals (TMA, swizzled)
-    static constexpr int RAW_B = NB * TU_KC * 2;       // bf16 split of delta/sd (TMA, swizzled; MMA operand B)
-    static constexpr int RAW = RAW_A + RAW_B;
-    static constexpr int PIPE = TU_NS * RAW;           // (the codes operand lives in tensor memory)
-    static constexpr int RED = 4 * CT * 128 * 4;       // column-group partials of the ra tiles
-    static constexpr size_t SMEM = 1024 + (size_t)(PIPE > RED ? PIPE : RED);
-    static_assert(RAW % 1024 == 0 && RAW_A % 1024 == 0, "buffers must keep 1024-byte alignment");
+    static constexpr int ROWS = 3 * CT;                // accumulator rows in use
+    static constexpr int RAW_A = NB * TV_K * 2;        // delta split tile: NB rows x 64 bf16, 128-byte swizzle
+    // an M = 128 MMA reads 128 rows (16 KB) from A's start: each A slot owns 16 KB, so that no
+    // byte the MMA reads is the target of a TMA load in flight (rows past NB are never written)
+    static constexpr int ASTRIDE = 128 * 128;
+    static constexpr int AREG = TV_NA * ASTRIDE;
+    static constexpr int RAW_C = TV_K * TV_N;          // codes: 64 positions x 256 individuals, unswizzled
+    static constexpr int C0 = AREG;
+    static constexpr int BOP = TV_K * TV_N * 2;        // B operand: 64 x 256 bf16
+    static constexpr int BOP0 = C0 + TV_NC * RAW_C;
+    static constexpr size_t SMEM = 1024 + (size_t)BOP0 + (size_t)TV_NOB * BOP;
+    static_assert(RAW_A % 1024 == 0 && AREG % 1024 == 0 && RAW_C % 1024 == 0, "buffer alignment");
 };
 
+// Units of one subset, as every role decodes them.
+struct UnitPlan {
+    int nact, nvt, nra, R, W;        // active stages, row tiles, ra tiles, row units, all units
+    int qs[TV_MAXRA];                // first active stage of each ra tile
+    int pref[TV_MAXRA + 1];          // first ra unit of each ra tile (relative to R)
+};
+
+struct Unit {
+    int kind, tile, q, term;         // kind 0: r, 1: ra; tile; index into the active stages; U term
+};
+
+__device__ __forceinline__ Unit decode_unit(const UnitPlan &P, int u, int &ra_hint)
+{
+    Unit x;
+    if (u < P.R) {
+        x.kind = 0;
+        x.tile = u / P.nact;
+        x.q = u - x.tile * P.nact;
+        x.term = 0;
+        return x;
+    }
+    const int v = u - P.R;
+    int a = ra_hint;
+    while (a + 1 < P.nra && P.pref[a + 1] <= v) ++a;
+    ra_hint = a;
+    const int w = v - P.pref[a];
+    x.kind = 1;
+    x.tile = a;
+    x.q = P.qs[a] + w / 3;
+    x.term = w % 3;
+    return x;
+}
+
+// First unit of CTA q when the units are split over G CTAs in equal shares of
+// weight (row units TV_WROW, ra units TV_WRA).
+__device__ __forceinline__ int split_bound(const UnitPlan &P, int q, int G)
+{
+    const long long wt = (long long)TV_WROW * P.R + (long long)TV_WRA * (P.W - P.R);
+    const long long x = ((long long)q * wt) / G;
+    if (x <= (long long)TV_WROW * P.R) return (int)((x + TV_WROW - 1) / TV_WROW);
+    return P.R + (int)((x - (long long)TV_WROW * P.R + TV_WRA - 1) / TV_WRA);
+}
+
+// CTA holding unit u: the last q with bnd[q] <= u.
+__device__ __forceinline__ int unit_cta(const int *bnd, int u, int G)
+{
+    int lo = 0, hi = G - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (bnd[mid] <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The centring term sum_j x0_j delta_j of the subset per chain into s_k0,
+// from the per-CTA sums of the draws (parts in a fixed order), by the 128
+// threads of the epilogue warps.
 template <int CT>
-__device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, const CUtensorMap *tm_d, const Dev &D,
-                                               int b, unsigned char *base)
+__device__ __forceinline__ void update_k0(const Dev &D, int b, int t, double *s_k0p, double *s_k0)
+{
+    constexpr int PARTS = 128 / CT;
+    const int N = D.blk_ls[b + 1] - D.blk_ls[b];
+    const int c = t / PARTS, part = t % PARTS;
+    const int ntl = (((N + TC_TM - 1) / TC_TM) * TC_TM * CT + 255) / 256;
+    double a = 0.0;
+    for (int q0 = part; q0 < ntl; q0 += 8 * PARTS) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int q = q0 + u * PARTS;
+            v[u] = q < ntl ? __ldcg(D.k0part + (size_t)q * CT + c) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a += v[u];
+    }
+    s_k0p[t] = a;
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (t < CT) {
+        double s = 0.0;
+        for (int q = 0; q < PARTS; ++q) s += s_k0p[t * PARTS + q];
+        s_k0[t] = s;
+    }
+}
+
+// Units [u0, u1) of global tile tg (row tiles, then ra tiles).
+__device__ __forceinline__ void tile_units(const UnitPlan &P, int tg, long long &u0, long long &u1)
+{
+    if (tg < P.nvt) {
+        u0 = (long long)tg * P.nact;
+        u1 = u0 + P.nact;
+    } else {
+        u0 = P.R + P.pref[tg - P.nvt];
+        u1 = P.R + P.pref[tg - P.nvt + 1];
+    }
+}
+
+// Adds the segments of chain c in half h (128 elements) of global tile tg in
+// segment order and applies the update: r, its bf16 split and the 128-row
+// partial sum of r for a row tile, ra and its split for an ra tile.  Lane l
+// takes the elements l + 32k of the half; the loads of up to four segments
+// are issued together.
+template <int CT>
+__device__ __forceinline__ void update_reduce_pair(const Dev &D, const UnitPlan &P, const int *bnd, int G, int tg,
+                                                   int h, int c, const double *s_k0, int N)
+{
+    const int lane = threadIdx.x & 31;
+    const bool is_r = tg < P.nvt;
+    const int tile = is_r ? tg : tg - P.nvt;
+    const int lim = is_r ? D.n : min(N, D.bs);
+    long long u0, u1;
+    tile_units(P, tg, u0, u1);
+    if (u1 <= u0) return;   // no unit touched this tile: nothing changed
+    const int sl = unit_cta(bnd, (int)u0, G), sh = unit_cta(bnd, (int)u1 - 1, G);
+    double rold[4];
+    float acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = tile * TV_N + h * 128 + lane + 32 * k;
+        rold[k] = 0.0;
+        if (i < lim) rold[k] = is_r ? __ldcg(D.r + (size_t)c * D.ldr + i) : __ldcg(D.ra + (size_t)c * D.ldra + i);
+        acc[k] = 0.0f;
+    }
+    for (int q0 = sl; q0 <= sh; q0 += 4) {
+        float v[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u;
+            const bool ok = q <= sh && bnd[q] < bnd[q + 1];   // CTAs without units have no slot
+            const float *pp = D.vpart + ((size_t)(tg + q) * CT + c) * TV_N + h * 128 + lane;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[u][k] = ok ? __ldcg(pp + 32 * k) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[k] += v[u][k];
+    }
+    float part = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = tile * TV_N + h * 128 + lane + 32 * k;
+        if (is_r) {
+            const double rn = rold[k] + ((double)acc[k] + s_k0[c]);
+            if (i < lim) {
+                const size_t o = (size_t)c * D.ldr + i;
+                D.r[o] = rn;
+                split_store(D.rsp, o, (size_t)D.chains * D.ldr, (float)rn);
+                part += (float)rn;
+            }
+        } else if (i < lim) {
+            store_ra(D, c, i, rold[k] + (double)acc[k]);
+        }
+    }
+    if (is_r) {
+        const float ws = warp_sumf(part);
+        if (lane == 0 && 2 * tile + h < D.nr_ctas) D.rsum[(size_t)c * D.nr_ctas + 2 * tile + h] = (double)ws;
+    }
+}
+
+// Grid-wide barrier of the G CTAs of one launch on a monotonic counter (each
+// launch adds G); bounded by %globaltimer (20 ms), false on time-out.
+__device__ __forceinline__ bool update_grid_sync(unsigned long long *ctr, unsigned G)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long old = atomicAdd(ctr, 1ull);
+        const unsigned long long target = (old / G + 1) * G;
+        const uint64_t t0 = tc::globaltimer_ns();
+        int ok = 1;
+        for (;;) {
+            unsigned long long v;
+            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ctr) : "memory");
+            if (v >= target) break;
+            if (tc::globaltimer_ns() - t0 > 20000000ull) {
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int CT>
+__global__ void __launch_bounds__(TV_THREADS, 1)
+    k_update_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_d,
+                const __grid_constant__ CUtensorMap tm_u, Dev D, int b)
 {
     using T = UpdTc<CT>;
-    constexpr int NB = T::NB;
-    constexpr int NW = TU_THREADS / 32;
-    __shared__ uint64_t s_full[TU_NS], s_empty[TU_NS], s_conv[2], s_opfree[2], s_done;
+    constexpr int NW = TV_THREADS / 32;
+    extern __shared__ __align__(1024) unsigned char smem_dyn[];
+    __shared__ uint64_t s_fulla[TV_NA], s_emptya[TV_NA], s_fullc[TV_NC], s_emptyc[TV_NC];
+    __shared__ uint64_t s_conv[TV_NOB], s_opfree[TV_NOB], s_segdone[2], s_dfree[2];
     __shared__ uint32_t s_tmem;
-    __shared__ int s_err, s_nact, s_wcnt[NW + 1];
-    __shared__ int s_act[TU_MAXQ];
-    __shared__ double s_k0[CT];
-    __shared__ double s_k0p[TU_CONV];
-    __shared__ double s_rsw[8][CT];
-    unsigned char *raw0 = base;
+    __shared__ int s_err, s_wcnt[NW];
+    __shared__ int s_act[TV_MAXQ];
+    __shared__ UnitPlan s_plan;
+    __shared__ double s_k0p[128], s_k0[CT];
+    __shared__ int s_bnd[TV_MAXG + 1];
+    __shared__ float s_stage[3 * CT][33];
+    unsigned char *raw0 = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
+    unsigned char *bop0 = raw0 + T::BOP0;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
-    const int tile = blockIdx.x, t0 = tile * 128;
-    const int nq = (N + TU_KC - 1) / TU_KC;
+    const int nq = (N + TV_K - 1) / TV_K;
+    const bool pd = D.blk_pd[b] != 0;
     tc::pdl_trigger();
     tc::pdl_wait();   // the draws of this subset are complete
 
-    // stages with a non-zero delta, in subset order (nq <= 256)
+    // active stages in subset order (nq <= 256), and the unit plan
     {
         bool f = false;
         if (tid < nq) {
-            const int jb = tid * TU_KC, e = min(N, jb + TU_KC);
-            if (e - jb == TU_KC) {   // full stage: four 16-byte loads
+            const int jb = tid * TV_K, e = min(N, jb + TV_K);
+            if (e - jb == TV_K) {   // full stage: four 16-byte loads
                 const uint4 *q = reinterpret_cast<const uint4 *>(D.nzflag + jb);
                 const uint4 a = q[0], bq = q[1], c2 = q[2], d2 = q[3];
                 f = ((a.x | a.y | a.z | a.w) | (bq.x | bq.y | bq.z | bq.w) | (c2.x | c2.y | c2.z | c2.w) |
@@ -85,290 +303,295 @@ __device__ __forceinline__ void update_tc_rows(const CUtensorMap *tm_codes, cons
         }
         const unsigned m = __ballot_sync(0xffffffffu, f);
         if (lane == 0) s_wcnt[warp] = __popc(m);
-        // the centring term: 256/CT threads per chain over interleaved draw CTAs, then in part order
-        constexpr int PARTS = TU_CONV / CT;
-        if (tid < TU_CONV) {
-            const int c = tid / PARTS, part = tid % PARTS;
-            const int ntl = (((N + TC_TM - 1) / TC_TM) * TC_TM * CT + 255) / 256;
-            double a = 0.0;
-            for (int q0 = part; q0 < ntl; q0 += 8 * PARTS) {
-                double v[8];
+        __syncthreads();
+        int before = 0, nact = 0;
+        for (int q = 0; q < NW; ++q) {
+            if (q < warp) before += s_wcnt[q];
+            nact += s_wcnt[q];
+        }
+        if (f) s_act[before + __popc(m & ((1u << lane) - 1u))] = tid;
+        __syncthreads();
+        if (warp == 0) {
+            // ra tile a (<= 64 of them, two per lane): its first active stage (upper triangular: rows
+            // 256a .. meet positions from 256a on, stages >= 4a) and an exclusive scan of its units
+            UnitPlan &P = s_plan;
+            const int nra = (N + TV_N - 1) / TV_N;
+            int cnt[2], qs[2];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int q = q0 + u * PARTS;
-                    v[u] = q < ntl ? D.k0part[(size_t)q * CT + c] : 0.0;
+            for (int h = 0; h < 2; ++h) {
+                const int a = 2 * lane + h;
+                int lo = 0, hi = nact;
+                if (pd) {
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (s_act[mid] < 4 * a) lo = mid + 1;
+                        else hi = mid;
+                    }
                 }
-#pragma unroll
-                for (int u = 0; u < 8; ++u) a += v[u];
+                qs[h] = lo;
+                cnt[h] = a < nra ? 3 * (nact - lo) : 0;
             }
-            s_k0p[tid] = a;
+            const int pair = cnt[0] + cnt[1];
+            int incl = pair;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int excl = incl - pair;
+            if (2 * lane < TV_MAXRA) {
+                P.qs[2 * lane] = qs[0];
+                P.pref[2 * lane] = excl;
+                P.qs[2 * lane + 1] = qs[1];
+                P.pref[2 * lane + 1] = excl + cnt[0];
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            if (lane == 0) {
+                P.nact = nact;
+                P.nvt = D.nvt;
+                P.nra = nra;
+                P.R = P.nvt * nact;
+                P.pref[TV_MAXRA] = total;
+                P.pref[nra] = total;
+                P.W = P.R + total;
+                s_err = 0;
+            }
         }
         __syncthreads();
+    }
+    const UnitPlan &P = s_plan;
+    const int G = gridDim.x;
+    for (int q = tid; q <= G; q += TV_THREADS) s_bnd[q] = split_bound(P, q, G);
+    __syncthreads();
+    const int u_begin = s_bnd[blockIdx.x], u_end = s_bnd[blockIdx.x + 1];
+    const int nu = u_end - u_begin;
+    // the centring term (epilogue warps, before their first segment)
+    if (warp >= TV_WARP_EPI) update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);
+    if (nu > 0) {
         if (tid == 0) {
-            int acc = 0;
-            for (int q = 0; q < NW; ++q) {
-                const int t = s_wcnt[q];
-                s_wcnt[q] = acc;
-                acc += t;
+            for (int i = 0; i < TV_NA; ++i) {
+                tc::mbar_init(&s_fulla[i], 1);
+                tc::mbar_init(&s_emptya[i], 1);   // the MMAs reading the tile
             }
-            s_nact = acc;
+            for (int i = 0; i < TV_NC; ++i) {
+                tc::mbar_init(&s_fullc[i], 1);
+                tc::mbar_init(&s_emptyc[i], TV_CONV);   // the converters
+            }
+            for (int i = 0; i < TV_NOB; ++i) {
+                tc::mbar_init(&s_conv[i], TV_CONV);
+                tc::mbar_init(&s_opfree[i], 1);
+            }
+            for (int i = 0; i < 2; ++i) {
+                tc::mbar_init(&s_segdone[i], 1);
+                tc::mbar_init(&s_dfree[i], 1);
+            }
+            tc::mbar_fence_init();
         }
-        if (tid < CT) {
-            double t = 0.0;
-            for (int q = 0; q < PARTS; ++q) t += s_k0p[tid * PARTS + q];
-            s_k0[tid] = t;
-        }
+        if (warp == TV_WARP_MMA) tc::tmem_alloc(&s_tmem, 512);   // two accumulators of 256 columns
+        tc::fence_before_sync();
         __syncthreads();
-        if (f) s_act[s_wcnt[warp] + __popc(m & ((1u << lane) - 1u))] = tid;
-        __syncthreads();
-    }
-    const int nact = s_nact;
-    if (nact == 0) return;   // nothing changed: r, r32 and rsum stay valid
-
-    if (tid == 0) {
-        for (int i = 0; i < TU_NS; ++i) {
-            tc::mbar_init(&s_full[i], 1);
-            tc::mbar_init(&s_empty[i], TU_CONV + 1);   // converters + the MMAs reading the delta split
-        }
-        for (int i = 0; i < 2; ++i) {
-            tc::mbar_init(&s_conv[i], TU_CONV);
-            tc::mbar_init(&s_opfree[i], 1);
-        }
-        tc::mbar_init(&s_done, 1);
-        tc::mbar_fence_init();
-        s_err = 0;
-    }
-    if (warp == TU_WARP_MMA) tc::tmem_alloc(&s_tmem, 128);   // accumulator 0-63, codes operand 64-127
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tm = s_tmem;
-
-    if (warp == TU_WARP_TMA) {
-        if (lane == 0) {
-            tc::tma_prefetch_desc(tm_codes);
-            tc::tma_prefetch_desc(tm_d);
-            for (int s = 0; s < nact; ++s) {
-                const int buf = s % TU_NS;
-                if (s >= TU_NS && !tc::mbar_wait(&s_empty[buf], ((s / TU_NS) - 1) & 1)) {
-                    s_err = 1;
-                    break;
-                }
-                unsigned char *rw = raw0 + (size_t)buf * T::RAW;
-                const int k0 = s_act[s] * TU_KC;
-                tc::mbar_expect_tx(&s_full[buf], T::RAW);
-                tc::tma_load_2d(rw, tm_codes, t0, ls + k0, &s_full[buf]);
-                tc::tma_load_2d(rw + T::RAW_A, tm_d, k0, 0, &s_full[buf]);
-            }
-        }
-    } else if (warp == TU_WARP_MMA) {
-        if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16(128, NB);
-            for (int s = 0; s < nact; ++s) {
-                const int ob = s & 1, buf = s % TU_NS;
-                if (!tc::mbar_wait(&s_conv[ob], (s >> 1) & 1)) {
-                    s_err = 1;
-                    break;
-                }
-                tc::fence_after_sync();
-                const uint32_t ta = tm + 64 + 32 * ob;
-                const uint32_t b0 = tc::smem_u32(raw0 + (size_t)buf * T::RAW + T::RAW_A);
-#pragma unroll
-                for (int kk = 0; kk < TU_KC / 16; ++kk)
-                    tc::mma_bf16_ta(tm, ta + 8 * kk, tc::desc_sw128(b0 + kk * 32, 1024), idesc, (s | kk) != 0 ? 1u : 0u);
-                tc::mma_commit(&s_opfree[ob]);
-                tc::mma_commit(&s_empty[buf]);
-            }
-            tc::mma_commit(&s_done);
-        }
-    } else {
-        // converters: warp w writes tensor-memory lanes 32*(w%4).. (individuals), positions 32*(w/4) ..
-        // +31 of the stage (16 columns): a thread gathers its individual's byte from 32 rows of the
-        // 128-byte-swizzled code tile (a warp reads 32 consecutive bytes of one row at a time)
-        const int ind = 32 * (warp & 3) + lane, kh = warp >> 2;
-        for (int s = 0; s < nact; ++s) {
-            const int buf = s % TU_NS, ob = s & 1;
-            bool ok = tc::mbar_wait(&s_full[buf], (s / TU_NS) & 1);
-            if (ok && s >= 2) ok = tc::mbar_wait(&s_opfree[ob], ((s - 2) >> 1) & 1);
-            if (!ok) {
-                s_err = 1;
-                break;
-            }
-            const unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
-            uint32_t v[16];
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int k = 32 * kh + 2 * j;
-                const uint32_t c0 = ra_[k * 128 + ((((ind >> 4) ^ (k & 7))) << 4) + (ind & 15)];
-                const uint32_t c1 = ra_[(k + 1) * 128 + ((((ind >> 4) ^ ((k + 1) & 7))) << 4) + (ind & 15)];
-                v[j] = tc::bf16x2_sub128(c0 | (c1 << 16) | 0x43004300u);
-            }
-            tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 32 * ob + 16 * kh, v);
-            tc::tmem_wait_st();
-            tc::fence_before_sync();
-            tc::mbar_arrive(&s_conv[ob]);
-            tc::mbar_arrive(&s_empty[buf]);
-        }
-        if (!tc::mbar_wait(&s_done, 0)) s_err = 1;
-    }
-    __syncthreads();
-    const bool ok = !s_err;
-    if (!ok && tid == 0) flag_err(D, 4);
-    tc::fence_after_sync();
-    // epilogue: warps w and w+4 read the same 32 accumulator rows, each for half of the chains
-    constexpr int HALF = CT >= 8 ? CT / 2 : CT;
-    const int h = warp >> 2;
-    if (warp < 8 && h * HALF < CT) {
-        const int i = t0 + (warp & 3) * 32 + lane;
-        const bool row_ok = i < D.n;
-        double rv[HALF];
-#pragma unroll
-        for (int c = 0; c < HALF; ++c) rv[c] = row_ok ? D.r[(size_t)(h * HALF + c) * D.ldr + i] : 0.0;
-#pragma unroll
-        for (int g = 0; g < (HALF + 7) / 8; ++g) {
-            // chains h*HALF + 8g ..: their hi, mid and lo accumulator columns
-            float hi[8], md[8], lo[8];
-            const uint32_t ta = tm + ((uint32_t)((warp & 3) * 32) << 16) + h * HALF + 8 * g;
-            tc::tmem_ld8(ta, hi);
-            tc::tmem_ld8(ta + CT, md);
-            tc::tmem_ld8(ta + 2 * CT, lo);
-            tc::tmem_wait_ld();
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int cl = 8 * g + e;
-                if (cl < HALF && ok && row_ok) rv[cl] += (double)((hi[e] + md[e]) + lo[e]) + s_k0[h * HALF + cl];
-            }
-        }
-        if (ok && row_ok) {
-#pragma unroll
-            for (int c = 0; c < HALF; ++c) store_r(D, h * HALF + c, i, rv[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < HALF; ++c) {
-            const double v = warp_sum(rv[c]);
-            if (lane == 0) s_rsw[warp][c] = v;
-        }
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    if (warp == TU_WARP_MMA) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tm, 128);
-    }
-    // this tile's partial sum of r (the centring of the next subset)
-    if (tid < CT) {
-        const int hh = tid / HALF, cl = tid % HALF;
-        D.rsum[(size_t)tid * D.nr_ctas + tile] =
-            ((s_rsw[4 * hh][cl] + s_rsw[4 * hh + 1][cl]) + s_rsw[4 * hh + 2][cl]) + s_rsw[4 * hh + 3][cl];
-    }
-}
+        const uint32_t tm = s_tmem;
 
-template <int CT>
-__device__ __forceinline__ void update_tc_ra(const Dev &D, int b, unsigned char *base)
-{
-    __shared__ int s_last;
-    float *s_red = reinterpret_cast<float *>(base);   // [4 column groups][CT][128 rows]
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    tc::pdl_trigger();
-    tc::pdl_wait();   // the draws of this subset are complete
-    const int ls = D.blk_ls[b];
-    const int N = D.blk_ls[b + 1] - ls;
-    const int npad = (N + 7) & ~7;
-    // this CTA's row tile and column split (tiles get splits in proportion to their width)
-    const int idx = blockIdx.x - D.nr_ctas;
-    const int32_t *at = D.atab + (size_t)b * D.tstride;
-    const int ntr = (N + 127) / 128;
-    int tr = 0;
-    while (tr + 1 < ntr && at[tr + 1] <= idx) ++tr;
-    const int ra_split = at[tr + 1] - at[tr], sp = idx - at[tr];
-    const int i0 = tr * 128;
-    const int kbeg = D.blk_pd[b] ? min(i0, N) : 0;   // upper triangular: rows i only meet columns k >= i
-    const int ka = kbeg + (int)(((long long)(N - kbeg) * sp) / ra_split);
-    const int kb = kbeg + (int)(((long long)(N - kbeg) * (sp + 1)) / ra_split);
-    // warp w of 8: rows i0 + 64*(w&1) + 2*lane (+1), columns ka + (w>>1) + 4q; the TMA/MMA warps idle here
-    const int rh = warp & 1, cg = warp >> 1;
-    const int ii = i0 + 64 * rh + 2 * lane;
-    const bool rows_ok = ii + 2 <= npad;
-    float acc[2][CT];
-#pragma unroll
-    for (int e = 0; e < 2; ++e)
-#pragma unroll
-        for (int c = 0; c < CT; ++c) acc[e][c] = 0.0f;
-    for (int k0 = ka + cg; warp < 8 && k0 < kb; k0 += 4 * TU_UNR) {
-        float2 u[TU_UNR];
-        int kk[TU_UNR];
-#pragma unroll
-        for (int q = 0; q < TU_UNR; ++q) {
-            const int k = k0 + 4 * q;
-            kk[q] = (k < kb && D.nzflag[k]) ? k : -1;
-            u[q] = make_float2(0.f, 0.f);
-            if (kk[q] >= 0 && rows_ok) u[q] = *reinterpret_cast<const float2 *>(D.U32 + D.uoff[ls + k] + ii);
-        }
-#pragma unroll
-        for (int q = 0; q < TU_UNR; ++q) {
-            if (kk[q] < 0) continue;
-#pragma unroll
-            for (int c = 0; c < CT; c += 4) {
-                const float4 v = *reinterpret_cast<const float4 *>(D.delta32 + (size_t)kk[q] * CT + c);
-                acc[0][c] = fmaf(u[q].x, v.x, acc[0][c]);
-                acc[1][c] = fmaf(u[q].y, v.x, acc[1][c]);
-                acc[0][c + 1] = fmaf(u[q].x, v.y, acc[0][c + 1]);
-                acc[1][c + 1] = fmaf(u[q].y, v.y, acc[1][c + 1]);
-                acc[0][c + 2] = fmaf(u[q].x, v.z, acc[0][c + 2]);
-                acc[1][c + 2] = fmaf(u[q].y, v.z, acc[1][c + 2]);
-                acc[0][c + 3] = fmaf(u[q].x, v.w, acc[0][c + 3]);
-                acc[1][c + 3] = fmaf(u[q].y, v.w, acc[1][c + 3]);
+        if (warp == TV_WARP_TMA) {
+            if (lane == 0) {
+                tc::tma_prefetch_desc(&tm_codes);
+                tc::tma_prefetch_desc(&tm_d);
+                tc::tma_prefetch_desc(&tm_u);
+                int hint = 0;
+                for (int s = 0; s < nu; ++s) {
+                    const int a = s % TV_NA, cb = s % TV_NC, ob = s % TV_NOB;
+                    const Unit x = decode_unit(P, u_begin + s, hint);
+                    // the slots' previous tiles are consumed: A by the MMAs of unit s - TV_NA, the code
+                    // tile by the converters of unit s - TV_NC and, for an ra unit (whose B operand TMA
+                    // writes), B by the MMAs of unit s - TV_NOB
+                    bool ok = s < TV_NA || tc::mbar_wait(&s_emptya[a], ((s / TV_NA) - 1) & 1);
+                    if (ok && s >= TV_NC) ok = tc::mbar_wait(&s_emptyc[cb], ((s / TV_NC) - 1) & 1);
+                    if (ok && x.kind == 1 && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TV_NOB) / TV_NOB) & 1);
+                    if (!ok) {
+                        s_err = 11;
+                        break;
+                    }
+                    const int k0 = s_act[x.q] * TV_K;
+                    tc::mbar_expect_tx(&s_fulla[a], T::RAW_A);
+                    tc::tma_load_2d(raw0 + (size_t)a * T::ASTRIDE, &tm_d, k0, 0, &s_fulla[a]);
+                    if (x.kind == 0) {
+                        tc::mbar_expect_tx(&s_fullc[cb], T::RAW_C);
+                        tc::tma_load_2d(raw0 + T::C0 + (size_t)cb * T::RAW_C, &tm_codes, x.tile * TV_N, ls + k0,
+                                        &s_fullc[cb]);
+                    } else {
+                        // four boxes of 64 rows of U x 64 positions: MN atoms 8 KB apart
+                        unsigned char *bo = bop0 + (size_t)ob * T::BOP;
+                        tc::mbar_expect_tx(&s_fullc[cb], T::BOP);
+    #pragma unroll
+                        for (int h = 0; h < 4; ++h)
+                            tc::tma_load_2d(bo + h * 8192, &tm_u, x.tile * TV_N + 64 * h, x.term * D.p + ls + k0,
+                                            &s_fullc[cb]);
+                    }
+                }
+            }
+        } else if (warp == TV_WARP_MMA) {
+            if (lane == 0) {
+                const uint32_t idesc = tc::idesc_bf16_bmn(128, TV_N);
+                int hint = 0, seg = -1, pkind = -1, ptile = -1;
+                bool ok = true;
+                for (int s = 0; s < nu && ok; ++s) {
+                    const int a = s % TV_NA, ob = s % TV_NOB;
+                    const Unit x = decode_unit(P, u_begin + s, hint);
+                    const bool first = x.kind != pkind || x.tile != ptile;
+                    if (first) {
+                        if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
+                        ++seg;
+                        pkind = x.kind;
+                        ptile = x.tile;
+                        // this accumulator was last used by segment seg - 2
+                        if (seg >= 2) ok = tc::mbar_wait(&s_dfree[seg & 1], ((seg - 2) >> 1) & 1);
+                        if (!ok) s_err = 17;
+                    }
+                    if (ok) {
+                        ok = tc::mbar_wait(&s_conv[ob], (s / TV_NOB) & 1);
+                        if (!ok) s_err = 12;
+                    }
+                    if (ok) {
+                        ok = tc::mbar_wait(&s_fulla[a], (s / TV_NA) & 1);
+                        if (!ok) s_err = 18;
+                    }
+                    if (!ok) {
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const uint32_t a0 = tc::smem_u32(raw0 + (size_t)a * T::ASTRIDE);
+                    const uint32_t b0 = tc::smem_u32(bop0 + (size_t)ob * T::BOP);
+                    const uint32_t dt = tm + 256 * (seg & 1);
+    #pragma unroll
+                    for (int kk = 0; kk < TV_K / 16; ++kk) {
+                        // codes operand: K groups of four atoms (4096 bytes), atoms 1024 apart;
+                        // U operand: atoms of eight K groups (8192 bytes), K groups 1024 apart
+                        const uint64_t bd = x.kind == 0 ? tc::desc_sw128_mn(b0 + kk * 8192, 1024, 4096)
+                                                        : tc::desc_sw128_mn(b0 + kk * 2048, 8192, 1024);
+                        tc::mma_bf16(dt, tc::desc_sw128(a0 + kk * 32, 1024), bd, idesc, (first && kk == 0) ? 0u : 1u);
+                    }
+                    tc::mma_commit(&s_opfree[ob]);
+                    tc::mma_commit(&s_emptya[a]);
+                }
+                if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
+            }
+        } else if (warp < TV_WARP_TMA) {
+            // converters: 16-byte chunk (position k, individuals 16c .. 16c+15) -> 32 bytes of bf16 in
+            // the MN-major operand: K group k/8 (4096 bytes: four atoms of 64 individuals), row k%8,
+            // chunks 2(c%4), 2(c%4)+1 of atom c/4, XOR-swizzled by the row
+            int hint = 0;
+            for (int s = 0; s < nu; ++s) {
+                const int cb = s % TV_NC, ob = s % TV_NOB;
+                const Unit x = decode_unit(P, u_begin + s, hint);
+                bool ok = tc::mbar_wait(&s_fullc[cb], (s / TV_NC) & 1);
+                if (x.kind == 0) {
+                    if (ok && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TV_NOB) / TV_NOB) & 1);
+                    if (!ok) {
+                        s_err = 13;
+                        break;
+                    }
+                    const unsigned char *rc = raw0 + T::C0 + (size_t)cb * T::RAW_C;
+                    unsigned char *bo = bop0 + (size_t)ob * T::BOP;
+    #pragma unroll
+                    for (int h4 = 0; h4 < 4; ++h4) {
+                        const int q = tid + TV_CONV * h4, k = q >> 4, c = q & 15;
+                        const uint4 w = *reinterpret_cast<const uint4 *>(rc + k * TV_N + 16 * c);
+                        uint32_t o[8];
+                        tc::codes_to_bf16x4(w.x, o[0], o[1]);
+                        tc::codes_to_bf16x4(w.y, o[2], o[3]);
+                        tc::codes_to_bf16x4(w.z, o[4], o[5]);
+                        tc::codes_to_bf16x4(w.w, o[6], o[7]);
+                        const int r = k & 7, j0 = 2 * (c & 3);
+                        unsigned char *ob_ = bo + (k >> 3) * 4096 + (c >> 2) * 1024 + r * 128;
+                        *reinterpret_cast<uint4 *>(ob_ + ((j0 ^ r) << 4)) = make_uint4(o[0], o[1], o[2], o[3]);
+                        *reinterpret_cast<uint4 *>(ob_ + (((j0 + 1) ^ r) << 4)) = make_uint4(o[4], o[5], o[6], o[7]);
+                    }
+                    tc::fence_async_smem();
+                } else if (!ok) {
+                    s_err = 14;
+                    break;
+                }
+                tc::mbar_arrive(&s_emptyc[cb]);
+                tc::mbar_arrive(&s_conv[ob]);
+            }
+        } else {
+            // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. (accumulator
+            // rows) for all 256 columns and stores rows < 3 * chains to the segment's slot of vpart
+            const int qd = warp & 3, row = 32 * qd + lane;
+            int hint = 0, seg = -1, pkind = -1, ptile = -1;
+            for (int s = 0; s <= nu; ++s) {
+                Unit x;
+                x.kind = -2;
+                x.tile = -2;
+                if (s < nu) x = decode_unit(P, u_begin + s, hint);
+                if (s < nu && x.kind == pkind && x.tile == ptile) continue;
+                if (seg >= 0) {
+                    // segment seg (pkind, ptile) is complete once its MMAs are
+                    const bool ok = tc::mbar_wait(&s_segdone[seg & 1], (seg >> 1) & 1);
+                    if (!ok) s_err = 15;
+                    tc::fence_after_sync();
+                    const int tg = pkind == 0 ? ptile : P.nvt + ptile;
+                    // per 32 columns: rows to shared memory, then hi + mid + lo per chain to the slot
+                    float *dst = D.vpart + (size_t)(tg + blockIdx.x) * CT * TV_N;
+                    const int t = tid - 32 * TV_WARP_EPI;
+                    const uint32_t ta = tm + 256 * (seg & 1) + ((uint32_t)(32 * qd) << 16);
+    #pragma unroll 1
+                    for (int j = 0; j < TV_N / 32; ++j) {
+                        if (ok && 32 * qd < T::ROWS) {
+                            float v0[8], v1[8], v2[8], v3[8];
+                            tc::tmem_ld8(ta + 32 * j, v0);
+                            tc::tmem_ld8(ta + 32 * j + 8, v1);
+                            tc::tmem_ld8(ta + 32 * j + 16, v2);
+                            tc::tmem_ld8(ta + 32 * j + 24, v3);
+                            tc::tmem_wait_ld();
+                            if (row < T::ROWS) {
+    #pragma unroll
+                                for (int e = 0; e < 8; ++e) {
+                                    s_stage[row][e] = v0[e];
+                                    s_stage[row][8 + e] = v1[e];
+                                    s_stage[row][16 + e] = v2[e];
+                                    s_stage[row][24 + e] = v3[e];
+                                }
+                            }
+                        }
+                        asm volatile("bar.sync 1, 128;" ::: "memory");
+                        for (int idx = t; idx < CT * 32; idx += 128) {
+                            const int cc = idx >> 5, col = idx & 31;
+                            dst[cc * TV_N + 32 * j + col] =
+                                (s_stage[cc][col] + s_stage[CT + cc][col]) + s_stage[2 * CT + cc][col];
+                        }
+                        asm volatile("bar.sync 1, 128;" ::: "memory");
+                    }
+                    __threadfence();   // the slot is read after the grid barrier
+                    tc::fence_before_sync();
+                    asm volatile("bar.sync 1, 128;" ::: "memory");
+                    if (warp == TV_WARP_EPI && lane == 0) tc::mbar_arrive(&s_dfree[seg & 1]);
+                }
+                if (s == nu) break;
+                ++seg;
+                pkind = x.kind;
+                ptile = x.tile;
             }
         }
-    }
-    if (warp < 8) {
-#pragma unroll
-        for (int c = 0; c < CT; ++c) {
-            s_red[(cg * CT + c) * 128 + 64 * rh + 2 * lane] = acc[0][c];
-            s_red[(cg * CT + c) * 128 + 64 * rh + 2 * lane + 1] = acc[1][c];
+        __syncthreads();
+        if (warp == TV_WARP_MMA) {
+            tc::fence_after_sync();
+            tc::tmem_dealloc(tm, 512);
         }
+    }   // nu > 0
+    // every segment is in vpart once all CTAs are here; then the reductions, an equal share of the
+    // (half tile, chain) pairs per CTA, one pair per warp at a time
+    if (!update_grid_sync(D.ugrid, (unsigned)G)) s_err = 16;
+    if (s_err) {
+        if (tid == 0) flag_err(D, s_err);
+        return;
     }
-    __syncthreads();
-    float *part = D.rapart + ((size_t)idx * CT) * 128;
-    for (int t = tid; t < CT * 128; t += TU_THREADS) {
-        const int c = t >> 7, rl = t & 127;
-        part[c * 128 + rl] = ((s_red[(0 * CT + c) * 128 + rl] + s_red[(1 * CT + c) * 128 + rl]) +
-                              s_red[(2 * CT + c) * 128 + rl]) + s_red[(3 * CT + c) * 128 + rl];
+    const int npair = 2 * (P.nvt + P.nra) * CT;
+    for (int pr = blockIdx.x * NW + warp; pr < npair; pr += G * NW) {
+        const int hh = pr / CT, c = pr - hh * CT;
+        update_reduce_pair<CT>(D, P, s_bnd, G, hh >> 1, hh & 1, c, s_k0, N);
     }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&D.raticket[tr], 1) == ra_split - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    // the last CTA of the row tile: split partial sums in split order
-    const float *p0 = D.rapart + ((size_t)at[tr] * CT) * 128;
-    for (int t = tid; t < CT * 128; t += TU_THREADS) {
-        const int c = t >> 7, rl = t & 127, i = i0 + rl;
-        if (i >= D.bs) continue;
-        float sum = 0.0f;
-        for (int q0 = 0; q0 < ra_split; q0 += 8) {
-            float pv[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                pv[q] = q0 + q < ra_split ? __ldcg(p0 + ((size_t)(q0 + q) * CT + c) * 128 + rl) : 0.0f;
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (q0 + q < ra_split) sum += pv[q];
-        }
-        store_ra(D, c, i, D.ra[(size_t)c * D.ldra + i] + (double)sum);
-    }
-    if (tid == 0) D.raticket[tr] = 0;
-}
-
-template <int CT>
-__global__ void __launch_bounds__(TU_THREADS, 2)
-    k_update_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_d, Dev D, int b)
-{
-    extern __shared__ __align__(1024) unsigned char smem_dyn[];
-    unsigned char *base = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
-    if ((int)blockIdx.x < D.nr_ctas) update_tc_rows<CT>(&tm_codes, &tm_d, D, b, base);
-    else update_tc_ra<CT>(D, b, base);
 }
 
 }  // namespace soda
