@@ -68,6 +68,16 @@ __host__ __device__ inline int rhs_tc_stages(int nG, int N, int mt, bool pd, int
     return nG + 3 * q;
 }
 
+// First stage of K split ks of ksplit over a tile's T stages (nG genotype
+// stages of weight 2, then U stages of weight 1), in equal shares of weight.
+__host__ __device__ inline int rhs_tc_split(int nG, int T, int ks, int ksplit)
+{
+    const long long wt = 2LL * nG + (T - nG);
+    const long long x = (wt * ks) / ksplit;
+    if (x <= 2LL * nG) return (int)((x + 1) / 2);
+    return nG + (int)(x - 2LL * nG);
+}
+
 template <int CT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_rhs_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_rsp,
@@ -84,7 +94,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
-    // this CTA's SNP tile and K split (tiles get splits in proportion to their stages)
+    // this CTA's SNP tile and K split: tiles get splits in proportion to their MMAs, and a tile's
+    // stages are split in equal shares of MMA work (a genotype stage has twice the MMAs of a U stage)
     const int32_t *rt = D.rtab + (size_t)b * D.tstride;
     const int mtiles = (N + TC_TM - 1) / TC_TM;
     int mt = 0;
@@ -94,7 +105,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (j0 >= N || ks >= ksplit) return;
     const int nG = D.ldx / TC_KC;
     const int T_ = rhs_tc_stages(nG, N, mt, D.blk_pd[b] != 0, nullptr);
-    const int t0 = (int)(((long long)T_ * ks) / ksplit), t1 = (int)(((long long)T_ * (ks + 1)) / ksplit);
+    const int t0 = rhs_tc_split(nG, T_, ks, ksplit), t1 = rhs_tc_split(nG, T_, ks + 1, ksplit);
     const int ns = t1 - t0;                              // stages of this CTA
     const int nck = max(0, min(t1, nG) - t0);            // of which genotype stages (first)
 

@@ -19,6 +19,7 @@
 #include "sweep.cuh"
 #include "tc.cuh"
 #include <algorithm>
+#include <vector>
 
 namespace soda {
 
@@ -1110,16 +1111,41 @@ void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count
     for (int b = 0; b < nb; ++b) {
         const int N = blk_sizes[b], tiles = (N + TC_TM - 1) / TC_TM;
         int32_t *rt = rtab + (size_t)b * stride;
-        // rhs: weight of tile m = its pipeline stages (genotype and U stages alike)
+        // K splits in proportion to each tile's MMAs (8 per genotype stage, 4 per U stage), largest
+        // remainders first, so that the CTAs (one per SM, all of them) get equal MMA work
+        std::vector<long long> w(tiles);
+        std::vector<int> ks(tiles), cap(tiles);
         long long W = 0;
-        for (int m = 0; m < tiles; ++m) W += rhs_tc_stages(nst, N, m, true, nullptr);
+        for (int m = 0; m < tiles; ++m) {
+            const int T = rhs_tc_stages(nst, N, m, true, nullptr);
+            w[m] = 8LL * nst + 4LL * (T - nst);
+            cap[m] = std::min(RHS_KSPLIT_MAX, T);
+            W += w[m];
+        }
+        int total = 0;
+        for (int m = 0; m < tiles; ++m) {
+            ks[m] = std::max(1, std::min(cap[m], (int)(((long long)sm_count * w[m]) / W)));
+            total += ks[m];
+        }
+        while (total < sm_count) {
+            int best = -1;
+            double bf = -1.0;
+            for (int m = 0; m < tiles; ++m) {
+                if (ks[m] >= cap[m]) continue;
+                const double f = (double)sm_count * (double)w[m] / (double)W - ks[m];
+                if (f > bf) {
+                    bf = f;
+                    best = m;
+                }
+            }
+            if (best < 0) break;
+            ++ks[best];
+            ++total;
+        }
         int acc = 0;
         for (int m = 0; m < tiles; ++m) {
-            const long long w = rhs_tc_stages(nst, N, m, true, nullptr);
-            int ks = (int)(((long long)sm_count * w) / W);
-            ks = std::max(1, std::min(ks, std::min(RHS_KSPLIT_MAX, nst)));
             rt[m] = acc;
-            acc += ks;
+            acc += ks[m];
         }
         rt[tiles] = acc;
     }
