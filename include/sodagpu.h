@@ -57,6 +57,13 @@ enum sodagpu_precision { SODAGPU_FP64 = 0, SODAGPU_FP32 = 1, SODAGPU_FP8 = 2 };
    on the FP32/FP64 cores.  Results agree to rounding. */
 enum sodagpu_kernels { SODAGPU_KERNELS_AUTO = 0, SODAGPU_KERNELS_CUDA_CORES = 1 };
 
+/* Sampler.  SODA is soda_bayes (models.f90:9-605): subsets drawn in parallel
+   against the augmented data.  REGULAR is regular_bayes (models.f90:607-962,
+   the -SODAOff path, SODABayes.f90:137): single-site Gibbs over the SNPs in
+   order, no augmenting matrix; it needs no sodagpu_build_z factorisation (the
+   call only lays out the genotypes) and always runs in FP64. */
+enum sodagpu_sampler { SODAGPU_SAMPLER_SODA = 0, SODAGPU_SAMPLER_REGULAR = 1 };
+
 /* Genotype input layouts for sodagpu_load_genotypes(). */
 enum sodagpu_geno_layout {
     /* int8 codes 0/1/2, column-major nind x nloci (one SNP per column);
@@ -110,7 +117,8 @@ typedef struct sodagpu_config {
     double vara0;       /* value of the module variable `vara` on entry: the
                            df_va<=0 branch adds to it (models.f90:99-102)       */
     int32_t kernels;    /* enum sodagpu_kernels: which sweep kernels run        */
-    int32_t reserved[7];
+    int32_t sampler;    /* enum sodagpu_sampler (-SODAOn / -SODAOff)            */
+    int32_t reserved[6];
 } sodagpu_config;
 
 /* One thinned iteration of the .hyp trace (models.f90:549-569). */

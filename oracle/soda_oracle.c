@@ -17,7 +17,10 @@
  *                  378-401 (power_method), 8-47 (choleskyPD), 49-124 and
  *                  128-376 (choleskyPSD with its LAPACK helpers)
  *   sampler        models.f90:56-128 (initialisation), 129-574 (iterations),
- *                  575-594 (posterior means)
+ *                  575-594 (posterior means); the regular (-SODAOff) sampler
+ *                  models.f90:607-962 as the same iteration with every SNP
+ *                  drawn single-site in order (draw_skipped restates 717-859)
+ *                  and no augmented data
  *   products       utilities.f90:609-622 (compute_residuals, compute_dgv)
  *
  * Parity status: unpinned for the sweep and the Z build (the reference has no
@@ -231,6 +234,7 @@ typedef struct {
 struct oracle_ctx {
     sodagpu_config cfg;
     int n, p, method, nmix, ngroup, nchain, bs, nb, bt;
+    int regular;                        /* regular_bayes (models.f90:607-962) */
     int rng_mode, ref_threads;
     xo_state *xo;                       /* reference streams                   */
     int8_t *G;                          /* n*p codes                           */
@@ -278,10 +282,11 @@ int oracle_create(const sodagpu_config *cfg, int32_t rng_mode, int32_t ref_threa
                   oracle_ctx **out)
 {
     if (!cfg || !out) return SODAGPU_E_ARG;
+    const int regular = cfg->sampler == SODAGPU_SAMPLER_REGULAR;
     if (cfg->nind < 2 || cfg->nloci < 1 || cfg->method < 1 || cfg->method > 6 ||
         cfg->nmix < 1 || cfg->nmix > SODAGPU_MAXDIST || cfg->ngroup < 1 ||
-        cfg->ngroup > SODAGPU_MAXGRP || cfg->blocksize < 2 || cfg->nblocks < 1 ||
-        cfg->thin < 1 || cfg->chains < 1)
+        cfg->ngroup > SODAGPU_MAXGRP || (!regular && (cfg->blocksize < 2 || cfg->nblocks < 1)) ||
+        cfg->thin < 1 || cfg->chains < 1 || (cfg->sampler != SODAGPU_SAMPLER_SODA && !regular))
         return SODAGPU_E_ARG;
     if (rng_mode == ORACLE_RNG_REFERENCE && cfg->chains != 1) return SODAGPU_E_ARG;
     oracle_ctx *o = (oracle_ctx *)calloc(1, sizeof *o);
@@ -293,9 +298,11 @@ int oracle_create(const sodagpu_config *cfg, int32_t rng_mode, int32_t ref_threa
     o->nmix = cfg->nmix;
     o->ngroup = cfg->ngroup;
     o->nchain = cfg->chains;
-    o->bs = cfg->blocksize;
-    o->nb = cfg->nblocks;
-    o->bt = cfg->blockt;
+    /* the regular sampler has no subsets and no augmented data */
+    o->regular = regular;
+    o->bs = regular ? 1 : cfg->blocksize;
+    o->nb = regular ? 0 : cfg->nblocks;
+    o->bt = regular ? 0 : cfg->blockt;
     o->rng_mode = rng_mode;
     o->ref_threads = ref_threads < 1 ? 1 : ref_threads;
     size_t np = (size_t)o->n * o->p;
@@ -307,7 +314,7 @@ int oracle_create(const sodagpu_config *cfg, int32_t rng_mode, int32_t ref_threa
     o->grp = (int32_t *)malloc(sizeof(int32_t) * o->p);
     o->perm = (int32_t *)malloc(sizeof(int32_t) * o->p);
     o->XA = (double *)calloc((size_t)o->bs * o->p, sizeof(double));
-    o->xxd = (double *)calloc(o->nb, sizeof(double));
+    o->xxd = (double *)calloc(o->nb > 0 ? o->nb : 1, sizeof(double));
     o->skip = (uint8_t *)calloc(o->p, 1);
     o->iskipped = (int32_t *)calloc(o->p, sizeof(int32_t));
     o->xo = (xo_state *)calloc(o->ref_threads, sizeof(xo_state));
@@ -673,6 +680,23 @@ int oracle_build_z(oracle_ctx *o, const int32_t *permvec, int64_t power_maxit,
 {
     if (!o || !o->have_geno) return SODAGPU_E_STATE;
     const int bs = o->bs, p = o->p;
+    if (o->regular) {
+        /* regular_bayes: every SNP single-site, in order (permvec(i) = i, models.f90:675-678) */
+        for (int k = 0; k < p; ++k) {
+            o->perm[k] = k;
+            o->iskipped[k] = k;
+        }
+        memset(o->skip, 0, p);
+        o->nskipped = p;
+        o->naless = 1;
+        o->naind = 0;
+        o->have_z = 1;
+        if (nskipped_out) *nskipped_out = 0;
+        (void)permvec;
+        (void)power_maxit;
+        (void)d_offset;
+        return 0;
+    }
     for (int k = 0; k < p; ++k) {
         int v = permvec ? permvec[k] - 1 : k;
         if (v < 0 || v >= p) return SODAGPU_E_ARG;
@@ -1261,7 +1285,10 @@ static void iterate(oracle_ctx *o, chain_t *c, int ci, int rep, sodagpu_trace_cb
         c->counter++;
         for (int j = 0; j < p; ++j) c->gstore[j] = c->gstore[j] + c->g[j];
         c->mu_store = c->mu_store + c->mu;
-        for (int t = 0; t < ng * nm; ++t) c->varstore[t] = c->varstore[t] + c->varindist[t];
+        /* soda_bayes keeps varstore for every method (models.f90:530), regular_bayes not
+           for BayesA (models.f90:893-896) */
+        if (!(o->regular && m == SODAGPU_BAYES_A))
+            for (int t = 0; t < ng * nm; ++t) c->varstore[t] = c->varstore[t] + c->varindist[t];
         c->vare_store = c->vare_store + c->vare;
         if (m != SODAGPU_BAYES_A) {
             c->included_store = c->included_store + c->included;

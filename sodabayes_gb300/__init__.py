@@ -113,6 +113,7 @@ class JobOptions:
     recal_every: int = 1000
     vara0: float = 0.0
     kernels: str = "auto"          # "auto" (tensor cores where they apply) or "cuda_cores"
+    soda: bool = True              # -SODAOn / -SODAOff: False runs the regular sampler (models.f90:607-962)
 
 
 def make_config(nind: int, nloci: int, opts: JobOptions) -> Config:
@@ -158,8 +159,11 @@ def make_config(nind: int, nloci: int, opts: JobOptions) -> Config:
             cfg.alpha[j] = fround(v)
     cfg.numit, cfg.burnin, cfg.thin, cfg.seed = opts.numit, opts.burnin, opts.thin, opts.seed
     bs, nb, bt, off = block_layout_py(nloci, opts.nthreads, opts.blocksize, opts.nblocks)
-    if off:
-        raise ValueError("blocksize <= 1: the reference switches SODA off (soda.f90:418-421)")
+    if off or not opts.soda:
+        # -SODAOff, or blocksize <= 1 (setup_soda switches SODA off, soda.f90:418-421): the
+        # regular sampler, which has no subsets
+        cfg.sampler = 1
+        bs, nb, bt = nloci, 1, 1
     cfg.blocksize, cfg.nblocks, cfg.blockt = bs, nb, bt
     cfg.precision = PRECISIONS[opts.precision] if isinstance(opts.precision, str) else int(opts.precision)
     cfg.chains = opts.chains

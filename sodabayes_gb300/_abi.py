@@ -25,7 +25,7 @@ class Config(C.Structure):
         ("pizero", C.c_double), ("scale_va", C.c_double), ("scale_ve", C.c_double),
         ("df_va", C.c_double), ("df_ve", C.c_double),
         ("mix", C.c_double * MAXDIST), ("alpha", C.c_double * MAXDIST), ("vara0", C.c_double),
-        ("kernels", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("kernels", C.c_int32), ("sampler", C.c_int32), ("reserved", C.c_int32 * 6),
     ]
 
 

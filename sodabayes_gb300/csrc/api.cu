@@ -123,6 +123,7 @@ struct sodagpu_ctx {
     int nskipped = 0, naind = 0, nsplit = 1;
     double d_offset = 0.0;
     bool have_geno = false, have_pheno = false, have_z = false, have_chain = false;
+    bool regular = false;   // regular_bayes (models.f90:607-962): no subsets, no Z
     std::vector<void *> allocs;
     std::vector<int32_t> blk_sizes, h_blk_ls;
     // device
@@ -259,7 +260,10 @@ int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out)
     if ((cfg->method >= SODAGPU_BAYES_B && cfg->method <= SODAGPU_BAYES_CPI) && cfg->nmix != 2)
         return fail(SODAGPU_E_ARG, "BayesB/C/Cpi need nmix=2");
     if (cfg->method != SODAGPU_BAYES_RC && cfg->ngroup != 1) return fail(SODAGPU_E_ARG, "ngroup>1 needs BayesRc");
-    if (cfg->blocksize < 2 || cfg->nblocks < 1 || cfg->blockt < 0 || cfg->blockt > cfg->nblocks)
+    if (cfg->sampler != SODAGPU_SAMPLER_SODA && cfg->sampler != SODAGPU_SAMPLER_REGULAR)
+        return fail(SODAGPU_E_ARG, "sampler %d out of range", cfg->sampler);
+    const bool regular = cfg->sampler == SODAGPU_SAMPLER_REGULAR;
+    if (!regular && (cfg->blocksize < 2 || cfg->nblocks < 1 || cfg->blockt < 0 || cfg->blockt > cfg->nblocks))
         return fail(SODAGPU_E_ARG, "invalid SODA block layout");
     if (cfg->thin < 1 || cfg->numit < 0 || cfg->burnin < 0) return fail(SODAGPU_E_ARG, "bad numit/burnin/thin");
     if (cfg->precision < 0 || cfg->precision > 2) return fail(SODAGPU_E_ARG, "precision out of range");
@@ -293,9 +297,11 @@ int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out)
     }
     c->n = cfg->nind;
     c->p = cfg->nloci;
-    c->bs = cfg->blocksize;
-    c->nb = cfg->nblocks;
-    c->bt = cfg->blockt;
+    // the regular sampler has no subsets: one nominal subset of all SNPs, a small scratch size
+    c->regular = regular;
+    c->bs = regular ? 8 : cfg->blocksize;
+    c->nb = regular ? 1 : cfg->nblocks;
+    c->bt = regular ? 1 : cfg->blockt;
     c->C = cfg->chains;
     c->ldx = (int)round_up((size_t)c->n, 128);
     c->ldr = c->ldx;
@@ -303,7 +309,7 @@ int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out)
     // block bounds (models.f90:136-142), 0-based first positions
     c->h_blk_ls.resize(c->nb + 1);
     c->blk_sizes.resize(c->nb);
-    for (int b = 0; b < c->nb; ++b) {
+    for (int b = 0; b < c->nb && !regular; ++b) {
         const int blocki = b + 1;
         int ls, le;
         if (blocki <= c->bt) {
@@ -319,6 +325,10 @@ int sodagpu_create(const sodagpu_config *cfg, sodagpu_ctx **out)
         }
         c->h_blk_ls[b] = ls - 1;
         c->blk_sizes[b] = le - ls + 1;
+    }
+    if (regular) {
+        c->h_blk_ls[0] = 0;
+        c->blk_sizes[0] = c->p;
     }
     c->h_blk_ls[c->nb] = c->h_blk_ls[c->nb - 1] + c->blk_sizes[c->nb - 1];
     if (c->h_blk_ls[c->nb] != c->p) {
@@ -420,12 +430,60 @@ int sodagpu_set_d_offset(sodagpu_ctx *c, double delta)
     return 0;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The regular sampler's set-up in place of the Z build: genotypes in SNP order
+// (permvec(i) = i, models.f90:675-678), every SNP drawn single-site in order by
+// k_skipped, no augmented data.
+int regular_layout(sodagpu_ctx *c, int32_t *nskipped_out, std::chrono::steady_clock::time_point t0)
+{
+    const int p = c->p;
+    std::vector<int32_t> h_id(p);
+    for (int k = 0; k < p; ++k) h_id[k] = k;
+    TRY(c->alloc(&c->perm, p, false));
+    TRY(c->alloc(&c->pos_of, p, false));
+    TRY(c->alloc(&c->G, (size_t)p * c->ldx, false));
+    TRY(c->alloc(&c->xv, (size_t)p * 4, false));
+    TRY(c->alloc(&c->xxd, c->nb));
+    TRY(c->alloc(&c->ulen, p));
+    TRY(c->alloc(&c->uoff, p + 1));
+    TRY(c->alloc(&c->skip, p));
+    TRY(c->alloc(&c->blk_pd, c->nb));
+    TRY(c->alloc(&c->U64, 1));
+    TRY(c->alloc(&c->U32, 1));
+    TRY(c->alloc(&c->iskipped, p, false));
+    TRY(c->alloc(&c->xpx, p));
+    CUDA_TRY(cudaMemcpyAsync(c->perm, h_id.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaMemcpyAsync(c->pos_of, h_id.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaMemcpyAsync(c->iskipped, h_id.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(zb_gather(c->Gsnp, c->G, c->perm, p, c->ldx, c->st));
+    CUDA_TRY(zb_xv(c->freq, c->perm, p, c->xv, c->st));
+    TRY(c->alloc(&c->xv32, (size_t)p * 4, false));
+    CUDA_TRY(zb_xv32(c->xv, p, c->xv32, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->release(c->Gsnp);
+    c->Gsnp = nullptr;
+    c->nskipped = p;
+    c->naind = 0;
+    c->have_z = true;
+    if (nskipped_out) *nskipped_out = 0;
+    c->t_build = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
 int sodagpu_build_z(sodagpu_ctx *c, const int32_t *permvec, int32_t *nskipped_out)
 {
     if (!c) return fail(SODAGPU_E_ARG, "null argument");
     if (!c->have_geno || !c->Gsnp) return fail(SODAGPU_E_STATE, "load genotypes before sodagpu_build_z");
     if (c->have_z) return fail(SODAGPU_E_STATE, "sodagpu_build_z already ran on this context");
     const auto t0 = std::chrono::steady_clock::now();
+    if (c->regular) return regular_layout(c, nskipped_out, t0);
     const int p = c->p, n = c->n, bs = c->bs, nb = c->nb;
     std::vector<int32_t> h_perm(p), h_pos(p, -1);
     for (int k = 0; k < p; ++k) {
@@ -684,7 +742,8 @@ int build_dev(sodagpu_ctx *c)
     D.n = c->n;
     D.p = c->p;
     D.bs = c->bs;
-    D.nb = c->nb;
+    D.nb = c->regular ? 0 : c->nb;   // the regular sampler's SNPs all run through k_skipped
+    D.regular = c->regular ? 1 : 0;
     D.bt = c->bt;
     D.method = c->cfg.method;
     D.nmix = c->cfg.nmix;
@@ -799,7 +858,8 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         TRY(c->alloc(&c->recal_part, (size_t)C * RECAL_SPLIT * c->ldr));
         TRY(c->alloc(&c->rpx, (size_t)RHS_KSPLIT_MAX * C * c->bs));
         TRY(c->alloc(&c->rpu, (size_t)RHS_KSPLIT_MAX * C * c->bs));
-        c->tc = c->cfg.kernels == SODAGPU_KERNELS_AUTO && sweep_tc_supported(c->cfg.precision, C, c->bs);
+        c->tc = !c->regular && c->cfg.kernels == SODAGPU_KERNELS_AUTO &&
+                sweep_tc_supported(c->cfg.precision, C, c->bs);
         if (c->tc) {
             c->ldd = (int)round_up((size_t)c->bs, 128);
             TRY(c->alloc(&c->dsplit, (size_t)sweep_tc_rows(C) * c->ldd));

@@ -572,11 +572,15 @@ void write_log(const Job &J)
             s905("Variance of dist ", J.mix);
             s905("Dirichlet prior", J.alpha);
         }
-        std::fprintf(f, "%s\n", Record().a("SODA on").t(30).a("= ").l(true).str().c_str());
-        s903("No. of threads", J.nthreads);
-        s903("No. of blocks", J.nblocks);
-        s903("Block size", J.blocksize);
-        std::fprintf(f, "%s\n", Record().a("Random blocks").t(30).a("= ").l(J.rblocks).str().c_str());
+        if (!J.sodaoff) {   // utilities.f90:225-233
+            std::fprintf(f, "%s\n", Record().a("SODA on").t(30).a("= ").l(true).str().c_str());
+            s903("No. of threads", J.nthreads);
+            s903("No. of blocks", J.nblocks);
+            s903("Block size", J.blocksize);
+            std::fprintf(f, "%s\n", Record().a("Random blocks").t(30).a("= ").l(J.rblocks).str().c_str());
+        } else {
+            std::fprintf(f, "%s\n", Record().a("SODA off").t(30).a("= ").l(true).str().c_str());
+        }
         std::fprintf(f, "%s\n", Record().a("Seed ").t(30).a("= ").i(J.seed1, 12).str().c_str());
         s902("Prefix for output files", J.outprefix);
     } else {
@@ -688,10 +692,15 @@ int run_program(Job &J)
     } else {
         if (J.alterpheno) load_alt_pheno(J);
         if (J.seed1 == 0) J.seed1 = (long long)std::chrono::steady_clock::now().time_since_epoch().count() % 2147483647LL;
-        if (J.sodaoff) throw JobError("-SODAOff: the regular (non-SODA) sampler is not provided by this build");
         int32_t bs = 0, nb = 0, bt = 0;
-        if (sodagpu_block_layout(J.nloci, J.nthreads, J.blocksize, J.nblocks, &bs, &nb, &bt) != 0)
-            throw JobError("blocksize <= 1: SODA cannot run (soda.f90:418-421)");
+        // blocksize <= 1 switches SODA off (soda.f90:418-421); -SODAOff runs regular_bayes
+        // (SODABayes.f90:136-137)
+        if (sodagpu_block_layout(J.nloci, J.nthreads, J.blocksize, J.nblocks, &bs, &nb, &bt) != 0) J.sodaoff = true;
+        if (J.sodaoff) {
+            bs = J.nloci;
+            nb = 1;
+            bt = 1;
+        }
         J.blocksize = bs;
         J.nblocks = nb;
         J.blockt = bt;
@@ -708,6 +717,7 @@ int run_program(Job &J)
         cfg.burnin = (int32_t)J.burnin;
         cfg.thin = (int32_t)J.thin;
         cfg.precision = J.precision;
+        cfg.sampler = J.sodaoff ? SODAGPU_SAMPLER_REGULAR : SODAGPU_SAMPLER_SODA;
         cfg.chains = 1;
         cfg.recal_every = 1000;
         cfg.seed = std::llabs(J.seed1);

@@ -61,6 +61,7 @@ struct Dev {
     int nskipped, naind;
     int nr_ctas;               // row tiles (ROW_TILE rows) of the residual kernels
     int recal;
+    int regular;               // 1: regular_bayes (every SNP single-site, no augmented data)
     int burnin, thin;
     uint64_t seed;
     double pizero, scale_ve, df_va, df_ve;

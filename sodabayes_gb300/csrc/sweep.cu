@@ -412,114 +412,185 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
 namespace soda {
 
 // ---------------------------------------------------------------------------
-// skipped SNPs (pivoted fallback only), one CTA per chain, SNPs in order.
-// The reference reads module copies of log_p / vare_gp here that its parallel
-// regions never assign; the current values are used.
+// Single-site updates, one CTA per chain, SNPs in order: the SNPs the pivoted
+// fallback skips (models.f90:178-193, 276-320, 433-495) and, for the regular
+// sampler, every SNP (regular_bayes, models.f90:717-859).  The residual is
+// held in shared memory when it fits (each thread owns the same individuals
+// in the dot product and in the update, so only the reduction and the draw
+// need barriers); the mixture-class scores and the exponentials of their
+// differences are computed by parallel lanes of warp 0 and added by lane 0 in
+// the reference's order.  The reference reads module copies of log_p /
+// vare_gp for skipped SNPs that its parallel regions never assign; the
+// current values are used.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_skipped(Dev D)
+constexpr int SS_THREADS = 512;
+constexpr int SS_SMEM_MAX = 200 * 1024;   // residual in shared memory up to 25,600 individuals
+
+// Lane 0 returns the update delta = g_old - g_new of SNP snploc of chain c
+// (its new effect, class and locus variance written); all 32 lanes enter.
+__device__ __forceinline__ double single_site_draw(const Dev &D, ChainScal *S, int c, int rep, int snploc, double dot)
 {
-    __shared__ double sh[33];
-    __shared__ double s_d;
+    const int lane = threadIdx.x & 31;
+    const size_t o = (size_t)c * D.p + snploc;
+    const double vare = S->vare, zz = D.xpx[snploc], zz_vare = zz / vare;
+    const int m = D.method, ng = D.ngroup, nm = D.nmix;
+    double rhs = dot, upd = 0.0;
+    int err = 0;
+    if (m != SODAGPU_BAYES_A && m != SODAGPU_BAYES_B) {
+        // BayesC/Cpi/R/Rc: scores by lanes 0..nm-1, exponentials of their differences by lanes (kk, j)
+        const double gk = D.g[o];
+        const int cl = D.cls[o];
+        if (cl > 1) rhs = rhs + zz * gk;
+        const int sg = D.grp[snploc] - 1;
+        double sv = 0.0;
+        if (lane == 0) sv = S->log_p[sg];
+        else if (lane < nm) {
+            const double logdetV = log(S->gp[lane] * zz_vare + 1.0);
+            const double uhat = rhs / (zz + S->vare_gp[lane]);
+            sv = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[sg + lane * ng];
+        }
+        const bool par = nm * nm <= 32;
+        const int kq = lane / (nm > 0 ? nm : 1), jq = lane % (nm > 0 ? nm : 1);
+        const double skq = __shfl_sync(0xffffffffu, sv, par ? kq : 0);
+        const double sjq = __shfl_sync(0xffffffffu, sv, par ? jq : 0);
+        double ev = 0.0;
+        if (par && lane < nm * nm && kq != jq) {
+            const double clike = sjq - skq;
+            if (clike >= -700 && clike <= 700) ev = exp(clike);
+        }
+        double s[MAXDIST];
+        double e[MAXDIST * MAXDIST > 32 ? 32 : MAXDIST * MAXDIST];
+#pragma unroll
+        for (int t = 0; t < MAXDIST; ++t) s[t] = __shfl_sync(0xffffffffu, sv, t < 32 ? t : 0);
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+            const double v = __shfl_sync(0xffffffffu, ev, t);
+            if (t < (int)(sizeof(e) / sizeof(e[0]))) e[t] = v;
+        }
+        if (lane == 0) {
+            CRng R;
+            crng_init(R, D.seed, c, rep, snploc, P_SKIP);
+            const double u = crng_unit(R);
+            double ssculm = 0.0;
+            int flag = 1;
+            for (int kk = 0; kk < nm; ++kk) {
+                const double skk = s[kk];
+                double sk = 0.0;
+                bool overflow = false;
+                for (int j = 0; j < nm; ++j) {
+                    if (j == kk) continue;
+                    const double clike = s[j] - skk;
+                    if (clike < -700) continue;
+                    if (clike > 700) { overflow = true; break; }
+                    sk = sk + (par ? e[kk * nm + j] : exp(clike));
+                }
+                ssculm = ssculm + (overflow ? 0.0 : 1.0 / (1.0 + sk));
+                if (u < ssculm) { flag = kk + 1; break; }
+            }
+            double gt = 0.0;
+            if (flag == 1) {
+                upd = cl > 1 ? gk : 0.0;
+            } else {
+                const double v1 = zz + vare / S->gp[flag - 1];
+                gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+                upd = gk - gt;
+            }
+            D.g[o] = gt;
+            D.cls[o] = flag;
+        }
+        return upd;
+    }
+    if (lane == 0) {
+        const double gk = D.g[o];
+        double gt = 0.0;
+        CRng R;
+        crng_init(R, D.seed, c, rep, snploc, P_SKIP);
+        if (m == SODAGPU_BAYES_A) {
+            rhs = rhs + zz * gk;
+            const double v1 = zz + vare / D.vara_s[o];
+            gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+            upd = gk - gt;
+            D.g[o] = gt;
+        } else {
+            if (D.cls[o] > 1) rhs = rhs + zz * gk;
+            const double vs = D.vara_s[o];
+            const double s1 = S->log_p[0];
+            const double logdetV = log(vs * zz_vare + 1.0);
+            const double uhat = rhs / (zz + vare / vs);
+            const double s2 = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[ng];
+            const double clike = s1 - s2;
+            double sk;
+            if (clike > 700) sk = 0.0;
+            else if (clike < -700) sk = 1.0;
+            else sk = 1.0 / (1.0 + exp(clike));
+            const double u = crng_unit(R);
+            const int flag = u < sk ? 2 : 1;
+            if (flag == 1) {
+                gt = d_rnorm(0.0, sqrt(vs), R);
+                upd = D.cls[o] > 1 ? gk : 0.0;
+                D.g[o] = 0.0;
+            } else {
+                const double v1 = zz + vare / vs;
+                gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
+                upd = gk - gt;
+                D.g[o] = gt;
+            }
+            D.cls[o] = flag;
+        }
+        const double scale = (gt * gt + S->scale_va * D.df_va) / (D.df_va + 1.0);
+        D.vara_s[o] = d_rscinvchi2(D.df_va + 1.0, scale, R, &err);
+        if (err) flag_err(D, 1);
+    }
+    return upd;
+}
+
+__global__ void __launch_bounds__(SS_THREADS) k_skipped(Dev D)
+{
+    extern __shared__ double s_r[];
+    __shared__ double s_part[SS_THREADS / 32];
+    __shared__ double s_upd;
     const int c = blockIdx.x, rep = cur_rep(D);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     ChainScal *S = &D.scal[c];
-    double *r = D.r + (size_t)c * D.ldr;
+    double *rg = D.r + (size_t)c * D.ldr;
+    const bool in_smem = (size_t)D.n * sizeof(double) <= (size_t)SS_SMEM_MAX;
+    double *r = in_smem ? s_r : rg;
+    if (in_smem) {
+        for (int i = tid; i < D.n; i += SS_THREADS) s_r[i] = rg[i];
+        __syncthreads();
+    }
     for (int t = 0; t < D.nskipped; ++t) {
         const int snploc = D.iskipped[t];
         const int k = D.pos_of[snploc];
         const int8_t *col = D.G + (size_t)k * D.ldx;
         const double *xv = D.xv + (size_t)k * 4;
+        const double x0 = xv[0], x1 = xv[1], x2 = xv[2];
         double part = 0.0;
-        for (int i = threadIdx.x; i < D.n; i += blockDim.x) part += r[i] * xv[col[i]];
-        const double dot = block_sum(part, sh);
-        if (threadIdx.x == 0) {
-            const size_t o = (size_t)c * D.p + snploc;
-            const double vare = S->vare, zz = D.xpx[snploc], zz_vare = zz / vare;
-            double gk = D.g[o], gt = 0.0, rhs = dot, upd = 0.0;
-            CRng R;
-            crng_init(R, D.seed, c, rep, snploc, P_SKIP);
-            int err = 0;
-            const int m = D.method, ng = D.ngroup, nm = D.nmix;
-            if (m == SODAGPU_BAYES_A) {
-                rhs = rhs + zz * gk;
-                const double v1 = zz + vare / D.vara_s[o];
-                gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
-                upd = gk - gt;
-                D.g[o] = gt;
-                const double scale = (gt * gt + S->scale_va * D.df_va) / (D.df_va + 1.0);
-                D.vara_s[o] = d_rscinvchi2(D.df_va + 1.0, scale, R, &err);
-            } else if (m == SODAGPU_BAYES_B) {
-                if (D.cls[o] > 1) rhs = rhs + zz * gk;
-                const double vs = D.vara_s[o];
-                const double s1 = S->log_p[0];
-                const double logdetV = log(vs * zz_vare + 1.0);
-                const double uhat = rhs / (zz + vare / vs);
-                const double s2 = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[ng];
-                const double clike = s1 - s2;
-                double sk;
-                if (clike > 700) sk = 0.0;
-                else if (clike < -700) sk = 1.0;
-                else sk = 1.0 / (1.0 + exp(clike));
-                const double u = crng_unit(R);
-                const int flag = u < sk ? 2 : 1;
-                if (flag == 1) {
-                    gt = d_rnorm(0.0, sqrt(vs), R);
-                    upd = D.cls[o] > 1 ? gk : 0.0;
-                    D.g[o] = 0.0;
-                } else {
-                    const double v1 = zz + vare / vs;
-                    gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
-                    upd = gk - gt;
-                    D.g[o] = gt;
-                }
-                D.cls[o] = flag;
-                const double scale = (gt * gt + S->scale_va * D.df_va) / (D.df_va + 1.0);
-                D.vara_s[o] = d_rscinvchi2(D.df_va + 1.0, scale, R, &err);
-            } else {
-                if (D.cls[o] > 1) rhs = rhs + zz * gk;
-                const int sg = D.grp[snploc] - 1;
-                double s[MAXDIST];
-                s[0] = S->log_p[sg];
-                for (int kk = 1; kk < nm; ++kk) {
-                    const double logdetV = log(S->gp[kk] * zz_vare + 1.0);
-                    const double uhat = rhs / (zz + S->vare_gp[kk]);
-                    s[kk] = -0.5 * (logdetV - (rhs * uhat / vare)) + S->log_p[sg + kk * ng];
-                }
-                const double u = crng_unit(R);
-                double ssculm = 0.0;
-                int flag = 1;
-                for (int kk = 0; kk < nm; ++kk) {
-                    const double skk = s[kk];
-                    double sk = 0.0;
-                    bool overflow = false;
-                    for (int j = 0; j < nm; ++j) {
-                        if (j == kk) continue;
-                        const double clike = s[j] - skk;
-                        if (clike < -700) continue;
-                        if (clike > 700) { overflow = true; break; }
-                        sk = sk + exp(clike);
-                    }
-                    ssculm = ssculm + (overflow ? 0.0 : 1.0 / (1.0 + sk));
-                    if (u < ssculm) { flag = kk + 1; break; }
-                }
-                if (flag == 1) {
-                    gt = 0.0;
-                    upd = D.cls[o] > 1 ? gk : 0.0;
-                } else {
-                    const double v1 = zz + vare / S->gp[flag - 1];
-                    gt = d_rnorm(rhs / v1, sqrt(vare / v1), R);
-                    upd = gk - gt;
-                }
-                D.g[o] = gt;
-                D.cls[o] = flag;
-            }
-            if (err) flag_err(D, 1);
-            s_d = upd;
+        for (int i = tid; i < D.n; i += SS_THREADS) {
+            const int g = col[i];
+            part += r[i] * (g == 0 ? x0 : (g == 1 ? x1 : x2));
+        }
+        part = warp_sum(part);
+        if (lane == 0) s_part[warp] = part;
+        __syncthreads();
+        if (warp == 0) {
+            double d = lane < SS_THREADS / 32 ? s_part[lane] : 0.0;
+            d = warp_sum(d);
+            const double upd = single_site_draw(D, S, c, rep, snploc, d);
+            if (lane == 0) s_upd = upd;
         }
         __syncthreads();
-        const double upd = s_d;
-        if (upd != 0.0)
-            for (int i = threadIdx.x; i < D.n; i += blockDim.x) r[i] = r[i] + xv[col[i]] * upd;
+        const double upd = s_upd;
+        if (upd != 0.0) {
+            for (int i = tid; i < D.n; i += SS_THREADS) {
+                const int g = col[i];
+                r[i] = r[i] + (g == 0 ? x0 : (g == 1 ? x1 : x2)) * upd;
+            }
+        }
+    }
+    if (in_smem) {
         __syncthreads();
+        for (int i = tid; i < D.n; i += SS_THREADS) rg[i] = s_r[i];
     }
 }
 
@@ -634,7 +705,10 @@ __global__ void __launch_bounds__(128) k_hyper(Dev D)
         if (keep) {
             S->counter += 1;
             S->mu_store = S->mu_store + mu;
-            for (int e = 0; e < ngm; ++e) S->varstore[e] = S->varstore[e] + S->varindist[e];
+            // soda_bayes keeps varstore for every method (models.f90:530), regular_bayes
+            // not for BayesA (models.f90:893-896)
+            if (!(D.regular && m == SODAGPU_BAYES_A))
+                for (int e = 0; e < ngm; ++e) S->varstore[e] = S->varstore[e] + S->varindist[e];
             S->vare_store = S->vare_store + S->vare;
             if (m != SODAGPU_BAYES_A) {
                 S->included_store = S->included_store + S->included;
@@ -999,6 +1073,7 @@ static cudaError_t carve_all()
     if (e == cudaSuccess) e = max_carveout(k_mu_partial);
     if (e == cudaSuccess) e = max_carveout(k_mu_apply);
     if (e == cudaSuccess) e = max_carveout(k_skipped);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_skipped, cudaFuncAttributeMaxDynamicSharedMemorySize, SS_SMEM_MAX);
     if (e == cudaSuccess) e = max_carveout(k_stats);
     if (e == cudaSuccess) e = max_carveout(k_hyper);
     if (e == cudaSuccess) e = max_carveout(k_post);
@@ -1194,7 +1269,10 @@ cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_c
     }
     {
         ProfScope ps(prof, st, PROF_OTHER);
-        if (D.nskipped > 0) k_skipped<<<C, 1024, 0, st>>>(D);
+        if (D.nskipped > 0) {
+            const size_t sm = (size_t)D.n * sizeof(double) <= (size_t)SS_SMEM_MAX ? (size_t)D.n * sizeof(double) : 0;
+            k_skipped<<<C, SS_THREADS, sm, st>>>(D);
+        }
         k_stats<<<dim3(NSTAT + D.nr_ctas, C), 256, 0, st>>>(D);
         k_hyper<<<C, 128, 0, st>>>(D);
         const int pgrid = (D.p + 255) / 256 < 4 * sm_count ? (D.p + 255) / 256 : 4 * sm_count;

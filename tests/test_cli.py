@@ -157,3 +157,31 @@ def test_cli_two_jobs_match_reference_layout(cli, gpu_lib, tmp_path):
     assert log[-1].startswith("Setup: ") and " MCMC: " in log[-1] and " Total: " in log[-1]
     plog = open(tmp_path / "pred_cli.log").readlines()
     assert [l[:31] for l in plog[2:9]] == [l[:31] for l in GOLDEN["log_predict"][2:9]]
+
+
+@pytest.mark.gpu
+def test_cli_sodaoff_runs_the_regular_sampler(cli, gpu_lib, tmp_path):
+    """-SODAOff (SODABayes.f90:134-137): regular_bayes on the GPU; the .log has
+    the reference's example-2 layout ('SODA off = T', no block lines) and the
+    .hyp its rows."""
+    from sodabayes_gb300 import synth
+    n, p = 200, 300
+    G, y, _ = synth.make(synth.SynthSpec(n=n, p=p, ld_block=25, rho=0.5, ncausal=20, h2=0.5, mean=50.0, seed=4))
+    write_plink(str(tmp_path / "train"), G, y)
+    (tmp_path / "off.par").write_text(
+        "BEGIN BayesR_Regular_MCMC\n"
+        "   -bfile train\n   -method BayesR\n   -scale_va 50\n   -scale_ve 50\n   -df_va 4.5\n   -df_ve 4.5\n"
+        "   -numit 30\n   -burnin 10\n   -thin 1\n   -nmix 4\n   -mix 0.0,0.0001,0.001,0.01\n   -SODAOff\n"
+        "   -seed 123456789\n   -out bayesr_off\n"
+        "END BayesR_Regular_MCMC\n")
+    r = subprocess.run([cli, "off.par"], capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    log = open(tmp_path / "bayesr_off.log").readlines()
+    ref = GOLDEN["log_sodaoff"]
+    assert log[0] == "Running program SODABayes: BayesR_Regular_MCMC\n"
+    assert [l[:31] for l in log[2:17]] == [l[:31] for l in ref[2:17]]
+    assert log[14] == "SODA off                     = T\n"
+    hyp = open(tmp_path / "bayesr_off.hyp").readlines()
+    assert hyp[0] == GOLDEN["hyp_bayesr"][0] and len(hyp) == 31
+    eff = open(tmp_path / "bayesr_off.eff").readlines()
+    assert len(eff) == p + 1

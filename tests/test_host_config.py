@@ -42,6 +42,8 @@ def test_method_names_and_pi_range():
         make_config(10, 20, JobOptions(method="BayesB", pi=1.0, blocksize=5))
 
 
-def test_soda_off_is_rejected():
-    with pytest.raises(ValueError):
-        make_config(10, 20, JobOptions(method="BayesC", nthreads=1))
+def test_soda_off_runs_the_regular_sampler():
+    """blocksize <= 1 switches SODA off (soda.f90:418-421): the regular sampler
+    (models.f90:607-962) runs, with one nominal subset of every SNP."""
+    cfg = make_config(10, 20, JobOptions(method="BayesC", nthreads=1))
+    assert cfg.sampler == 1 and (cfg.blocksize, cfg.nblocks, cfg.blockt) == (20, 1, 1)
