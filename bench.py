@@ -190,6 +190,14 @@ def _rhs_bytes(n, N, chains, prec, tc=False):
     return n * N * ex + N * (N + 1) // 2 * eu + chains * (n * er + N * 8)
 
 
+def _update_bytes(n, N, chains):
+    """Algorithmic bytes of one tensor-core update launch (every stage
+    active): the subset's genotype columns and the three bf16 terms of the
+    upper triangle of U once, the delta split once, and each chain's FP64
+    residual read and written with its bf16 split."""
+    return n * N + N * (N + 1) // 2 * 6 + 3 * chains * N * 2 + chains * n * (8 + 8 + 6)
+
+
 def bench_ours(args, rank, ws):
     import torch
 
@@ -224,18 +232,23 @@ def bench_ours(args, rank, ws):
     res["clocks"] = clk.summary()
     res["included_at_timing"] = st["included"]
     nb = spec.p // BLOCKSIZE
-    rhs_ms = prof["rhs"][0] / prof["rhs"][1]
     hbm, peak_kind = _peaks()
-    bytes_rhs = _rhs_bytes(spec.n, BLOCKSIZE, C, "fp8", tc=True)
-    achieved = bytes_rhs / (rhs_ms / 1000.0) / 1e9
-    res["roofline"] = {"bound": "hbm", "kernel": "k_rhs_tc<%d>" % C, "achieved": round(achieved, 1),
-                       "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                       "traffic": _measured_traffic("k_rhs_tc%d_n20000_s2000.md" % C),
-                       "traffic_source": "ncu --set full of one launch of the same kernel at the same subset shape "
-                                         "(profiles/k_rhs_tc%d_n20000_s2000.md)" % C,
-                       "peak_source": peak_kind, "bytes_per_launch": bytes_rhs,
-                       "launch_ms": round(rhs_ms, 5),
-                       "kernel_ms_per_iter": {k: round(v[0] / 2, 4) for k, v in prof.items()}}
+    kms = {k: round(v[0] / 2, 4) for k, v in prof.items()}
+
+    def _roof(cls, kernel, nbytes):
+        ms = prof[cls][0] / prof[cls][1]
+        achieved = nbytes / (ms / 1000.0) / 1e9
+        return {"bound": "hbm", "kernel": kernel % C, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4),
+                "traffic": _measured_traffic(kernel.split("<")[0] + "%d_n20000_s2000.md" % C),
+                "traffic_source": "ncu --set full of one launch of the same kernel at the same subset shape "
+                                  "(profiles/%s%d_n20000_s2000.md)" % (kernel.split("<")[0], C),
+                "peak_source": peak_kind, "bytes_per_launch": nbytes, "launch_ms": round(ms, 5)}
+
+    # the dominant kernel (the residual update), then the rhs
+    res["roofline"] = _roof("update", "k_update_tc<%d>", _update_bytes(spec.n, BLOCKSIZE, C))
+    res["roofline"]["kernel_ms_per_iter"] = kms
+    res["roofline_rhs"] = _roof("rhs", "k_rhs_tc<%d>", _rhs_bytes(spec.n, BLOCKSIZE, C, "fp8", tc=True))
     res["gpu_launches"] = K * (3 + 3 * nb + 5)   # mu; rhs, draws, update per subset; hyper/stats/recal
 
     # ---- plain FP32 path (1 chain), same timing -----------------------------------
@@ -425,7 +438,7 @@ def main():
                            "parallelism": f"replicas x{ws}"},
                 "fp32_plain": res["fp32_plain"],
                 "speedup_vs_fp32_plain": res["value"] / ws / res["fp32_plain"]["value"],
-                "error_vs_fp64": res["error_vs_fp64"], "roofline": res["roofline"],
+                "error_vs_fp64": res["error_vs_fp64"], "roofline": res["roofline"], "roofline_rhs": res["roofline_rhs"],
                 "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
                 "included_at_timing": res["included_at_timing"]}
