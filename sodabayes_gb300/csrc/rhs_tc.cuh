@@ -38,6 +38,7 @@ constexpr int TC_KC = 128;       // individuals per genotype stage
 constexpr int TC_KU = 64;        // U rows per augmenting stage
 constexpr int TC_THREADS = 576;  // 16 converter warps, the TMA warp, the MMA warp
 constexpr int TC_CONV = 512;     // converter threads
+constexpr int TC_CONV_WARPS = TC_CONV / 32;   // each converter warp arrives once per stage
 constexpr int TC_NOB = 4;        // bf16 codes operands in tensor memory (converters run up to 4 stages ahead)
 constexpr int TC_WARP_TMA = 16, TC_WARP_MMA = 17;
 
@@ -112,10 +113,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) {
             tc::mbar_init(&s_full[i], 1);
-            tc::mbar_init(&s_empty[i], TC_CONV + 1);    // converters + the MMAs reading B (and U's A)
+            tc::mbar_init(&s_empty[i], TC_CONV_WARPS + 1);   // converter warps + the MMAs reading B (and U's A)
         }
         for (int i = 0; i < TC_NOB; ++i) {
-            tc::mbar_init(&s_conv[i], TC_CONV);
+            tc::mbar_init(&s_conv[i], TC_CONV_WARPS);
             tc::mbar_init(&s_opfree[i], 1);
         }
         tc::mbar_init(&s_done, 1);
@@ -223,6 +224,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (s < nck) {
                 // the operand buffer was last read by the MMAs of stage s - TC_NOB
                 if (ok && s >= TC_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
+                ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
                 if (!ok) {
                     s_err = 1;
                     break;
@@ -244,12 +246,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 64 * ob + 16 * s4, v);
                 tc::tmem_wait_st();
                 tc::fence_before_sync();
-                tc::mbar_arrive(&s_conv[ob]);
-            } else if (!ok) {
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
+            } else if (!__all_sync(0xffffffffu, ok)) {
                 s_err = 1;
                 break;
             }
-            tc::mbar_arrive(&s_empty[buf]);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&s_empty[buf]);
         }
         if (ns > 0 && !tc::mbar_wait(&s_done, 0)) s_err = 1;
     }

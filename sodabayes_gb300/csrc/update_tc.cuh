@@ -50,6 +50,7 @@ constexpr int TV_THREADS = 448;    // 8 converter warps, TMA, MMA, 4 epilogue wa
 constexpr int TV_MAXG = 512;       // CTAs (one per SM)
 constexpr int TV_WROW = 1, TV_WRA = 1;   // unit weights of the split (row / ra units)
 constexpr int TV_CONV = 256;
+constexpr int TV_CONV_WARPS = TV_CONV / 32;   // each converter warp arrives once per unit
 constexpr int TV_WARP_TMA = 8, TV_WARP_MMA = 9, TV_WARP_EPI = 10;
 
 template <int CT>
@@ -375,10 +376,10 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             }
             for (int i = 0; i < TV_NC; ++i) {
                 tc::mbar_init(&s_fullc[i], 1);
-                tc::mbar_init(&s_emptyc[i], TV_CONV);   // the converters
+                tc::mbar_init(&s_emptyc[i], TV_CONV_WARPS);   // the converter warps
             }
             for (int i = 0; i < TV_NOB; ++i) {
-                tc::mbar_init(&s_conv[i], TV_CONV);
+                tc::mbar_init(&s_conv[i], TV_CONV_WARPS);
                 tc::mbar_init(&s_opfree[i], 1);
             }
             for (int i = 0; i < 2; ++i) {
@@ -487,6 +488,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 bool ok = tc::mbar_wait(&s_fullc[cb], (s / TV_NC) & 1);
                 if (x.kind == 0) {
                     if (ok && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TV_NOB) / TV_NOB) & 1);
+                    ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
                     if (!ok) {
                         s_err = 13;
                         break;
@@ -508,12 +510,15 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         *reinterpret_cast<uint4 *>(ob_ + (((j0 + 1) ^ r) << 4)) = make_uint4(o[4], o[5], o[6], o[7]);
                     }
                     tc::fence_async_smem();
-                } else if (!ok) {
+                } else if (!__all_sync(0xffffffffu, ok)) {
                     s_err = 14;
                     break;
                 }
-                tc::mbar_arrive(&s_emptyc[cb]);
-                tc::mbar_arrive(&s_conv[ob]);
+                __syncwarp();
+                if (lane == 0) {
+                    tc::mbar_arrive(&s_emptyc[cb]);
+                    tc::mbar_arrive(&s_conv[ob]);
+                }
             }
         } else {
             // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. (accumulator

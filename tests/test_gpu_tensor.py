@@ -16,6 +16,7 @@ from sodabayes_gb300 import JobOptions, SodaJob, make_config, synth
 pytestmark = pytest.mark.gpu
 
 N, P, S = 1000, 1700, 300   # n not a multiple of 128, subsets of 300 and 299 SNPs
+GROUPS = (np.arange(P) % 3 + 1).astype(np.int32)   # three annotation classes for BayesRc
 
 
 @pytest.fixture(scope="module")
@@ -32,9 +33,12 @@ def _opts(**kw):
 
 def _run(data, iters, d_offset=0.0, **kw):
     G, y, _ = data
-    with SodaJob(make_config(N, P, _opts(**kw))) as job:
+    cfg = make_config(N, P, _opts(**kw))
+    with SodaJob(cfg) as job:
         job.load_genotypes(G)
         job.load_pheno(y)
+        if cfg.ngroup > 1:
+            job.set_groups(GROUPS)
         if d_offset:
             job.set_d_offset(d_offset)
         job.build_z()
@@ -58,6 +62,25 @@ def test_tensor_sweep_matches_cuda_core_sweep(gpu_lib, data, chains):
         assert agree >= 0.999, (c, agree)
         assert rel <= 1e-4, (c, rel)
         assert abs(tcs[c]["vare"] - ref[c]["vare"]) <= 1e-4 * ref[c]["vare"]
+
+
+@pytest.mark.parametrize("method", ["BayesA", "BayesB", "BayesC", "BayesR", "BayesRc"])
+def test_tensor_sweep_every_method(gpu_lib, data, method):
+    """Every model on the tensor-core path with 16 chains on shared genotypes
+    (BayesRc: four-class mixtures in three annotation groups, the shape of the
+    16-chain BayesRc analysis at a size the CUDA-core sweep checks quickly)."""
+    kw = dict(method=method, chains=16, pi=0.95)
+    if method in ("BayesR", "BayesRc"):
+        kw.update(nmix=4, mix=(0.0, 1e-4, 1e-3, 1e-2))
+    if method == "BayesRc":
+        kw.update(ngroup=3)
+    tcs = _run(data, 1, **kw)
+    ref = _run(data, 1, kernels="cuda_cores", **kw)
+    for c in range(16):
+        agree, rel = _agree(tcs[c], ref[c])
+        assert agree >= 0.999, (c, agree)
+        assert rel <= 1e-3, (c, rel)
+        assert abs(tcs[c]["vare"] - ref[c]["vare"]) <= 1e-3 * ref[c]["vare"]
 
 
 def test_tensor_sweep_tracks_fp64(gpu_lib, data):
