@@ -60,6 +60,22 @@ CUresult make_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, const void *base, 
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
 
+// 3-D tile map over the tiled codes (blocks of 128 positions x 256
+// individuals, one contiguous [128][256] byte array each), loaded in boxes of
+// b0 individuals x b1 positions of one block.
+CUresult make_tmap_codes(CUtensorMap *m, const void *base, long long nblocks, uint32_t b0, uint32_t b1,
+                         CUtensorMapSwizzle sw)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 fn = tmap_encoder();
+    if (!fn) return CUDA_ERROR_NOT_SUPPORTED;
+    const cuuint64_t dims[3] = {256, 128, (cuuint64_t)nblocks};
+    const cuuint64_t strides[2] = {256, 256 * 128};
+    const cuuint32_t box[3] = {b0, b1, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<void *>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
 thread_local std::string g_last_error;
 
 int fail(int code, const char *fmt, ...)
@@ -163,6 +179,10 @@ struct sodagpu_ctx {
     TcMaps maps{};
     std::vector<int32_t> h_rtab;         // work table of the tensor-core rhs
     int32_t *rtab = nullptr;
+    std::vector<int32_t> h_qoff;         // first code block of each subset (tiled codes)
+    int32_t *qoff = nullptr;
+    int8_t *Gt = nullptr;                // tiled codes: [blocks][128][256]
+    long long ncblk = 0;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
     cudaGraphExec_t graph = nullptr;
@@ -818,6 +838,7 @@ int build_dev(sodagpu_ctx *c)
     D.ugrid = c->ugrid;
     D.nvt = sweep_tc_update_tiles(c->n);
     D.rtab = c->rtab;
+    D.qoff = c->qoff;
     D.tstride = sweep_tc_table_stride(c->bs);
     D.rsp = c->rsp;
     D.rasp = c->rasp;
@@ -877,16 +898,20 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             TRY(c->alloc(&c->rtab, c->h_rtab.size(), false));
             CUDA_TRY(cudaMemcpyAsync(c->rtab, c->h_rtab.data(), c->h_rtab.size() * 4, cudaMemcpyHostToDevice, c->st));
             c->maps.h_rtab = c->h_rtab.data();
+            c->h_qoff.assign((size_t)c->nb + 1, 0);
+            c->ncblk = (long long)sweep_tc_code_blocks(c->blk_sizes.data(), c->nb, c->h_qoff.data()) *
+                       sweep_tc_update_tiles(c->n);
+            TRY(c->alloc(&c->qoff, c->h_qoff.size(), false));
+            CUDA_TRY(cudaMemcpyAsync(c->qoff, c->h_qoff.data(), c->h_qoff.size() * 4, cudaMemcpyHostToDevice, c->st));
+            TRY(c->alloc(&c->Gt, (size_t)c->ncblk * TC_CODE_BLOCK, false));
         }
     }
     build_dev(c);
     if (c->tc) {
         const int NB = sweep_tc_rows(C);
-        CUresult r = make_tmap_2d(&c->maps.codes128, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 128,
-                                  128, CU_TENSOR_MAP_SWIZZLE_128B);
+        CUresult r = make_tmap_codes(&c->maps.codes128, c->Gt, c->ncblk, 128, 128, CU_TENSOR_MAP_SWIZZLE_128B);
         if (r == CUDA_SUCCESS)
-            r = make_tmap_2d(&c->maps.codes256, CU_TENSOR_MAP_DATA_TYPE_UINT8, c->G, c->ldx, c->p, c->ldx, 256, 64,
-                             CU_TENSOR_MAP_SWIZZLE_NONE);
+            r = make_tmap_codes(&c->maps.codes256, c->Gt, c->ncblk, 256, 64, CU_TENSOR_MAP_SWIZZLE_NONE);
         if (r == CUDA_SUCCESS)
             r = make_tmap_2d(&c->maps.rsp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->rsp, c->ldr, NB, (uint64_t)c->ldr * 2,
                              64, NB, CU_TENSOR_MAP_SWIZZLE_128B);
@@ -905,6 +930,7 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         if (r != CUDA_SUCCESS) return fail(SODAGPU_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
         if (!c->usp_ready) {
             CUDA_TRY(sweep_tc_prepare(c->G, c->D, c->st));
+            CUDA_TRY(sweep_tc_tile_codes(c->G, c->D, c->Gt, c->ncblk, c->sm_count, c->st));
             c->usp_ready = true;
         }
     }

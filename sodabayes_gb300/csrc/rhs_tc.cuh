@@ -16,9 +16,10 @@
 // draw kernel.  A CTA owns one M tile and a contiguous range of its stages
 // (genotype stages first) and runs a warp-specialised pipeline synchronised
 // by mbarriers:
-//   warp 16 (one thread) TMA: each stage's A tile (codes: 128 x 128 bytes;
-//           U terms: 128 x 64 bf16) and B tile, all 128-byte swizzled, into a
-//           raw buffer (NS buffers in flight);
+//   warp 16 (one thread) TMA: each stage's A tile (codes: 128 x 128 bytes,
+//           half of one 32 KB block of the tiled copy, so 128-byte rows 256
+//           bytes apart; U terms: 128 x 64 bf16) and B tile, all 128-byte
+//           swizzled, into a raw buffer (NS buffers in flight);
 //   warps 0-15 convert a genotype stage's codes into one of four bf16
 //           operands in tensor memory (lane = SNP, tcgen05.st);
 //   warp 17 (one thread) issues the stage's MMAs (A from tensor memory or,
@@ -136,14 +137,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc::tma_prefetch_desc(&tm_rsp);
             tc::tma_prefetch_desc(&tm_usp);
             tc::tma_prefetch_desc(&tm_rasp);
-            // A tiles (codes, U terms) do not depend on the previous kernel; B tiles do
+            // A tiles (codes, U terms) do not depend on the previous kernel; B tiles do.  Codes:
+            // half t % 2 of the tiled block (tile mt of the subset, individuals 256 (t / 2) ..)
+            const int cblk = (D.qoff[b] + mt) * D.nvt;
             auto load_a = [&](int s) {
                 const int t = t0 + s;
                 unsigned char *rw = raw0 + (size_t)(s % NS) * T::RAW;
                 uint64_t *bar = &s_full[s % NS];
                 if (t < nG) {
                     tc::mbar_expect_tx(bar, T::TX_G);
-                    tc::tma_load_2d(rw, &tm_codes, t * TC_KC, ls + j0, bar);
+                    tc::tma_load_3d(rw, &tm_codes, (t & 1) * TC_KC, 0, cblk + (t >> 1), bar);
                 } else {
                     const int u = t - nG;
                     tc::mbar_expect_tx(bar, T::TX_U);

@@ -117,6 +117,7 @@ struct Dev {
     float *vpart;              // [tiles + update CTAs][C][256] update partial sums, one slot per segment
     unsigned long long *ugrid; // grid-barrier counter of the update (each launch adds its CTA count)
     int nvt;                   // row tiles of 256 individuals of the update
+    const int32_t *qoff;       // [nb+1] first 128-position code block of each subset (tiled codes)
     const int32_t *rtab;       // [nb][tstride] first rhs CTA of each 128-SNP tile, then the total
     int tstride;
     uint16_t *rsp;             // [round_up(3C,16)][ldr] bf16 hi/mid/lo of r32 (rows c, C+c, 2C+c), or null

@@ -1177,6 +1177,56 @@ cudaError_t sweep_tc_prepare(int8_t *G, const Dev &D, cudaStream_t st)
     return cudaGetLastError();
 }
 
+int sweep_tc_code_blocks(const int *blk_sizes, int nb, int32_t *qoff)
+{
+    int tot = 0;
+    for (int b = 0; b < nb; ++b) {
+        qoff[b] = tot;
+        tot += (blk_sizes[b] + TC_TM - 1) / TC_TM;
+    }
+    qoff[nb] = tot;
+    return tot;
+}
+
+// Code block (q2, t) = positions 128 (q2 - qoff[b]) .. of subset b x individuals 256 t .., one
+// contiguous [128][256] byte array; positions past the subset and individuals past n hold 0.
+// A warp copies two rows per pass (16-byte chunks), so reads and writes are coalesced.
+__global__ void __launch_bounds__(256) k_tile_codes(const int8_t *G, Dev D, int8_t *Gt, long long nblocks)
+{
+    const int ch = threadIdx.x & 15;
+    for (long long blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+        const int q2 = (int)(blk / D.nvt), t = (int)(blk - (long long)q2 * D.nvt);
+        int lo = 0, hi = D.nb - 1;   // the subset: last b with qoff[b] <= q2
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (D.qoff[mid] <= q2) lo = mid;
+            else hi = mid - 1;
+        }
+        const int ls = D.blk_ls[lo], N = D.blk_ls[lo + 1] - ls, r0 = (q2 - D.qoff[lo]) * TC_TM;
+        const int i0 = t * TV_N + 16 * ch;
+        for (int row = threadIdx.x >> 4; row < TC_TM; row += 16) {
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (r0 + row < N && i0 < D.n) {
+                v = *reinterpret_cast<const uint4 *>(G + (size_t)(ls + r0 + row) * D.ldx + i0);
+                if (i0 + 16 > D.n) {
+                    uint8_t *bv = reinterpret_cast<uint8_t *>(&v);
+                    for (int e = D.n - i0; e < 16; ++e) bv[e] = 0;
+                }
+            }
+            *reinterpret_cast<uint4 *>(Gt + (size_t)blk * (TC_TM * TV_N) + row * TV_N + 16 * ch) = v;
+        }
+    }
+}
+
+cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, int8_t *Gt, long long nblocks, int sm_count,
+                                cudaStream_t st)
+{
+    if (!Gt || !D.qoff || nblocks <= 0) return cudaErrorInvalidValue;
+    const long long grid = std::min<long long>(nblocks, 8LL * sm_count);
+    k_tile_codes<<<(unsigned)grid, 256, 0, st>>>(G, D, Gt, nblocks);
+    return cudaGetLastError();
+}
+
 int sweep_tc_table_stride(int bs) { return (bs + TC_TM - 1) / TC_TM + 1; }
 
 void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count, int32_t *rtab)

@@ -27,6 +27,18 @@ void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count
 // sd_k = 1 where 1/sd_k is 0) and zeroes the codes of those columns in G (their
 // x values are all 0, so no product changes).
 cudaError_t sweep_tc_prepare(int8_t *G, const Dev &D, cudaStream_t st);
+// Tiled copy of the codes for the tensor-core kernels: per subset b, code
+// blocks qoff[b] .. qoff[b+1]-1 of 128 positions (the last one zero-padded);
+// block (q2, t) of 128 positions x 256 individuals is one contiguous
+// [128][256] byte array at Gt + (q2 * D.nvt + t) * 32768, so every TMA box
+// the kernels load is a contiguous 16 KB (update) or half of a 32 KB block
+// (rhs).  sweep_tc_code_blocks fills qoff[0..nb] and returns the block rows;
+// sweep_tc_tile_codes writes all nblocks = rows * D.nvt blocks from G (after
+// sweep_tc_prepare, on the same stream).
+constexpr int TC_CODE_BLOCK = 128 * 256;   // bytes of one code block
+int sweep_tc_code_blocks(const int *blk_sizes, int nb, int32_t *qoff);
+cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, int8_t *Gt, long long nblocks, int sm_count,
+                                cudaStream_t st);
 // Optional per-launch event recording (eager profiling, never inside a graph):
 // before/after every launch an event pair is recorded and its kernel class
 // stored.  Classes: 0 rhs, 1 residual update, 2 mu, 3 everything else, 4 draws.
@@ -37,13 +49,14 @@ struct ProfHook {
     int n, cap;
 };
 
-// TMA descriptors of the tensor-core sweep: genotype codes in 128 x 128
-// (individuals x SNPs, 128-byte swizzle) and 256 x 64 (unswizzled) boxes; the
+// TMA descriptors of the tensor-core sweep: the tiled genotype codes in
+// 128 x 128 x 1 (individuals x positions x block, 128-byte swizzle) and
+// 256 x 64 x 1 (unswizzled) boxes; the
 // bf16 splits of delta, r and ra in 64 x rows boxes; the bf16 U terms in
 // 64 x 128 and 64 x 64 (U rows x SNPs) boxes (all 128-byte swizzle); and the
 // host copy of the rhs work table.
 struct TcMaps {
-    CUtensorMap codes128, codes256, d;  // codes (128 x 128 and 256 x 64 boxes), delta split
+    CUtensorMap codes128, codes256, d;  // tiled codes (128 x 128 and 256 x 64 boxes), delta split
     CUtensorMap rsp, usp, usp64, rasp;  // residual split, U-term split (two box heights), ra split
     const int32_t *h_rtab;              // host copy of D.rtab
 };

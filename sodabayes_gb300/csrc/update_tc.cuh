@@ -8,14 +8,17 @@
 // Both products run on tcgen05 as transposed products D = S B' with
 //   S (operand A, K-major, TMA) = the bf16 hi/mid/lo split of delta/sd written
 //     by the draws (delta itself for columns with sd = 0, whose codes are
-//     zero): rows term * chains + c (3 * chains of the M = 128 rows are
+//     zero): rows term * chains + c (3 * chains of the M = 64 rows are
 //     used), K = subset positions, 64 per stage;
 //   B (N = 256) = for r, the genotype codes of 256 individuals, loaded by TMA
-//     as they are stored (64 positions x 256 bytes) and widened to bf16 by
+//     from the tiled copy of the codes as one contiguous 16 KB (64 positions
+//     x 256 bytes; SNP-major rows n bytes apart load at about half the
+//     bandwidth when every SM streams) and widened to bf16 by
 //     the converter warps into an MN-major operand (individuals contiguous);
 //     for ra, one bf16 term of sd * U (256 rows of U), loaded by TMA straight
 //     into an MN-major operand (the factor is stored column by column);
-//   D = 128 x 256 FP32 in tensor memory, double-buffered.
+//   D = 64 x 256 FP32 in tensor memory (rows 16q .. in lanes 32q ..),
+//     double-buffered.
 // A tcgen05.mma costs about the same for any N up to 256, so the codes sit on
 // the N = 256 side: one instruction consumes 4 KB of codes.
 //
@@ -41,6 +44,7 @@ namespace soda {
 
 constexpr int TV_N = 256;          // individuals per row tile / rows of U per ra tile (MMA N)
 constexpr int TV_K = 64;           // subset positions per stage
+constexpr int TV_M = 64;           // MMA M (the 3 * chains <= 48 rows of the delta split)
 constexpr int TV_NA = 4;           // delta-split tiles (operand A) in flight
 constexpr int TV_NC = 4;           // code tiles in flight
 constexpr int TV_NOB = 2;          // B operands
@@ -58,16 +62,20 @@ struct UpdTc {
     static constexpr int NB = RhsTc<CT>::NB;
     static constexpr int ROWS = 3 * CT;                // accumulator rows in use
     static constexpr int RAW_A = NB * TV_K * 2;        // delta split tile: NB rows x 64 bf16, 128-byte swizzle
-    // an M = 128 MMA reads 128 rows (16 KB) from A's start: each A slot owns 16 KB, so that no
-    // byte the MMA reads is the target of a TMA load in flight (rows past NB are never written)
-    static constexpr int ASTRIDE = 128 * 128;
+    // an M = 64 MMA reads 64 rows (8 KB) from A's start: each A slot owns 8 KB, so that no byte
+    // the MMA reads is the target of a TMA load in flight (rows past NB are never written)
+    static constexpr int ASTRIDE = TV_M * 128;
     static constexpr int AREG = TV_NA * ASTRIDE;
     static constexpr int RAW_C = TV_K * TV_N;          // codes: 64 positions x 256 individuals, unswizzled
     static constexpr int C0 = AREG;
     static constexpr int BOP = TV_K * TV_N * 2;        // B operand: 64 x 256 bf16
     static constexpr int BOP0 = C0 + TV_NC * RAW_C;
-    static constexpr size_t SMEM = 1024 + (size_t)BOP0 + (size_t)TV_NOB * BOP;
+    // epilogue staging: the accumulator rows in use, all 256 columns (row stride 257 floats)
+    static constexpr int STG0 = BOP0 + TV_NOB * BOP;
+    static constexpr int STG = ((ROWS * (TV_N + 1) * 4 + 1023) / 1024) * 1024;
+    static constexpr size_t SMEM = 1024 + (size_t)STG0 + (size_t)STG;
     static_assert(RAW_A % 1024 == 0 && AREG % 1024 == 0 && RAW_C % 1024 == 0, "buffer alignment");
+    static_assert(NB <= TV_M, "delta split rows exceed the MMA's M");
 };
 
 // Units of one subset, as every role decodes them.
@@ -99,6 +107,33 @@ __device__ __forceinline__ Unit decode_unit(const UnitPlan &P, int u, int &ra_hi
     x.kind = 1;
     x.tile = a;
     x.q = P.qs[a] + w / 3;
+    x.term = w % 3;
+    return x;
+}
+
+// decode_unit without a hint (binary search over the ra tiles), for lanes that
+// decode different units at once.
+__device__ __forceinline__ Unit decode_unit_bs(const UnitPlan &P, int u)
+{
+    Unit x;
+    if (u < P.R) {
+        x.kind = 0;
+        x.tile = u / P.nact;
+        x.q = u - x.tile * P.nact;
+        x.term = 0;
+        return x;
+    }
+    const int v = u - P.R;
+    int lo = 0, hi = P.nra - 1;   // last a with pref[a] <= v
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.pref[mid] <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    const int w = v - P.pref[lo];
+    x.kind = 1;
+    x.tile = lo;
+    x.q = P.qs[lo] + w / 3;
     x.term = w % 3;
     return x;
 }
@@ -167,6 +202,24 @@ __device__ __forceinline__ void tile_units(const UnitPlan &P, int tg, long long 
     }
 }
 
+// The old values (r or ra) of chain c in half h of global tile tg, lane l
+// holding elements l + 32k; nothing else writes them during the update.
+template <int CT>
+__device__ __forceinline__ void update_pair_rold(const Dev &D, const UnitPlan &P, int tg, int h, int c, int N,
+                                                 double (&rold)[4])
+{
+    const int lane = threadIdx.x & 31;
+    const bool is_r = tg < P.nvt;
+    const int tile = is_r ? tg : tg - P.nvt;
+    const int lim = is_r ? D.n : min(N, D.bs);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = tile * TV_N + h * 128 + lane + 32 * k;
+        rold[k] = 0.0;
+        if (i < lim) rold[k] = is_r ? __ldcg(D.r + (size_t)c * D.ldr + i) : __ldcg(D.ra + (size_t)c * D.ldra + i);
+    }
+}
+
 // Adds the segments of chain c in half h (128 elements) of global tile tg in
 // segment order and applies the update: r, its bf16 split and the 128-row
 // partial sum of r for a row tile, ra and its split for an ra tile.  Lane l
@@ -174,7 +227,7 @@ __device__ __forceinline__ void tile_units(const UnitPlan &P, int tg, long long 
 // are issued together.
 template <int CT>
 __device__ __forceinline__ void update_reduce_pair(const Dev &D, const UnitPlan &P, const int *bnd, int G, int tg,
-                                                   int h, int c, const double *s_k0, int N)
+                                                   int h, int c, const double *s_k0, int N, const double (&rold)[4])
 {
     const int lane = threadIdx.x & 31;
     const bool is_r = tg < P.nvt;
@@ -184,15 +237,9 @@ __device__ __forceinline__ void update_reduce_pair(const Dev &D, const UnitPlan 
     tile_units(P, tg, u0, u1);
     if (u1 <= u0) return;   // no unit touched this tile: nothing changed
     const int sl = unit_cta(bnd, (int)u0, G), sh = unit_cta(bnd, (int)u1 - 1, G);
-    double rold[4];
     float acc[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int i = tile * TV_N + h * 128 + lane + 32 * k;
-        rold[k] = 0.0;
-        if (i < lim) rold[k] = is_r ? __ldcg(D.r + (size_t)c * D.ldr + i) : __ldcg(D.ra + (size_t)c * D.ldra + i);
-        acc[k] = 0.0f;
-    }
+    for (int k = 0; k < 4; ++k) acc[k] = 0.0f;
     for (int q0 = sl; q0 <= sh; q0 += 4) {
         float v[4][4];
 #pragma unroll
@@ -275,7 +322,6 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     __shared__ UnitPlan s_plan;
     __shared__ double s_k0p[128], s_k0[CT];
     __shared__ int s_bnd[TV_MAXG + 1];
-    __shared__ float s_stage[3 * CT][33];
     unsigned char *raw0 = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
     unsigned char *bop0 = raw0 + T::BOP0;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -283,6 +329,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     const int N = D.blk_ls[b + 1] - ls;
     const int nq = (N + TV_K - 1) / TV_K;
     const bool pd = D.blk_pd[b] != 0;
+    const int cblk = D.qoff[b];   // the subset's first code block row (set up before the sweep)
     tc::pdl_trigger();
     tc::pdl_wait();   // the draws of this subset are complete
 
@@ -366,8 +413,6 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     __syncthreads();
     const int u_begin = s_bnd[blockIdx.x], u_end = s_bnd[blockIdx.x + 1];
     const int nu = u_end - u_begin;
-    // the centring term (epilogue warps, before their first segment)
-    if (warp >= TV_WARP_EPI) update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);
     if (nu > 0) {
         if (tid == 0) {
             for (int i = 0; i < TV_NA; ++i) {
@@ -395,45 +440,77 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
         const uint32_t tm = s_tmem;
 
         if (warp == TV_WARP_TMA) {
+            // the warp decodes 32 units at a time into registers (lane l: unit s0 + l); lane 0 issues
+            // their loads, taking each unit's coordinates by shuffle, so that no chain of shared-memory
+            // loads sits between two issues
             if (lane == 0) {
                 tc::tma_prefetch_desc(&tm_codes);
                 tc::tma_prefetch_desc(&tm_d);
                 tc::tma_prefetch_desc(&tm_u);
-                int hint = 0;
-                for (int s = 0; s < nu; ++s) {
-                    const int a = s % TV_NA, cb = s % TV_NC, ob = s % TV_NOB;
-                    const Unit x = decode_unit(P, u_begin + s, hint);
-                    // the slots' previous tiles are consumed: A by the MMAs of unit s - TV_NA, the code
-                    // tile by the converters of unit s - TV_NC and, for an ra unit (whose B operand TMA
-                    // writes), B by the MMAs of unit s - TV_NOB
-                    bool ok = s < TV_NA || tc::mbar_wait(&s_emptya[a], ((s / TV_NA) - 1) & 1);
-                    if (ok && s >= TV_NC) ok = tc::mbar_wait(&s_emptyc[cb], ((s / TV_NC) - 1) & 1);
-                    if (ok && x.kind == 1 && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TV_NOB) / TV_NOB) & 1);
-                    if (!ok) {
-                        s_err = 11;
-                        break;
-                    }
-                    const int k0 = s_act[x.q] * TV_K;
-                    tc::mbar_expect_tx(&s_fulla[a], T::RAW_A);
-                    tc::tma_load_2d(raw0 + (size_t)a * T::ASTRIDE, &tm_d, k0, 0, &s_fulla[a]);
+            }
+            bool ok = true;
+            for (int s0 = 0; s0 < nu && ok; s0 += 32) {
+                int kind = 0, ax = 0, cy = 0, cz = 0;
+                if (s0 + lane < nu) {
+                    const Unit x = decode_unit_bs(P, u_begin + s0 + lane);
+                    const int st = s_act[x.q];
+                    kind = x.kind;
+                    ax = st * TV_K;
                     if (x.kind == 0) {
-                        tc::mbar_expect_tx(&s_fullc[cb], T::RAW_C);
-                        tc::tma_load_2d(raw0 + T::C0 + (size_t)cb * T::RAW_C, &tm_codes, x.tile * TV_N, ls + k0,
-                                        &s_fullc[cb]);
+                        // one contiguous 16 KB: half st % 2 of code block (st / 2, tile)
+                        cy = (st & 1) * TV_K;
+                        cz = (cblk + (st >> 1)) * P.nvt + x.tile;
                     } else {
-                        // four boxes of 64 rows of U x 64 positions: MN atoms 8 KB apart
-                        unsigned char *bo = bop0 + (size_t)ob * T::BOP;
-                        tc::mbar_expect_tx(&s_fullc[cb], T::BOP);
-    #pragma unroll
-                        for (int h = 0; h < 4; ++h)
-                            tc::tma_load_2d(bo + h * 8192, &tm_u, x.tile * TV_N + 64 * h, x.term * D.p + ls + k0,
-                                            &s_fullc[cb]);
+                        // four boxes of 64 rows of U x 64 positions from row 256 tile, term's plane
+                        cy = x.tile * TV_N;
+                        cz = x.term * D.p + ls + ax;
                     }
+                }
+                const int m = min(32, nu - s0);
+                for (int i = 0; i < m; ++i) {
+                    const int s = s0 + i;
+                    const int kd = __shfl_sync(0xffffffffu, kind, i), k0 = __shfl_sync(0xffffffffu, ax, i);
+                    const int y = __shfl_sync(0xffffffffu, cy, i), z = __shfl_sync(0xffffffffu, cz, i);
+                    if (lane == 0) {
+                        const int a = s % TV_NA, cb = s % TV_NC, ob = s % TV_NOB;
+                        // the slots' previous tiles are consumed: A by the MMAs of unit s - TV_NA, the
+                        // code tile by the converters of unit s - TV_NC and, for an ra unit (whose B
+                        // operand TMA writes), B by the MMAs of unit s - TV_NOB
+                        ok = s < TV_NA || tc::mbar_wait(&s_emptya[a], ((s / TV_NA) - 1) & 1);
+                        if (ok && s >= TV_NC) ok = tc::mbar_wait(&s_emptyc[cb], ((s / TV_NC) - 1) & 1);
+                        if (ok && kd == 1 && s >= TV_NOB) {
+                            // a parity wait for the MMAs of unit s - NOB is only sound once those of
+                            // s - 2 NOB are complete (else the barrier may be a whole phase behind);
+                            // with more A slots than 2 NOB nothing else guarantees that, so wait for
+                            // them on their A slot first
+                            if (TV_NA > 2 * TV_NOB && s >= 2 * TV_NOB)
+                                ok = tc::mbar_wait(&s_emptya[(s - 2 * TV_NOB) % TV_NA], ((s - 2 * TV_NOB) / TV_NA) & 1);
+                            if (ok) ok = tc::mbar_wait(&s_opfree[ob], ((s - TV_NOB) / TV_NOB) & 1);
+                        }
+                        if (!ok) {
+                            s_err = 11;
+                        } else {
+                            tc::mbar_expect_tx(&s_fulla[a], T::RAW_A);
+                            tc::tma_load_2d(raw0 + (size_t)a * T::ASTRIDE, &tm_d, k0, 0, &s_fulla[a]);
+                            if (kd == 0) {
+                                tc::mbar_expect_tx(&s_fullc[cb], T::RAW_C);
+                                tc::tma_load_3d(raw0 + T::C0 + (size_t)cb * T::RAW_C, &tm_codes, 0, y, z, &s_fullc[cb]);
+                            } else {
+                                unsigned char *bo = bop0 + (size_t)ob * T::BOP;   // MN atoms 8 KB apart
+                                tc::mbar_expect_tx(&s_fullc[cb], T::BOP);
+    #pragma unroll
+                                for (int h = 0; h < 4; ++h)
+                                    tc::tma_load_2d(bo + h * 8192, &tm_u, y + 64 * h, z, &s_fullc[cb]);
+                            }
+                        }
+                    }
+                    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                    if (!ok) break;
                 }
             }
         } else if (warp == TV_WARP_MMA) {
             if (lane == 0) {
-                const uint32_t idesc = tc::idesc_bf16_bmn(128, TV_N);
+                const uint32_t idesc = tc::idesc_bf16_bmn(TV_M, TV_N);
                 int hint = 0, seg = -1, pkind = -1, ptile = -1;
                 bool ok = true;
                 for (int s = 0; s < nu && ok; ++s) {
@@ -521,9 +598,13 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 }
             }
         } else {
-            // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. (accumulator
-            // rows) for all 256 columns and stores rows < 3 * chains to the segment's slot of vpart
-            const int qd = warp & 3, row = 32 * qd + lane;
+            // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. for all 256
+            // columns (an M = 64 accumulator keeps rows 16q .. 16q+15 in lanes 32q .. 32q+15) and stores
+            // rows < 3 * chains to the segment's slot of vpart
+            const int qd = warp & 3, row = lane < 16 ? 16 * qd + lane : T::ROWS;
+            float *stg = reinterpret_cast<float *>(raw0 + T::STG0);
+            // the centring term first: the reductions need it, the first segment takes several units
+            update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);
             int hint = 0, seg = -1, pkind = -1, ptile = -1;
             for (int s = 0; s <= nu; ++s) {
                 Unit x;
@@ -537,13 +618,14 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     if (!ok) s_err = 15;
                     tc::fence_after_sync();
                     const int tg = pkind == 0 ? ptile : P.nvt + ptile;
-                    // per 32 columns: rows to shared memory, then hi + mid + lo per chain to the slot
+                    // all 256 columns of the rows in use to the staging buffer (32 at a time), then
+                    // hi + mid + lo per chain to the slot in one coalesced pass
                     float *dst = D.vpart + (size_t)(tg + blockIdx.x) * CT * TV_N;
                     const int t = tid - 32 * TV_WARP_EPI;
                     const uint32_t ta = tm + 256 * (seg & 1) + ((uint32_t)(32 * qd) << 16);
+                    if (ok && 16 * qd < T::ROWS) {
     #pragma unroll 1
-                    for (int j = 0; j < TV_N / 32; ++j) {
-                        if (ok && 32 * qd < T::ROWS) {
+                        for (int j = 0; j < TV_N / 32; ++j) {
                             float v0[8], v1[8], v2[8], v3[8];
                             tc::tmem_ld8(ta + 32 * j, v0);
                             tc::tmem_ld8(ta + 32 * j + 8, v1);
@@ -551,22 +633,22 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                             tc::tmem_ld8(ta + 32 * j + 24, v3);
                             tc::tmem_wait_ld();
                             if (row < T::ROWS) {
+                                float *sr = stg + row * (TV_N + 1) + 32 * j;
     #pragma unroll
                                 for (int e = 0; e < 8; ++e) {
-                                    s_stage[row][e] = v0[e];
-                                    s_stage[row][8 + e] = v1[e];
-                                    s_stage[row][16 + e] = v2[e];
-                                    s_stage[row][24 + e] = v3[e];
+                                    sr[e] = v0[e];
+                                    sr[8 + e] = v1[e];
+                                    sr[16 + e] = v2[e];
+                                    sr[24 + e] = v3[e];
                                 }
                             }
                         }
-                        asm volatile("bar.sync 1, 128;" ::: "memory");
-                        for (int idx = t; idx < CT * 32; idx += 128) {
-                            const int cc = idx >> 5, col = idx & 31;
-                            dst[cc * TV_N + 32 * j + col] =
-                                (s_stage[cc][col] + s_stage[CT + cc][col]) + s_stage[2 * CT + cc][col];
-                        }
-                        asm volatile("bar.sync 1, 128;" ::: "memory");
+                    }
+                    asm volatile("bar.sync 1, 128;" ::: "memory");
+                    for (int idx = t; idx < CT * TV_N; idx += 128) {
+                        const int cc = idx >> 8, col = idx & (TV_N - 1);
+                        dst[cc * TV_N + col] = (stg[cc * (TV_N + 1) + col] + stg[(CT + cc) * (TV_N + 1) + col]) +
+                                               stg[(2 * CT + cc) * (TV_N + 1) + col];
                     }
                     __threadfence();   // the slot is read after the grid barrier
                     tc::fence_before_sync();
@@ -584,7 +666,17 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             tc::fence_after_sync();
             tc::tmem_dealloc(tm, 512);
         }
-    }   // nu > 0
+    } else if (warp >= TV_WARP_EPI) {
+        update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);   // the centring term
+    }
+    // the old values of this warp's first pair, loaded while the other CTAs finish
+    const int npair = 2 * (P.nvt + P.nra) * CT;
+    const int pr0 = blockIdx.x * NW + warp;
+    double rold[4];
+    if (pr0 < npair) {
+        const int hh = pr0 / CT;
+        update_pair_rold<CT>(D, P, hh >> 1, hh & 1, pr0 - hh * CT, N, rold);
+    }
     // every segment is in vpart once all CTAs are here; then the reductions, an equal share of the
     // (half tile, chain) pairs per CTA, one pair per warp at a time
     if (!update_grid_sync(D.ugrid, (unsigned)G)) s_err = 16;
@@ -592,10 +684,10 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
         if (tid == 0) flag_err(D, s_err);
         return;
     }
-    const int npair = 2 * (P.nvt + P.nra) * CT;
-    for (int pr = blockIdx.x * NW + warp; pr < npair; pr += G * NW) {
+    for (int pr = pr0; pr < npair; pr += G * NW) {
         const int hh = pr / CT, c = pr - hh * CT;
-        update_reduce_pair<CT>(D, P, s_bnd, G, hh >> 1, hh & 1, c, s_k0, N);
+        if (pr != pr0) update_pair_rold<CT>(D, P, hh >> 1, hh & 1, c, N, rold);
+        update_reduce_pair<CT>(D, P, s_bnd, G, hh >> 1, hh & 1, c, s_k0, N, rold);
     }
 }
 
