@@ -202,79 +202,115 @@ __device__ __forceinline__ void tile_units(const UnitPlan &P, int tg, long long 
     }
 }
 
-// The old values (r or ra) of chain c in half h of global tile tg, lane l
-// holding elements l + 32k; nothing else writes them during the update.
+// One (128-element half tile, chain) pair of the reductions: global tile tg
+// (row tiles, then ra tiles), half h, chain c, the CTAs sl..sh whose segments
+// cover the tile (sl > sh: no unit touched it, nothing changes) and the old
+// values (r or ra) of the half, lane l holding elements l + 32k.  Everything
+// here is known before the grid barrier: nothing else writes those values
+// during the update.
+struct PairJob {
+    int tg, h, c, sl, sh;
+    double rold[4];
+};
+
 template <int CT>
-__device__ __forceinline__ void update_pair_rold(const Dev &D, const UnitPlan &P, int tg, int h, int c, int N,
-                                                 double (&rold)[4])
+__device__ __forceinline__ void pair_prepare(const Dev &D, const UnitPlan &P, const int *bnd, int G, int pr, int npair,
+                                             int N, PairJob &j)
 {
+    j.tg = j.h = j.c = 0;
+    j.sl = 1;
+    j.sh = 0;
+    if (pr >= npair) return;
+    const int hh = pr / CT;
+    j.c = pr - hh * CT;
+    j.tg = hh >> 1;
+    j.h = hh & 1;
+    long long u0, u1;
+    tile_units(P, j.tg, u0, u1);
+    if (u1 <= u0) return;
+    j.sl = unit_cta(bnd, (int)u0, G);
+    j.sh = unit_cta(bnd, (int)u1 - 1, G);
     const int lane = threadIdx.x & 31;
-    const bool is_r = tg < P.nvt;
-    const int tile = is_r ? tg : tg - P.nvt;
+    const bool is_r = j.tg < P.nvt;
+    const int tile = is_r ? j.tg : j.tg - P.nvt;
     const int lim = is_r ? D.n : min(N, D.bs);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int i = tile * TV_N + h * 128 + lane + 32 * k;
-        rold[k] = 0.0;
-        if (i < lim) rold[k] = is_r ? __ldcg(D.r + (size_t)c * D.ldr + i) : __ldcg(D.ra + (size_t)c * D.ldra + i);
+        const int i = tile * TV_N + j.h * 128 + lane + 32 * k;
+        j.rold[k] = 0.0;
+        if (i < lim) j.rold[k] = is_r ? __ldcg(D.r + (size_t)j.c * D.ldr + i) : __ldcg(D.ra + (size_t)j.c * D.ldra + i);
     }
 }
 
-// Adds the segments of chain c in half h (128 elements) of global tile tg in
-// segment order and applies the update: r, its bf16 split and the 128-row
-// partial sum of r for a row tile, ra and its split for an ra tile.  Lane l
-// takes the elements l + 32k of the half; the loads of up to four segments
-// are issued together.
+// The segments of job j from CTA q0 + u (u < 4) of its range: loads only.
 template <int CT>
-__device__ __forceinline__ void update_reduce_pair(const Dev &D, const UnitPlan &P, const int *bnd, int G, int tg,
-                                                   int h, int c, const double *s_k0, int N, const double (&rold)[4])
+__device__ __forceinline__ void pair_load4(const Dev &D, const int *bnd, const PairJob &j, int q0, float (&v)[4][4])
 {
     const int lane = threadIdx.x & 31;
-    const bool is_r = tg < P.nvt;
-    const int tile = is_r ? tg : tg - P.nvt;
-    const int lim = is_r ? D.n : min(N, D.bs);
-    long long u0, u1;
-    tile_units(P, tg, u0, u1);
-    if (u1 <= u0) return;   // no unit touched this tile: nothing changed
-    const int sl = unit_cta(bnd, (int)u0, G), sh = unit_cta(bnd, (int)u1 - 1, G);
-    float acc[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) acc[k] = 0.0f;
-    for (int q0 = sl; q0 <= sh; q0 += 4) {
-        float v[4][4];
+    for (int u = 0; u < 4; ++u) {
+        const int q = q0 + u;
+        const bool ok = q <= j.sh && bnd[q] < bnd[q + 1];   // CTAs without units have no slot
+        const float *pp = D.vpart + ((size_t)(j.tg + q) * CT + j.c) * TV_N + j.h * 128 + lane;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int q = q0 + u;
-            const bool ok = q <= sh && bnd[q] < bnd[q + 1];   // CTAs without units have no slot
-            const float *pp = D.vpart + ((size_t)(tg + q) * CT + c) * TV_N + h * 128 + lane;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) v[u][k] = ok ? __ldcg(pp + 32 * k) : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) acc[k] += v[u][k];
+        for (int k = 0; k < 4; ++k) v[u][k] = ok ? __ldcg(pp + 32 * k) : 0.0f;
     }
+}
+
+// Applies the update of job j from its segment sum acc: r, its bf16 split and
+// the 128-row partial sum of r for a row tile, ra and its split for an ra tile.
+template <int CT>
+__device__ __forceinline__ void pair_finish(const Dev &D, const UnitPlan &P, const PairJob &j, const float (&acc)[4],
+                                            const double *s_k0, int N)
+{
+    const int lane = threadIdx.x & 31;
+    const bool is_r = j.tg < P.nvt;
+    const int tile = is_r ? j.tg : j.tg - P.nvt;
+    const int lim = is_r ? D.n : min(N, D.bs);
     float part = 0.0f;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int i = tile * TV_N + h * 128 + lane + 32 * k;
+        const int i = tile * TV_N + j.h * 128 + lane + 32 * k;
         if (is_r) {
-            const double rn = rold[k] + ((double)acc[k] + s_k0[c]);
+            const double rn = j.rold[k] + ((double)acc[k] + s_k0[j.c]);
             if (i < lim) {
-                const size_t o = (size_t)c * D.ldr + i;
+                const size_t o = (size_t)j.c * D.ldr + i;
                 D.r[o] = rn;
                 split_store(D.rsp, o, (size_t)D.chains * D.ldr, (float)rn);
                 part += (float)rn;
             }
         } else if (i < lim) {
-            store_ra(D, c, i, rold[k] + (double)acc[k]);
+            store_ra(D, j.c, i, j.rold[k] + (double)acc[k]);
         }
     }
     if (is_r) {
         const float ws = warp_sumf(part);
-        if (lane == 0 && 2 * tile + h < D.nr_ctas) D.rsum[(size_t)c * D.nr_ctas + 2 * tile + h] = (double)ws;
+        if (lane == 0 && 2 * tile + j.h < D.nr_ctas) D.rsum[(size_t)j.c * D.nr_ctas + 2 * tile + j.h] = (double)ws;
     }
+}
+
+// Two jobs of one warp: the segments of each are added in segment order (the
+// same order for any grouping), with the loads of both jobs issued together.
+template <int CT>
+__device__ __forceinline__ void pair_reduce2(const Dev &D, const UnitPlan &P, const int *bnd, const PairJob &ja,
+                                             const PairJob &jb, const double *s_k0, int N)
+{
+    float aa[4] = {0.0f, 0.0f, 0.0f, 0.0f}, ab[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const int na = ja.sh - ja.sl + 1, nb_ = jb.sh - jb.sl + 1, nmax = max(na, nb_);
+    for (int q0 = 0; q0 < nmax; q0 += 4) {
+        float va[4][4], vb[4][4];
+        pair_load4<CT>(D, bnd, ja, ja.sl + q0, va);
+        pair_load4<CT>(D, bnd, jb, jb.sl + q0, vb);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                aa[k] += va[u][k];
+                ab[k] += vb[u][k];
+            }
+    }
+    if (na > 0) pair_finish<CT>(D, P, ja, aa, s_k0, N);
+    if (nb_ > 0) pair_finish<CT>(D, P, jb, ab, s_k0, N);
 }
 
 // Grid-wide barrier of the G CTAs of one launch on a monotonic counter (each
@@ -581,10 +617,13 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         tc::codes_to_bf16x4(w.y, o[2], o[3]);
                         tc::codes_to_bf16x4(w.z, o[4], o[5]);
                         tc::codes_to_bf16x4(w.w, o[6], o[7]);
-                        const int r = k & 7, j0 = 2 * (c & 3);
+                        // lanes with c % 8 >= 4 store their two chunks in the other order, so that the
+                        // eight lanes of each store phase meet eight different 16-byte bank groups
+                        const int r = k & 7, j0 = 2 * (c & 3), sw = (c >> 2) & 1;
                         unsigned char *ob_ = bo + (k >> 3) * 4096 + (c >> 2) * 1024 + r * 128;
-                        *reinterpret_cast<uint4 *>(ob_ + ((j0 ^ r) << 4)) = make_uint4(o[0], o[1], o[2], o[3]);
-                        *reinterpret_cast<uint4 *>(ob_ + (((j0 + 1) ^ r) << 4)) = make_uint4(o[4], o[5], o[6], o[7]);
+                        const uint4 w0 = make_uint4(o[0], o[1], o[2], o[3]), w1 = make_uint4(o[4], o[5], o[6], o[7]);
+                        *reinterpret_cast<uint4 *>(ob_ + (((j0 + sw) ^ r) << 4)) = sw ? w1 : w0;
+                        *reinterpret_cast<uint4 *>(ob_ + (((j0 + 1 - sw) ^ r) << 4)) = sw ? w0 : w1;
                     }
                     tc::fence_async_smem();
                 } else if (!__all_sync(0xffffffffu, ok)) {
@@ -669,14 +708,12 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     } else if (warp >= TV_WARP_EPI) {
         update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);   // the centring term
     }
-    // the old values of this warp's first pair, loaded while the other CTAs finish
+    // this warp's first two pairs (pr0 and pr0 + stride) prepared while the other CTAs finish
     const int npair = 2 * (P.nvt + P.nra) * CT;
-    const int pr0 = blockIdx.x * NW + warp;
-    double rold[4];
-    if (pr0 < npair) {
-        const int hh = pr0 / CT;
-        update_pair_rold<CT>(D, P, hh >> 1, hh & 1, pr0 - hh * CT, N, rold);
-    }
+    const int pr0 = blockIdx.x * NW + warp, stride = G * NW;
+    PairJob ja, jb;
+    pair_prepare<CT>(D, P, s_bnd, G, pr0, npair, N, ja);
+    pair_prepare<CT>(D, P, s_bnd, G, pr0 + stride, npair, N, jb);
     // every segment is in vpart once all CTAs are here; then the reductions, an equal share of the
     // (half tile, chain) pairs per CTA, one pair per warp at a time
     if (!update_grid_sync(D.ugrid, (unsigned)G)) s_err = 16;
@@ -684,10 +721,12 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
         if (tid == 0) flag_err(D, s_err);
         return;
     }
-    for (int pr = pr0; pr < npair; pr += G * NW) {
-        const int hh = pr / CT, c = pr - hh * CT;
-        if (pr != pr0) update_pair_rold<CT>(D, P, hh >> 1, hh & 1, c, N, rold);
-        update_reduce_pair<CT>(D, P, s_bnd, G, hh >> 1, hh & 1, c, s_k0, N, rold);
+    for (int pr = pr0; pr < npair; pr += 2 * stride) {
+        if (pr != pr0) {
+            pair_prepare<CT>(D, P, s_bnd, G, pr, npair, N, ja);
+            pair_prepare<CT>(D, P, s_bnd, G, pr + stride, npair, N, jb);
+        }
+        pair_reduce2<CT>(D, P, s_bnd, ja, jb, s_k0, N);
     }
 }
 
