@@ -134,6 +134,34 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
         const int32_t *rt = D.rtab + (size_t)b * D.tstride + jl / 128;
         ksplit = rt[1] - rt[0];
     }
+    if (MODE == SODAGPU_FP8 || TC) {
+        // sum(r) per chain from the row-tile partial sums of the previous residual update, before
+        // the dependency wait: that update is complete once this kernel runs, because the rhs
+        // kernel lets it launch only after its own dependency wait.  256/CT threads per chain
+        // take interleaved tiles, loaded 16 at a time in one batch, then added in part order
+        constexpr int PARTS = 256 / CT;
+        const int cc = tid / PARTS, part = tid % PARTS;
+        double a = 0.0;
+        for (int q0 = part; q0 < D.nr_ctas; q0 += 16 * PARTS) {
+            double v[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const int q = q0 + u * PARTS;
+                v[u] = q < D.nr_ctas ? __ldcg(D.rsum + (size_t)cc * D.nr_ctas + q) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 16; ++u) a += v[u];
+        }
+        s_k[tid] = a;
+    }
+    __syncthreads();
+    if ((MODE == SODAGPU_FP8 || TC) && tid < CT) {
+        constexpr int PARTS = 256 / CT;
+        double tt = 0.0;
+        for (int q = 0; q < PARTS; ++q) tt += s_k[tid * PARTS + q];
+        s_rs[tid] = tt;
+    }
+    __syncthreads();
     tc::pdl_trigger();
     tc::pdl_wait();
     // the rhs partial sums of all splits, added in split order (the tensor-core rhs
@@ -170,32 +198,6 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
             }
         }
     }
-    if (MODE == SODAGPU_FP8 || TC) {
-        // sum(r) per chain from the row-tile partial sums: 256/CT threads per chain take
-        // interleaved tiles, loaded 16 at a time in one batch, then added in part order
-        constexpr int PARTS = 256 / CT;
-        const int cc = tid / PARTS, part = tid % PARTS;
-        double a = 0.0;
-        for (int q0 = part; q0 < D.nr_ctas; q0 += 16 * PARTS) {
-            double v[16];
-#pragma unroll
-            for (int u = 0; u < 16; ++u) {
-                const int q = q0 + u * PARTS;
-                v[u] = q < D.nr_ctas ? __ldcg(D.rsum + (size_t)cc * D.nr_ctas + q) : 0.0;
-            }
-#pragma unroll
-            for (int u = 0; u < 16; ++u) a += v[u];
-        }
-        s_k[tid] = a;
-    }
-    __syncthreads();
-    if ((MODE == SODAGPU_FP8 || TC) && tid < CT) {
-        constexpr int PARTS = 256 / CT;
-        double tt = 0.0;
-        for (int q = 0; q < PARTS; ++q) tt += s_k[tid * PARTS + q];
-        s_rs[tid] = tt;
-    }
-    __syncthreads();
     double delta = 0.0;
     if (snp >= 0) {
         if (TC) xr = xr * (inv != 0.0 ? inv : 1.0) + x0 * s_rs[c];   // columns with sd = 0 carry U unscaled
@@ -268,8 +270,10 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     extern __shared__ __align__(16) unsigned char smem[];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    tc::pdl_trigger();
+    // the draw kernel launches only after this wait (its prologue reads what the previous
+    // residual update wrote)
     tc::pdl_wait();
+    tc::pdl_trigger();
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
     const int mt = blockIdx.x / ksplit, ks = blockIdx.x % ksplit;

@@ -27,7 +27,9 @@
 //           and commits their completion, which frees the buffers.
 // With programmatic dependent launch the prologue (barriers, tensor memory,
 // the first A tiles, which are constant) overlaps the previous kernel; the
-// residual splits are read after it completes.  The accumulator rows go to
+// residual splits are read after it completes.  Each thread lets the draw
+// kernel launch only after its own dependency wait, so that the draw's
+// prologue may read what the previous residual update wrote.  The accumulator rows go to
 // rpx as FP32 partial sums, one slot per K split, added by k_draw.
 #pragma once
 #include <cuda.h>
@@ -125,7 +127,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         s_err = 0;
     }
     if (warp == TC_WARP_MMA) tc::tmem_alloc(&s_tmem, 512);   // accumulator 0-63, codes operands 64-319
-    tc::pdl_trigger();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int pre = ns < NS ? ns : NS;
             for (int s = 0; s < pre; ++s) load_a(s);
             tc::pdl_wait();
+            tc::pdl_trigger();
             for (int s = 0; s < pre; ++s) load_b(s);
             for (int s = pre; s < ns; ++s) {
                 // the buffer's previous stage has been consumed
@@ -179,9 +181,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         } else {
             tc::pdl_wait();
+            tc::pdl_trigger();
         }
     } else if (warp == TC_WARP_MMA) {
         tc::pdl_wait();
+        tc::pdl_trigger();
         if (lane == 0 && ns > 0) {
             const uint32_t idesc = tc::idesc_bf16(TC_TM, NB);
             for (int s = 0; s < ns; ++s) {
@@ -219,6 +223,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     } else {
         tc::pdl_wait();
+        tc::pdl_trigger();
         // converters: genotype stages -> bf16 codes in tensor memory; augmenting stages
         // need no conversion (they only release the buffer after its TMA completed)
         for (int s = 0; s < ns; ++s) {
