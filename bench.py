@@ -350,6 +350,70 @@ def cpu_sample(args, steps=1, warmup=0):
             "seconds_per_iteration": t_iter}
 
 
+def workload_c5(args):
+    """Config 5 on one GPU: BayesRc, 16 chains on shared genotypes, three annotation classes (0.1, 0.3, 0.6),
+    4-class mixtures, n=50,000, p=1,000,000, subset 1000.  Prints its own JSON line: iterations x chains / s
+    of the batched FP8 sampler (inputs resident, CUDA-event timed) and the error of one chain against an FP64
+    run of the same chain.  The default run (config 3) is unchanged."""
+    import torch
+    from sodabayes_gb300 import JobOptions, SodaJob, make_config, synth
+    spec = synth.CONFIGS["c5"]
+    groups = synth.annotation_groups(spec.p)
+    t0 = time.perf_counter()
+    codes, y, _ = synth.make_device(spec)
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    vy = float(np.var(y))
+
+    def job_of(prec, chains, seed):
+        o = JobOptions(method="BayesRc", nmix=4, mix=(0.0, 1e-4, 1e-3, 1e-2), ngroup=3, numit=100000, burnin=0,
+                       blocksize=1000, seed=seed, precision=prec, chains=chains, scale_va=0.5 * vy, df_va=4.0,
+                       scale_ve=0.5 * vy, df_ve=4.0)
+        job = SodaJob(make_config(spec.n, spec.p, o))
+        job.load_genotypes(device_ptr=codes.data_ptr())
+        job.load_pheno(y)
+        job.set_groups(groups)
+        t = time.perf_counter()
+        job.build_z()
+        job.init_chains()
+        torch.cuda.synchronize()
+        return job, time.perf_counter() - t
+
+    C, K = args.chains, args.steps
+    job, t_setup = job_of("fp8", C, 77)
+    job.run(args.settle + args.warmup)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        job.run(K)
+        torch.cuda.synchronize()
+    dev_ms = job.timings()[2]
+    free, total = torch.cuda.mem_get_info()
+    used_gb = (total - free) / 1e9
+    job.close()
+    E = args.error_iters
+    g = {}
+    for prec in ("fp64", "fp8"):
+        job, _ = job_of(prec, 1, 99)
+        job.run(E)
+        st = job.state(0)
+        g[prec] = (st["g"], st["cls"], st["vare"])
+        job.close()
+    d = g["fp8"][0] - g["fp64"][0]
+    line = {"workload": "config 5: SODA BayesRc n=50000 p=1000000 subset 1000 (1000 subsets), 16 chains on shared "
+                        "genotypes, 3 annotation classes (0.1, 0.3, 0.6), mixture (0, 1e-4, 1e-3, 1e-2), LD generator "
+                        "(100-SNP AR(1) blocks rho=0.8, maf~U(0.01,0.5)), 5000 causal effects, h2=0.5",
+            "metric": "SODA Gibbs iters/s x chains", "value": K * C / (dev_ms / 1000.0), "unit": UNIT,
+            "ms_per_step": dev_ms / K, "chains": C, "steps": K, "warmup": args.warmup,
+            "settle_iterations": args.settle, "precision": "fp8", "data": "synthetic (seeded generator of config 5)",
+            "error_vs_fp64": {"iterations": E, "g_rel_rms": float(np.sqrt(np.mean(d ** 2)) /
+                                                                  max(1e-300, np.sqrt(np.mean(g["fp64"][0] ** 2)))),
+                              "class_agreement": float(np.mean(g["fp8"][1] == g["fp64"][1])),
+                              "vare_rel": float(abs(g["fp8"][2] / g["fp64"][2] - 1))},
+            "device_gb_in_use_fp8_job": round(used_gb, 1), "generate_s": round(t_gen, 2),
+            "z_build_and_init_s": round(t_setup, 2), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def profile_case(args):
     """Small case for kernel captures: same per-subset shape as the workload."""
     import torch
@@ -401,9 +465,16 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="n=20000, p=20000 case of the same subset shape, for ncu captures")
     ap.add_argument("--precision", default="fp8", choices=["fp64", "fp32", "fp8"], help="--profile-case only")
+    ap.add_argument("--workload", default="c3", choices=["c3", "c5"],
+                    help="c5: config 5 (BayesRc, n=50000, p=1000000, 16 chains) on its own JSON line")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)
+        return
+    if args.workload == "c5":
+        if args.warmup < 3:
+            args.warmup = 3
+        workload_c5(args)
         return
     if args.warmup < 3:
         args.warmup = 3

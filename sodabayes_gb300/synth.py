@@ -107,7 +107,24 @@ CONFIGS = {
                     mixture=(1e-4, 1e-3, 1e-2), seed=20260002),
     "c3": SynthSpec(n=20000, p=500000, maf_lo=0.01, maf_hi=0.5, ld_block=50, rho=0.7, ncausal=2000, h2=0.5,
                     seed=20260003),
+    # BayesRc, 16 chains on shared genotypes: 100-SNP LD blocks, rho = 0.8, 5000 causal effects from the
+    # non-zero mixture components, three annotation classes (annotation_groups)
+    "c5": SynthSpec(n=50000, p=1000000, maf_lo=0.01, maf_hi=0.5, ld_block=100, rho=0.8, ncausal=5000, h2=0.5,
+                    mixture=(1e-4, 1e-3, 1e-2), seed=20260005),
 }
+
+
+def annotation_groups(p: int, proportions=(0.1, 0.3, 0.6), seed: int = 20260105) -> np.ndarray:
+    """SNP annotation classes 1..len(proportions) (the group file of BayesRc),
+    in the given proportions, assigned at random positions."""
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(p)
+    grp = np.empty(p, dtype=np.int32)
+    edges = np.round(np.cumsum((0.0,) + tuple(proportions)) * p).astype(np.int64)
+    edges[-1] = p
+    for g in range(len(proportions)):
+        grp[order[edges[g]:edges[g + 1]]] = g + 1
+    return grp
 
 
 def make_device(spec: SynthSpec, device="cuda"):
