@@ -1,0 +1,157 @@
+"""The mbarrier protocol of the tensor-core rhs (k_rhs_tc in
+sodabayes_gb300/csrc/rhs_tc.cuh), as a model run on the CPU, like
+test_update_protocol.py for the residual update.
+
+Roles: the TMA thread loads each stage's A and B tiles into raw buffer
+s % NS (one barrier phase per stage); the converter warps widen a genotype
+stage's codes into tensor-memory operand s % NOB; the MMA thread reads that
+operand and the stage's B tile (genotype stages) or both raw tiles (U stages,
+which follow the genotype stages).  A raw buffer is free once the converters
+and the MMAs of its stage are done (one barrier, converter warps + MMA
+commit); an operand once the MMAs of its stage completed.
+
+Checked for every number of stages and genotype/U split, for the kernel's
+NS (computed from its buffer sizes for 4, 8 and 16 chains) and NOB, under
+random interleavings: no parity wait returns a phase early, and no raw
+buffer or operand is overwritten while a reader of its previous contents is
+pending."""
+import os
+import random
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "sodabayes_gb300", "csrc", "rhs_tc.cuh")
+
+
+def _consts():
+    txt = open(SRC).read()
+    nob = int(re.search(r"constexpr int TC_NOB = (\d+);", txt).group(1))
+    tm = int(re.search(r"constexpr int TC_TM = (\d+);", txt).group(1))
+    kc = int(re.search(r"constexpr int TC_KC = (\d+);", txt).group(1))
+    ns = {}
+    for ct in (4, 8, 16):
+        nb = ((3 * ct + 15) // 16) * 16
+        raw = tm * kc + nb * kc * 2
+        ns[ct] = min(8, (220 * 1024 - 1024) // raw)
+    return nob, ns
+
+
+class Unsound(AssertionError):
+    pass
+
+
+class Bar:
+    def __init__(self):
+        self.k = 0
+
+    def ready(self, i):
+        ok = (self.k & 1) != (i & 1)
+        if ok and self.k < i + 1:
+            raise Unsound("parity wait for phase %d returned with %d phases complete" % (i, self.k))
+        return ok
+
+
+def run(ns_total, nck, NS, NOB, seed, skip_opfree=False):
+    rnd = random.Random(seed)
+    full = [Bar() for _ in range(NS)]
+    empty = [Bar() for _ in range(NS)]   # converters + MMA commit: the model counts two arrivals per phase
+    empty_arr = [0] * NS
+    conv = [Bar() for _ in range(NOB)]
+    opfree = [Bar() for _ in range(NOB)]
+    raw_owner = [None] * NS
+    op_owner = [None] * NOB
+    conv_done, mma_done = set(), set()
+    pending = []
+
+    def empty_arrive(buf):
+        empty_arr[buf] += 1
+        if empty_arr[buf] == 2:
+            empty_arr[buf] = 0
+            empty[buf].k += 1
+
+    def producer():
+        for s in range(ns_total):
+            buf = s % NS
+            if s >= NS:
+                yield empty[buf], s // NS - 1
+            prev = raw_owner[buf]
+            if prev is not None and not (prev in conv_done and prev in mma_done):
+                raise Unsound("raw buffer %d overwritten by stage %d while stage %d is read" % (buf, s, prev))
+            raw_owner[buf] = s
+            pending.append(lambda buf=buf: setattr(full[buf], "k", full[buf].k + 1))
+
+    def converter():
+        for s in range(ns_total):
+            buf, ob = s % NS, s % NOB
+            yield full[buf], s // NS
+            if s < nck:
+                if s >= NOB and not skip_opfree:
+                    yield opfree[ob], (s - NOB) // NOB
+                prev = op_owner[ob]
+                if prev is not None and prev not in mma_done:
+                    raise Unsound("operand %d overwritten by stage %d while stage %d's MMAs read it" % (ob, s, prev))
+                op_owner[ob] = s
+                conv[ob].k += 1
+            conv_done.add(s)
+            empty_arrive(buf)
+
+    def mma():
+        for s in range(ns_total):
+            buf, ob = s % NS, s % NOB
+            if s < nck:
+                yield conv[ob], s // NOB
+            else:
+                yield full[buf], s // NS
+
+            def commit(s=s, buf=buf, ob=ob):
+                mma_done.add(s)
+                if s < nck:
+                    opfree[ob].k += 1
+                empty_arrive(buf)
+            pending.append(commit)
+
+    roles = [producer(), converter(), mma()]
+    waits = [next(r, None) for r in roles]
+    steps = 0
+    while any(w is not None for w in waits) or pending:
+        steps += 1
+        assert steps < 100000
+        choices = [("async", j) for j in range(len(pending))]
+        for i, w in enumerate(waits):
+            if w is not None and w[0].ready(w[1]):
+                choices.append(("role", i))
+        if not choices:
+            raise AssertionError("deadlock")
+        kind, j = rnd.choice(choices)
+        if kind == "async":
+            pending.pop(j)()
+        else:
+            waits[j] = next(roles[j], None)
+
+
+def test_rhs_protocol_is_sound():
+    nob, ns = _consts()
+    rnd = random.Random(3)
+    t = 0
+    for ct, NS in ns.items():
+        assert NS >= 4
+        for _ in range(150):
+            total = rnd.randint(1, 48)
+            nck = rnd.randint(0, total)
+            run(total, nck, NS, nob, seed=t)
+            t += 1
+
+
+def test_rhs_protocol_model_catches_a_missing_wait():
+    """The mistake planted in the model: converters that do not wait for the
+    MMAs of the operand's previous stage."""
+    nob, ns = _consts()
+    rnd = random.Random(5)
+    caught = 0
+    for t in range(200):
+        total = rnd.randint(nob + 1, 48)
+        try:
+            run(total, total, ns[16], nob, seed=t, skip_opfree=True)
+        except Unsound:
+            caught += 1
+    assert caught > 0
