@@ -260,24 +260,14 @@ def bench_ours(args, rank, ws):
     job.close()
     res["fp32_plain"] = {"value": K / (fp32_ms / 1000.0), "ms_per_step": fp32_ms / K, "chains": 1}
 
-    # ---- error against an FP64 run of the same chain ------------------------------
-    E = args.error_iters
-    g = {}
-    for prec in ("fp64", "fp32", "fp8"):
-        job = _make_job(spec, codes, y, prec, 1, 99)
-        job.run(E)
-        s = job.state(0)
-        g[prec] = (s["g"], s["cls"], s["mu"], s["vare"])
-        job.close()
-    err = {}
-    for prec in ("fp32", "fp8"):
-        d = g[prec][0] - g["fp64"][0]
-        nz = g["fp64"][0] != 0
-        err[prec] = {"g_rel_rms": float(np.sqrt(np.mean(d ** 2)) / max(1e-300, np.sqrt(np.mean(g["fp64"][0] ** 2)))),
-                     "class_agreement": float(np.mean(g[prec][1] == g["fp64"][1])),
-                     "vare_rel": float(abs(g[prec][3] / g["fp64"][3] - 1)),
-                     "nonzero_effects_fp64": int(nz.sum())}
-    res["error_vs_fp64"] = {"iterations": E, **err}
+    # ---- error against FP64 runs of the same chains ---------------------------------
+    # The headline's own kernels: the FP8 context with the headline's chain count runs on the
+    # tensor cores (k_rhs_tc / k_draw / k_update_tc); chains 0 and 1 are compared with an FP64
+    # context of two chains (same seed: every draw uses the same counter-based uniforms).
+    res["error_vs_fp64"] = error_vs_fp64(spec, codes, y, C, args.error_iters)
+    res["conditional_check"] = conditional_check_c3(codes, y, C)
+    if args.accept_iters > 0:
+        res["acceptance"] = acceptance(spec, codes, y, C, args.accept_burnin, args.accept_iters)
 
     # ---- e2e: the whole job through the C ABI, host buffers in and out ------------
     host_codes = torch.empty(codes.shape, dtype=torch.int8, pin_memory=True)
@@ -307,6 +297,159 @@ def bench_ours(args, rank, ws):
                               "posterior means download"}
     del outs
     return res
+
+
+def _err(a, b):
+    d = a["g"] - b["g"]
+    return {"g_rel_rms": float(np.sqrt(np.mean(d ** 2)) / max(1e-300, np.sqrt(np.mean(b["g"] ** 2)))),
+            "class_agreement": float(np.mean(a["cls"] == b["cls"])),
+            "vare_rel": float(abs(a["vare"] / b["vare"] - 1))}
+
+
+def error_vs_fp64(spec, codes, y, C, E):
+    """State after E iterations of the FP8 context with C chains (tensor-core kernels when C is 4, 8
+    or 16) and of the plain FP32 context (1 chain) against FP64 contexts of the same seed."""
+    st = {}
+    for prec, chains in (("fp64", 2), ("fp8", C), ("fp32", 1)):
+        job = _make_job(spec, codes, y, prec, chains, 99)
+        job.run(E)
+        st[prec] = [job.state(c) for c in range(min(chains, 2))]
+        job.close()
+    out = {"iterations": E,
+           "fp8": {"kernels": "k_rhs_tc<%d>, k_draw<fp8,%d,tc>, k_update_tc<%d> (the headline's)" % (C, C, C)
+                   if C in (4, 8, 16) else "k_rhs<fp8,%d>, k_draw, k_update<fp8,%d>" % (C, C),
+                   "chains_compared": [0, 1]},
+           "fp32": {"kernels": "k_rhs<fp32,1>, k_draw<fp32,1>, k_update<fp32,1> (the plain FP32 path)",
+                    "chains_compared": [0]}}
+    for c in range(min(C, 2)):
+        out["fp8"]["chain%d" % c] = _err(st["fp8"][c], st["fp64"][c])
+    out["fp32"]["chain0"] = _err(st["fp32"][0], st["fp64"][0])
+    out["nonzero_effects_fp64"] = int(np.sum(st["fp64"][0]["g"] != 0))
+    return out
+
+
+def conditional_check_c3(codes, y, C, nsub=2):
+    """One subset of one loaded state (a settled-looking sparse state, 1% of SNPs in the model) at the
+    config-3 subset shape, FP8 with C chains against FP64 with C chains: right-hand sides, conditional
+    means, class draws with their decision margins, residual identity after the update.  The first
+    nsub subsets of the workload's genotypes (n = 20,000) serve as the data."""
+    from sodabayes_gb300 import precision
+    G = np.asfortranarray(codes[:nsub * BLOCKSIZE].cpu().numpy().T)
+    jobs = {}
+    for prec in ("fp8", "fp64"):
+        from sodabayes_gb300 import JobOptions, SodaJob, make_config
+        cfg = make_config(G.shape[0], G.shape[1], JobOptions(method=METHOD, numit=100, burnin=0,
+                                                             blocksize=BLOCKSIZE, seed=4242, precision=prec,
+                                                             chains=C, **PRIORS))
+        job = SodaJob(cfg)
+        job.load_genotypes(G)
+        job.load_pheno(y)
+        job.build_z()
+        job.init_chains()
+        jobs[prec] = job
+    vare = 0.5 * float(np.var(y))
+    states = [precision.sparse_state(G, y, None, 2, (0.0, 1.0), 1.0, vare, 0.01, np.array([[0.99, 0.01]]), None,
+                                     seed=1000 + c, naind=BLOCKSIZE) for c in range(C)]
+    try:
+        res = precision.conditional_check(jobs["fp8"], jobs["fp64"], G, y, 0, 7, states, tau=1e-4)
+    finally:
+        for j in jobs.values():
+            j.close()
+    res["shape"] = "n=%d, subset %d, %d chains, BayesCpi" % (G.shape[0], BLOCKSIZE, C)
+    dis = res.pop("disagreements", [])
+    res["disagreement_margins"] = [round(x["margin"], 9) for x in dis][:20]
+    return res
+
+
+def _batch_means(x):
+    """(mean, Monte-Carlo standard error, effective sample size) of a trace by
+    non-overlapping batch means with batches of floor(sqrt(N))."""
+    x = np.asarray(x, dtype=np.float64)
+    n = len(x)
+    b = max(1, int(np.sqrt(n)))
+    nb = n // b
+    bm = x[:nb * b].reshape(nb, b).mean(axis=1)
+    var_bm = b * bm.var(ddof=1) if nb > 1 else 0.0
+    se = float(np.sqrt(var_bm / n)) if var_bm > 0 else 0.0
+    v = x.var(ddof=1)
+    ess = float(n * v / var_bm) if var_bm > 0 else float(n)
+    return float(x.mean()), se, min(ess, float(n))
+
+
+def acceptance(spec, codes, y, C, burn, keep):
+    """Free-running config-3 chains (the benchmark spec acceptance): the FP8 sampler with C chains, the plain
+    FP32 path (1 chain) and two FP64 runs (1 chain each, seeds A and B: the Monte-Carlo floor of two
+    independent FP64 runs).  Posterior means of the SNP effects and GEBVs (compute_dgv,
+    utilities.f90:616-622, of the posterior means, models.f90:576-598), pi = included / p, the model's
+    genetic variance share h2 = sum_k n_k gamma_k s2g / (that + s2e) and s2e per kept iteration with
+    batch-means standard errors, and effective samples per second of mu, s2e and s2g."""
+    seeds = {"fp64": 77, "fp64_seedB": 78, "fp8": 77, "fp32": 77}
+    runs = {}
+    for name, prec, chains in (("fp64", "fp64", 1), ("fp64_seedB", "fp64", 1), ("fp8", "fp8", C),
+                               ("fp32", "fp32", 1)):
+        from sodabayes_gb300 import JobOptions, SodaJob, make_config
+        opts = JobOptions(method=METHOD, numit=burn + keep, burnin=burn, blocksize=BLOCKSIZE, seed=seeds[name],
+                          precision=prec, chains=chains, **PRIORS)
+        job = SodaJob(make_config(spec.n, spec.p, opts))
+        job.load_genotypes(device_ptr=codes.data_ptr())
+        job.load_pheno(y)
+        job.build_z()
+        job.init_chains()
+        job.run(burn)
+        rows = []
+        job.run(keep, trace=lambda r: rows.append((r.chain, r.mu, r.vare, r.vara, r.included)))
+        dev_s = job.timings()[2] / 1000.0
+        res = [job.results(c) for c in range(chains)]
+        gebv = [job.compute_dgv(r["mu_store"], r["gstore"]) for r in res[:2]]
+        avg = np.mean([r["gstore"] for r in res], axis=0)
+        mu_avg = float(np.mean([r["mu_store"] for r in res]))
+        gebv_avg = job.compute_dgv(mu_avg, avg) if chains > 1 else gebv[0]
+        job.close()
+        tr = np.array(rows)
+        per = {}
+        ess = {"mu": 0.0, "vare": 0.0, "vara": 0.0}
+        for c in range(chains):
+            t = tr[tr[:, 0] == c]
+            for k, col in (("mu", 1), ("vare", 2), ("vara", 3)):
+                ess[k] += _batch_means(t[:, col])[2]
+            vg = t[:, 3] * t[:, 4]                   # BayesCpi: included SNPs x effect variance
+            per[c] = {"pi": _batch_means(t[:, 4] / spec.p), "h2": _batch_means(vg / (vg + t[:, 2])),
+                      "vare": _batch_means(t[:, 2])}
+        runs[name] = {"g": [r["gstore"] for r in res[:2]], "g_avg": avg, "gebv": gebv, "gebv_avg": gebv_avg,
+                      "per": per, "ess_per_s": {k: v / dev_s for k, v in ess.items()}, "device_s": dev_s,
+                      "chains": chains}
+
+    def rel_rms(a, b):
+        return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
+
+    ref = runs["fp64"]
+    out = {"burn_in": burn, "kept": keep, "seeds": seeds,
+           "targets": {"effects_rel_rms_max": 1e-3, "gebv_corr_min": 0.9999, "pi_h2_vare_within_z": 3.0}}
+    for name in ("fp8", "fp32", "fp64_seedB"):
+        r = runs[name]
+        e = {"effects_rel_rms_chain0": rel_rms(r["g"][0], ref["g"][0]),
+             "gebv_corr_chain0": float(np.corrcoef(r["gebv"][0], ref["gebv"][0])[0, 1])}
+        if r["chains"] > 1:
+            e["effects_rel_rms_mean_of_chains"] = rel_rms(r["g_avg"], ref["g"][0])
+            e["gebv_corr_mean_of_chains"] = float(np.corrcoef(r["gebv_avg"], ref["gebv"][0])[0, 1])
+        z = {}
+        for k in ("pi", "h2", "vare"):
+            m, se = r["per"][0][k][0], r["per"][0][k][1]
+            m0, se0 = ref["per"][0][k][0], ref["per"][0][k][1]
+            z[k] = {"mean": m, "se": se, "fp64_mean": m0, "fp64_se": se0,
+                    "z": float(abs(m - m0) / max(1e-300, np.sqrt(se * se + se0 * se0)))}
+        e["chain0_vs_fp64"] = z
+        e["pass"] = {"effects": e["effects_rel_rms_chain0"] <= 1e-3, "gebv": e["gebv_corr_chain0"] >= 0.9999,
+                     "pi_h2_vare": all(v["z"] <= 3.0 for v in z.values())}
+        e["ess_per_s"] = r["ess_per_s"]
+        e["chains"] = r["chains"]
+        out[name] = e
+    out["fp64"] = {"ess_per_s": ref["ess_per_s"], "chains": 1}
+    out["note"] = ("fp64_seedB is a second FP64 chain with another seed: its distance from the FP64 run is the "
+                   "Monte-Carlo floor of the comparison.  Same-seed chains share every uniform, so their "
+                   "trajectories coincide until the first class decision whose margin is below the FP32 "
+                   "rounding of the draw; after that they differ by Monte-Carlo error.")
+    return out
 
 
 def cpu_sample(args, steps=1, warmup=0):
@@ -391,24 +534,51 @@ def workload_c5(args):
     used_gb = (total - free) / 1e9
     job.close()
     E = args.error_iters
-    g = {}
-    for prec in ("fp64", "fp8"):
-        job, _ = job_of(prec, 1, 99)
+    st = {}
+    for prec, chains in (("fp64", 2), ("fp8", C)):
+        job, _ = job_of(prec, chains, 99)
         job.run(E)
-        st = job.state(0)
-        g[prec] = (st["g"], st["cls"], st["vare"])
+        st[prec] = [job.state(c) for c in range(2)]
         job.close()
-    d = g["fp8"][0] - g["fp64"][0]
+    err = {"iterations": E, "kernels": "k_rhs_tc<%d>, k_draw<fp8,%d,tc>, k_update_tc<%d>" % (C, C, C),
+           "chain0": _err(st["fp8"][0], st["fp64"][0]), "chain1": _err(st["fp8"][1], st["fp64"][1])}
+    # one subset of one loaded state at the config-5 subset shape (n = 50,000, subsets of 1,000, BayesRc in
+    # three groups): the first two subsets of the workload's genotypes
+    from sodabayes_gb300 import precision
+    G = np.asfortranarray(codes[:2000].cpu().numpy().T)
+    del codes
+    torch.cuda.empty_cache()
+    g2 = groups[:2000]
+    jobs = {}
+    for prec in ("fp8", "fp64"):
+        o = JobOptions(method="BayesRc", nmix=4, mix=(0.0, 1e-4, 1e-3, 1e-2), ngroup=3, numit=100, burnin=0,
+                       blocksize=1000, seed=4242, precision=prec, chains=C, scale_va=0.5 * vy, df_va=4.0,
+                       scale_ve=0.5 * vy, df_ve=4.0)
+        j = SodaJob(make_config(G.shape[0], G.shape[1], o))
+        j.load_genotypes(G)
+        j.load_pheno(y)
+        j.set_groups(g2)
+        j.build_z()
+        j.init_chains()
+        jobs[prec] = j
+    pi = np.array([[0.97, 0.015, 0.01, 0.005], [0.95, 0.03, 0.015, 0.005], [0.99, 0.006, 0.003, 0.001]])
+    states = [precision.sparse_state(G, y, None, 4, (0.0, 1e-4, 1e-3, 1e-2), 1.0, 0.5 * vy, 0.01, pi, g2,
+                                     seed=1000 + c, naind=1000) for c in range(C)]
+    try:
+        cond = precision.conditional_check(jobs["fp8"], jobs["fp64"], G, y, 0, 7, states, groups=g2, tau=1e-4)
+    finally:
+        for j in jobs.values():
+            j.close()
+    dis = cond.pop("disagreements", [])
+    cond["disagreement_margins"] = [round(x["margin"], 9) for x in dis][:20]
+    cond["shape"] = "n=50000, subset 1000, %d chains, BayesRc (3 groups, 4 classes)" % C
     line = {"workload": "config 5: SODA BayesRc n=50000 p=1000000 subset 1000 (1000 subsets), 16 chains on shared "
                         "genotypes, 3 annotation classes (0.1, 0.3, 0.6), mixture (0, 1e-4, 1e-3, 1e-2), LD generator "
                         "(100-SNP AR(1) blocks rho=0.8, maf~U(0.01,0.5)), 5000 causal effects, h2=0.5",
             "metric": "SODA Gibbs iters/s x chains", "value": K * C / (dev_ms / 1000.0), "unit": UNIT,
             "ms_per_step": dev_ms / K, "chains": C, "steps": K, "warmup": args.warmup,
             "settle_iterations": args.settle, "precision": "fp8", "data": "synthetic (seeded generator of config 5)",
-            "error_vs_fp64": {"iterations": E, "g_rel_rms": float(np.sqrt(np.mean(d ** 2)) /
-                                                                  max(1e-300, np.sqrt(np.mean(g["fp64"][0] ** 2)))),
-                              "class_agreement": float(np.mean(g["fp8"][1] == g["fp64"][1])),
-                              "vare_rel": float(abs(g["fp8"][2] / g["fp64"][2] - 1))},
+            "error_vs_fp64": err, "conditional_check": cond,
             "device_gb_in_use_fp8_job": round(used_gb, 1), "generate_s": round(t_gen, 2),
             "z_build_and_init_s": round(t_setup, 2), "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
@@ -461,6 +631,9 @@ def main():
     ap.add_argument("--settle", type=int, default=60, help="untimed iterations before the warm-up")
     ap.add_argument("--error-iters", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--accept-iters", type=int, default=500,
+                    help="kept iterations of the free-running acceptance comparison (0 skips it)")
+    ap.add_argument("--accept-burnin", type=int, default=100)
     ap.add_argument("--cpu-blocks", type=int, default=4)
     ap.add_argument("--profile-case", action="store_true",
                     help="n=20000, p=20000 case of the same subset shape, for ncu captures")
@@ -502,14 +675,17 @@ def main():
         cb = cpu_sample(args, steps=3, warmup=1)
         line = {"metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "u8 genotypes x f32 (FP8-exact codes, FP32 "
-                                                                  "accumulation, FP64 draws)",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "u8 genotype codes (exact 0/1/2) x bf16 hi/mid/lo splits of the residuals, delta and "
+                         "U, FP32 accumulation, FP32 draws; FP64 residual masters",
                 "data": "synthetic (seeded generator of config 3)",
                 "config": {**config, "chains": args.chains, "precision": "fp8", "settle_iterations": args.settle,
                            "parallelism": f"replicas x{ws}"},
                 "fp32_plain": res["fp32_plain"],
                 "speedup_vs_fp32_plain": res["value"] / ws / res["fp32_plain"]["value"],
-                "error_vs_fp64": res["error_vs_fp64"], "roofline": res["roofline"], "roofline_rhs": res["roofline_rhs"],
+                "error_vs_fp64": res["error_vs_fp64"], "conditional_check": res["conditional_check"],
+                "acceptance": res.get("acceptance"),
+                "roofline": res["roofline"], "roofline_rhs": res["roofline_rhs"],
                 "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": res["e2e"], "gpu_launches": res["gpu_launches"], "clocks": res["clocks"],
                 "included_at_timing": res["included_at_timing"]}

@@ -197,6 +197,37 @@ int sodagpu_get_results(sodagpu_ctx *ctx, int32_t chain, double *gstore,
 int sodagpu_get_state(sodagpu_ctx *ctx, int32_t chain, double *g, int32_t *cls,
                       double *vara_s, double *yadj, double *yaadj, double *scalars);
 
+/* Loads the sampler state of one chain, the inverse of sodagpu_get_state:
+ * g, cls (1-based classes), vara_s by SNP id (nloci each), yadj (nind),
+ * yaadj (blocksize; entries past naind are ignored), scalars[4] = {mu, vare,
+ * vara, included} and pi, the mixture proportions p(ngroup, nmix) column-major
+ * (globals.f90: p; NULL keeps the chain's current ones).  The module state
+ * soda_bayes carries from one iteration to the next (models.f90:129-574) is
+ * exactly this plus the iteration counter (sodagpu_set_iteration), so a chain
+ * restarted from it draws what it would have drawn; the posterior
+ * accumulators are not touched. */
+int sodagpu_set_state(sodagpu_ctx *ctx, int32_t chain, const double *g, const int32_t *cls,
+                      const double *vara_s, const double *yadj, const double *yaadj,
+                      const double *scalars, const double *pi);
+
+/* Sets the iteration counter `rep` (models.f90:129): the draws of
+ * sodagpu_run_subset / sodagpu_subset_rhs belong to iteration rep, and the
+ * next sodagpu_run iteration is rep + 1. */
+int sodagpu_set_iteration(sodagpu_ctx *ctx, int32_t rep);
+
+/* The conditional right-hand side of every SNP of subset b (0-based) on the
+ * current state, for every chain: rhs[chain * N_b + j] = x_j'yadj + u_j'yAadj
+ * (models.f90:154, 219, 358), before the d*g term, exactly as the draw of
+ * this context's precision consumes it (rounded to FP32 in the FP32/FP8
+ * modes); 0 for SNPs the pivoted fallback skipped.  Draws nothing and changes
+ * no state. */
+int sodagpu_subset_rhs(sodagpu_ctx *ctx, int32_t b, double *rhs);
+
+/* One subset b (0-based) of the current iteration for every chain: the
+ * per-SNP draws (models.f90:349-414) and the residual update (415-430),
+ * without the mu and hyper-parameter draws around the subset loop. */
+int sodagpu_run_subset(sodagpu_ctx *ctx, int32_t b);
+
 /* The augmenting matrix as the reference stores it: XA(blocksize, nloci)
  * column-major (globals.f90:52) and xxd(nblocks) (any pointer may be NULL),
  * plus skip flags by position (1 = skipped). */

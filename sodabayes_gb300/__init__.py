@@ -275,6 +275,50 @@ class SodaJob:
         return {"g": g, "cls": cls, "vara_s": vs, "yadj": r, "yaadj": ra, "mu": sc[0], "vare": sc[1],
                 "vara": sc[2], "included": int(sc[3])}
 
+    def set_state(self, chain: int, g, cls, vara_s, yadj, yaadj, mu: float, vare: float, vara: float,
+                  included: int = 0, pi=None) -> None:
+        """Loads one chain's state (the inverse of state()); pi is the
+        (ngroup, nmix) table of mixture proportions, or None to keep it."""
+        gg = np.ascontiguousarray(g, dtype=np.float64)
+        cc = np.ascontiguousarray(cls, dtype=np.int32)
+        vv = np.ascontiguousarray(vara_s, dtype=np.float64)
+        rr = np.ascontiguousarray(yadj, dtype=np.float64)
+        ra = np.zeros(self.cfg.blocksize)
+        ra[:min(len(yaadj), len(ra))] = np.asarray(yaadj, dtype=np.float64)[:len(ra)]
+        sc = np.array([mu, vare, vara, included], dtype=np.float64)
+        pp = None if pi is None else np.asfortranarray(pi, dtype=np.float64)
+        if gg.shape != (self.p,) or cc.shape != (self.p,) or vv.shape != (self.p,) or rr.shape != (self.n,):
+            raise ValueError("g, cls, vara_s must have nloci entries and yadj nind")
+        _check(self._lib.sodagpu_set_state(self._ctx, chain, _dp(gg), _ip(cc), _dp(vv), _dp(rr), _dp(ra), _dp(sc),
+                                           None if pp is None else pp.ctypes.data_as(C.POINTER(C.c_double))),
+               "sodagpu_set_state")
+
+    def set_iteration(self, rep: int) -> None:
+        _check(self._lib.sodagpu_set_iteration(self._ctx, int(rep)), "sodagpu_set_iteration")
+
+    def subset_rhs(self, b: int) -> np.ndarray:
+        """(chains, N_b) conditional right-hand sides of subset b on the current state."""
+        ls, le = self.subset_bounds(b)
+        nsnp = le - ls
+        out = np.empty(self.chains * nsnp)
+        _check(self._lib.sodagpu_subset_rhs(self._ctx, int(b), _dp(out)), "sodagpu_subset_rhs")
+        return out.reshape(self.chains, nsnp)
+
+    def subset_bounds(self, b: int):
+        """0-based [first, end) subset positions of subset b (models.f90:136-142)."""
+        bs, bt, p = self.cfg.blocksize, self.cfg.blockt, self.p
+        blocki = b + 1
+        if blocki <= bt:
+            ls = (blocki - 1) * bs + 1
+            le = min(ls + bs - 1, p)
+        else:
+            ls = bs * bt + (blocki - bt - 1) * (bs - 1) + 1
+            le = min(ls + bs - 2, p)
+        return ls - 1, le
+
+    def run_subset(self, b: int) -> None:
+        _check(self._lib.sodagpu_run_subset(self._ctx, int(b)), "sodagpu_run_subset")
+
     def results(self, chain: int = 0) -> dict:
         p, nm, ng = self.p, self.cfg.nmix, self.cfg.ngroup
         gs = np.empty(p)

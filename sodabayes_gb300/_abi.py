@@ -60,6 +60,10 @@ PROTOTYPES = {
     "sodagpu_run": (C.c_int, [_P, C.c_int32, TRACE_CB, _P]),
     "sodagpu_get_results": (C.c_int, [_P, C.c_int32, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
     "sodagpu_get_state": (C.c_int, [_P, C.c_int32, _DP, _IP, _DP, _DP, _DP, _DP]),
+    "sodagpu_set_state": (C.c_int, [_P, C.c_int32, _DP, _IP, _DP, _DP, _DP, _DP, _DP]),
+    "sodagpu_set_iteration": (C.c_int, [_P, C.c_int32]),
+    "sodagpu_subset_rhs": (C.c_int, [_P, C.c_int32, _DP]),
+    "sodagpu_run_subset": (C.c_int, [_P, C.c_int32]),
     "sodagpu_get_z": (C.c_int, [_P, _DP, _DP, _IP]),
     "sodagpu_compute_dgv": (C.c_int, [_P, C.c_double, _DP, _DP]),
     "sodagpu_predict": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int32, _DP, C.c_double, _DP, _DP]),

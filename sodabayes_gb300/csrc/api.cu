@@ -185,6 +185,10 @@ struct sodagpu_ctx {
     long long ncblk = 0;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
+    // staging of sodagpu_set_state and the output of sodagpu_subset_rhs
+    double *st_g = nullptr, *st_vs = nullptr, *st_r = nullptr, *st_ra = nullptr, *st_pi = nullptr;
+    int32_t *st_cls = nullptr;
+    double *rhs_buf = nullptr;
     cudaGraphExec_t graph = nullptr;
     double t_build = 0.0, t_run = 0.0, t_run_dev_ms = 0.0;
     Dev D;
@@ -1082,6 +1086,88 @@ int sodagpu_get_state(sodagpu_ctx *c, int32_t chain, double *g, int32_t *cls, do
     }
     return 0;
 }
+
+int sodagpu_set_state(sodagpu_ctx *c, int32_t chain, const double *g, const int32_t *cls, const double *vara_s,
+                      const double *yadj, const double *yaadj, const double *scalars, const double *pi)
+{
+    if (!c || !g || !cls || !vara_s || !yadj || !yaadj || !scalars) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_chain) return fail(SODAGPU_E_STATE, "call sodagpu_init_chains first");
+    if (chain < 0 || chain >= c->C) return fail(SODAGPU_E_ARG, "chain out of range");
+    const int p = c->p, nm = c->cfg.nmix, ngm = c->cfg.ngroup * nm;
+    for (int j = 0; j < p; ++j)
+        if (cls[j] < 1 || cls[j] > nm) return fail(SODAGPU_E_ARG, "class of SNP %d is %d, not in 1..%d", j + 1, cls[j], nm);
+    if (!(scalars[1] > 0.0)) return fail(SODAGPU_E_ARG, "vare must be positive");
+    if (c->cfg.method != SODAGPU_BAYES_A && !(scalars[2] > 0.0)) return fail(SODAGPU_E_ARG, "vara must be positive");
+    if (pi)
+        for (int e = 0; e < ngm; ++e)
+            if (!(pi[e] > 0.0)) return fail(SODAGPU_E_ARG, "pi entries must be positive");
+    if (!c->st_g) {
+        TRY(c->alloc(&c->st_g, p, false));
+        TRY(c->alloc(&c->st_vs, p, false));
+        TRY(c->alloc(&c->st_cls, p, false));
+        TRY(c->alloc(&c->st_r, c->n, false));
+        TRY(c->alloc(&c->st_ra, c->bs, false));
+        TRY(c->alloc(&c->st_pi, ngm, false));
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->st_g, g, sizeof(double) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaMemcpyAsync(c->st_cls, cls, sizeof(int32_t) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaMemcpyAsync(c->st_vs, vara_s, sizeof(double) * p, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaMemcpyAsync(c->st_r, yadj, sizeof(double) * c->n, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaMemcpyAsync(c->st_ra, yaadj, sizeof(double) * c->bs, cudaMemcpyHostToDevice, c->st));
+    if (pi) CUDA_TRY(cudaMemcpyAsync(c->st_pi, pi, sizeof(double) * ngm, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(sweep_set_state(c->D, chain, c->st_g, c->st_cls, c->st_vs, c->st_r, c->st_ra, pi ? c->st_pi : nullptr,
+                             scalars[0], scalars[1], scalars[2], (int)scalars[3], c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sodagpu_set_iteration(sodagpu_ctx *c, int32_t rep)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_chain) return fail(SODAGPU_E_STATE, "call sodagpu_init_chains first");
+    if (rep < 0) return fail(SODAGPU_E_ARG, "rep < 0");
+    RunCtl h{};
+    CUDA_TRY(cudaMemcpyAsync(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    h.rep = rep;
+    CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+namespace {
+int subset_call(sodagpu_ctx *c, int32_t b, bool rhs_only)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (!c->have_chain) return fail(SODAGPU_E_STATE, "call sodagpu_init_chains first");
+    if (c->regular) return fail(SODAGPU_E_UNSUPPORTED, "the regular sampler has no subsets");
+    if (b < 0 || b >= c->nb) return fail(SODAGPU_E_ARG, "subset %d out of range 0..%d", b, c->nb - 1);
+    Dev D = c->D;
+    if (rhs_only) {
+        if (!c->rhs_buf) TRY(c->alloc(&c->rhs_buf, (size_t)c->C * c->bs));
+        D.rhs_out = c->rhs_buf;
+    }
+    CUDA_TRY(sweep_enqueue_subset(D, b, c->blk_sizes[b], c->sm_count, &c->maps, c->st, rhs_only));
+    RunCtl h{};
+    CUDA_TRY(cudaMemcpyAsync(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    if (h.err) return fail(SODAGPU_E_TIMEOUT, "a bounded device loop gave up (code %d)", h.err);
+    return 0;
+}
+}  // namespace
+
+int sodagpu_subset_rhs(sodagpu_ctx *c, int32_t b, double *rhs)
+{
+    if (!rhs) return fail(SODAGPU_E_ARG, "null argument");
+    TRY(subset_call(c, b, true));
+    const int N = c->blk_sizes[b];
+    for (int ch = 0; ch < c->C; ++ch)
+        CUDA_TRY(cudaMemcpy(rhs + (size_t)ch * N, c->rhs_buf + (size_t)ch * c->bs, sizeof(double) * N,
+                            cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int sodagpu_run_subset(sodagpu_ctx *c, int32_t b) { return subset_call(c, b, false); }
 
 int sodagpu_get_z(sodagpu_ctx *c, double *xa, double *xxd, int32_t *skip)
 {

@@ -198,6 +198,19 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
             }
         }
     }
+    if (D.rhs_out) {   // the same for every thread: the whole CTA leaves here
+        if (act) {
+            double v = 0.0;
+            if (snp >= 0) {
+                double x = xr;
+                if (TC) x = x * (inv != 0.0 ? inv : 1.0) + x0 * s_rs[c];
+                else if (MODE == SODAGPU_FP8) x = x * inv + x0 * s_rs[c];
+                v = MODE == SODAGPU_FP64 ? x + ur : (double)(float)(x + ur);   // what the draw consumes
+            }
+            D.rhs_out[(size_t)c * D.bs + jl] = v;
+        }
+        return;
+    }
     double delta = 0.0;
     if (snp >= 0) {
         if (TC) xr = xr * (inv != 0.0 ? inv : 1.0) + x0 * s_rs[c];   // columns with sd = 0 carry U unscaled

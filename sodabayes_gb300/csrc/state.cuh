@@ -124,6 +124,10 @@ struct Dev {
     uint16_t *rasp;            // [round_up(3C,16)][ldra] the same split of ra32, or null
     const uint16_t *usp;       // [3][nloci][ldu] bf16 hi/mid/lo of U column k times sd_k (1 if sd_k = 0)
     int ldu;                   // row stride of usp (bs rounded up to 8)
+    // conditional right-hand sides only: when set, k_draw writes the rhs of
+    // (chain c, subset SNP jl) to rhs_out[c * bs + jl] (exactly the value its
+    // draw would consume) and draws nothing
+    double *rhs_out;
 };
 
 constexpr int RHS_KSPLIT_MAX = 16;

@@ -961,7 +961,7 @@ static cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
 // the FP32 cores; two CTAs per SM).
 template <int CT>
 static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_count, const TcMaps *maps,
-                                   cudaStream_t st, ProfHook *prof)
+                                   cudaStream_t st, ProfHook *prof, bool rhs_only)
 {
     const int mtiles = (nblk_snps + TC_TM - 1) / TC_TM;
     const int nrhs = maps->h_rtab[(size_t)b * D.tstride + mtiles];
@@ -977,7 +977,7 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
         ProfScope ps(prof, st, PROF_DRAW);
         e = launch_pdl(k_draw<SODAGPU_FP8, CT, true>, dim3((span * CT + 255) / 256), dim3(256), 0, st, D, b, 0, span);
     }
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || rhs_only) return e != cudaSuccess ? e : cudaGetLastError();
     {
         ProfScope ps(prof, st, PROF_UPDATE);
         e = launch_pdl(k_update_tc<CT>, dim3(std::min(sm_count, TV_MAXG)), dim3(TV_THREADS), UpdTc<CT>::SMEM, st,
@@ -990,10 +990,10 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
 
 template <int MODE, int CT>
 static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count, const TcMaps *maps, cudaStream_t st,
-                               ProfHook *prof)
+                               ProfHook *prof, bool rhs_only)
 {
     if constexpr (MODE == SODAGPU_FP8 && CT >= 4) {
-        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, sm_count, maps, st, prof);
+        if (D.tc) return launch_block_tc<CT>(D, b, nblk_snps, sm_count, maps, st, prof, rhs_only);
     }
     constexpr int MTS = 8 * SptOf<CT>::v;
     const int mtiles = (nblk_snps + MTS - 1) / MTS;
@@ -1013,7 +1013,7 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
         e = launch_pdl(k_draw<MODE, CT, false>, dim3((nblk_snps * CT + 255) / 256), dim3(256), 0, st, D, b, ks,
                        nblk_snps);
     }
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || rhs_only) return e != cudaSuccess ? e : cudaGetLastError();
     const int ntile = D.nr_ctas + (D.bs + UT - 1) / UT;
     {
         ProfScope ps(prof, st, PROF_UPDATE);
@@ -1025,14 +1025,14 @@ static cudaError_t launch_block(const Dev &D, int b, int nblk_snps, int sm_count
 
 template <int MODE>
 static cudaError_t launch_block_mode(const Dev &D, int b, int nsnp, int sm_count, const TcMaps *maps, cudaStream_t st,
-                                    ProfHook *prof)
+                                    ProfHook *prof, bool rhs_only = false)
 {
     switch (D.chains) {
-    case 1: return launch_block<MODE, 1>(D, b, nsnp, sm_count, maps, st, prof);
-    case 2: return launch_block<MODE, 2>(D, b, nsnp, sm_count, maps, st, prof);
-    case 4: return launch_block<MODE, 4>(D, b, nsnp, sm_count, maps, st, prof);
-    case 8: return launch_block<MODE, 8>(D, b, nsnp, sm_count, maps, st, prof);
-    case 16: return launch_block<MODE, 16>(D, b, nsnp, sm_count, maps, st, prof);
+    case 1: return launch_block<MODE, 1>(D, b, nsnp, sm_count, maps, st, prof, rhs_only);
+    case 2: return launch_block<MODE, 2>(D, b, nsnp, sm_count, maps, st, prof, rhs_only);
+    case 4: return launch_block<MODE, 4>(D, b, nsnp, sm_count, maps, st, prof, rhs_only);
+    case 8: return launch_block<MODE, 8>(D, b, nsnp, sm_count, maps, st, prof, rhs_only);
+    case 16: return launch_block<MODE, 16>(D, b, nsnp, sm_count, maps, st, prof, rhs_only);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -1338,6 +1338,73 @@ cudaError_t sweep_enqueue_init(const Dev &D, double vara0, double scale_va0, int
     k_init_chain<<<D.chains, 256, 0, st>>>(D, vara0, scale_va0);
     const int pgrid = (D.p + 255) / 256 < 4 * sm_count ? (D.p + 255) / 256 : 4 * sm_count;
     k_init_snp<<<dim3(pgrid > 0 ? pgrid : 1, D.chains), 256, 0, st>>>(D);
+    return cudaGetLastError();
+}
+
+cudaError_t sweep_enqueue_subset(const Dev &D, int b, int nsnp, int sm_count, const TcMaps *maps, cudaStream_t st,
+                                 bool rhs_only)
+{
+    if (D.tc && !maps) return cudaErrorInvalidValue;
+    if (D.precision == SODAGPU_FP64) return launch_block_mode<SODAGPU_FP64>(D, b, nsnp, sm_count, maps, st, nullptr, rhs_only);
+    if (D.precision == SODAGPU_FP32) return launch_block_mode<SODAGPU_FP32>(D, b, nsnp, sm_count, maps, st, nullptr, rhs_only);
+    return launch_block_mode<SODAGPU_FP8>(D, b, nsnp, sm_count, maps, st, nullptr, rhs_only);
+}
+
+// ---------------------------------------------------------------------------
+// Loading one chain's state (the inverse of sodagpu_get_state): the residuals
+// with every copy derived from them (FP32 copy or bf16 split, and the 128-row
+// partial sums of r that the FP8 centring reads), the per-SNP state, and the
+// chain scalars with the tables the draws read (models.f90:198-199, 330-338).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(ROW_THREADS) k_set_rows(Dev D, int c, const double *r)
+{
+    __shared__ double sh[33];
+    const int i = blockIdx.x * ROW_TILE + threadIdx.x;
+    double v = 0.0;
+    if (i < D.n) {
+        v = r[i];
+        store_r(D, c, i, v);
+    }
+    const double t = block_sum(v, sh);
+    if (threadIdx.x == 0) D.rsum[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(256) k_set_snps(Dev D, int c, const double *g, const int32_t *cls, const double *vs,
+                                                  const double *ra, const double *pi, double mu, double vare,
+                                                  double vara, int included)
+{
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    for (int j = t0; j < D.p; j += stride) {
+        const size_t o = (size_t)c * D.p + j;
+        D.g[o] = g[j];
+        D.cls[o] = cls[j];
+        D.vara_s[o] = vs[j];
+    }
+    for (int i = t0; i < D.bs; i += stride) store_ra(D, c, i, i < D.naind ? ra[i] : 0.0);
+    if (t0 == 0) {
+        ChainScal *S = &D.scal[c];
+        S->mu[0] = S->mu[1] = mu;
+        S->vare = vare;
+        S->vara = vara;
+        S->included = included;
+        const int ngm = D.ngroup * D.nmix;
+        if (pi)
+            for (int e = 0; e < ngm; ++e) S->p[e] = pi[e];
+        for (int j = 0; j < D.nmix; ++j) S->gp[j] = D.mix[j] * vara;
+        if (D.method != SODAGPU_BAYES_A) {
+            for (int e = 0; e < ngm; ++e) S->log_p[e] = log(S->p[e]);
+            for (int j = 1; j < D.nmix; ++j) S->vare_gp[j] = vare / S->gp[j];
+        }
+    }
+}
+
+cudaError_t sweep_set_state(const Dev &D, int c, const double *g, const int32_t *cls, const double *vs,
+                            const double *r, const double *ra, const double *pi, double mu, double vare, double vara,
+                            int included, cudaStream_t st)
+{
+    k_set_rows<<<D.nr_ctas, ROW_THREADS, 0, st>>>(D, c, r);
+    const int grid = std::max(1, std::min((D.p + 255) / 256, 1024));
+    k_set_snps<<<grid, 256, 0, st>>>(D, c, g, cls, vs, ra, pi, mu, vare, vara, included);
     return cudaGetLastError();
 }
 

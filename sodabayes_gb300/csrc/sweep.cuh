@@ -66,6 +66,17 @@ struct TcMaps {
 cudaError_t sweep_enqueue_iteration(const Dev &D, const int *blk_sizes, int sm_count, const TcMaps *maps,
                                     cudaStream_t st, ProfHook *prof = nullptr);
 cudaError_t sweep_enqueue_init(const Dev &D, double vara0, double scale_va0, int sm_count, cudaStream_t st);
+// One subset b (nsnp SNPs) of the current iteration, eagerly: rhs, draws and
+// residual update, or with rhs_only the rhs and the draw kernel in its
+// rhs-only mode (D.rhs_out set by the caller), which changes no state.
+cudaError_t sweep_enqueue_subset(const Dev &D, int b, int nsnp, int sm_count, const TcMaps *maps, cudaStream_t st,
+                                 bool rhs_only);
+// Loads chain c's state from device arrays: g, cls, vs by SNP id (nloci), r
+// (nind), ra (naind used), pi ((ngroup, nmix) column-major, or null to keep
+// the chain's current pi), and its scalars.
+cudaError_t sweep_set_state(const Dev &D, int c, const double *g, const int32_t *cls, const double *vs,
+                            const double *r, const double *ra, const double *pi, double mu, double vare, double vara,
+                            int included, cudaStream_t st);
 cudaError_t sweep_enqueue_recal(const Dev &D, double unused, cudaStream_t st);
 
 }  // namespace soda

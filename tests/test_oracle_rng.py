@@ -97,3 +97,31 @@ def test_dirichlet(oracle_mod):
     x = oracle_mod.sample(4, 0, 3, 20000, 4, 2.5)
     assert np.allclose(x.sum(axis=1), 1.0, atol=1e-12)
     assert np.allclose(x.mean(axis=0), 0.25, atol=0.01)
+
+
+def test_precision_module_philox_matches_oracle(oracle_mod):
+    """The numpy Philox of sodabayes_gb300.precision (class-draw uniforms for
+    the decision-margin analysis) gives the oracle's counter uniforms."""
+    import ctypes as C
+
+    from sodabayes_gb300 import precision as P
+    L = oracle_mod.lib()
+    for seed, ch, it, slot in [(4242, 0, 7, 0), (4242, 3, 7, 1999), (77, 15, 120, 499999), (2 ** 40 + 5, 2, 1, 12)]:
+        out = np.empty(1)
+        L.oracle_counter_uniforms(seed, ch, it, slot, 1, 1, out.ctypes.data_as(C.POINTER(C.c_double)))
+        assert P.class_uniform(seed, ch, it, np.array([slot]), fp32=False)[0] == out[0]
+        u32 = P.class_uniform(seed, ch, it, np.array([slot]), fp32=True)[0]
+        assert 0.0 < u32 < 1.0 and abs(u32 - out[0]) <= 2.0 ** -24
+
+
+def test_class_cumulative_two_classes():
+    """BayesC class probability (models.f90:362-377) against the closed form
+    of the two-class case, P(class 2) = 1 / (1 + exp(s1 - s2))."""
+    from sodabayes_gb300 import precision as P
+    rhs, zz, vare, gp = np.array([-3.0, 0.0, 0.7, 25.0]), 900.0, 2.0, np.array([0.0, 0.01])
+    logp = np.log(np.array([[0.99, 0.01]] * 4))
+    cum = P.class_cumulative(rhs, zz, vare, gp, logp)
+    s2 = -0.5 * (np.log(gp[1] * zz / vare + 1.0) - rhs * (rhs / (zz + vare / gp[1])) / vare) + logp[:, 1]
+    p2 = 1.0 / (1.0 + np.exp(logp[:, 0] - s2))
+    assert np.allclose(cum[:, 0], 1.0 - p2, rtol=1e-12, atol=1e-15)
+    assert np.allclose(cum[:, 1], 1.0)
