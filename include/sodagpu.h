@@ -175,6 +175,28 @@ int sodagpu_build_z(sodagpu_ctx *ctx, const int32_t *permvec, int32_t *nskipped)
  * d*I - X'X indefinite for negative delta and exercises the pivoted path. */
 int sodagpu_set_d_offset(sodagpu_ctx *ctx, double delta);
 
+/* Injected draws (the reference's per-thread xoroshiro128+ streams,
+ * parallelrng.f90:100-149, or any other source of uniforms in [0,1)).
+ * Without a tape every draw is a counter-based Philox draw keyed by (seed,
+ * chain, iteration, site); with one, each draw site of chain 0 takes the
+ * uniforms its distribution transforms consume (rand_normal two per normal,
+ * parallelrng.f90:264-277; rand_gamma's rejection loop as many as it needs,
+ * 294-333) from its record instead.
+ * Layout: draws[(rep * sites + site) * SODAGPU_TAPE_W + k], k-th uniform of
+ * `site` in iteration rep (rep 0 = chain initialisation, models.f90:56-128),
+ * sites = 3 + ngroup + blocksize + nloci:
+ *   0 mu (models.f90:130-132), 1 sigma2_g (505-513), 2 sigma2_e (515-516; at
+ *   rep 0 the initial draw, models.f90:118), 3 + i pi of group i (517-522),
+ *   3 + ngroup + i yAadj(i) (523-525; at rep 0, models.f90:124-127),
+ *   3 + ngroup + blocksize + j SNP j by id (its draw in its subset,
+ *   models.f90:146-162, 211-256, 350-413, or its single-site draw).
+ * n doubles cover n / (sites * SODAGPU_TAPE_W) iterations from rep 0; a draw
+ * past them, or one needing more than SODAGPU_TAPE_W uniforms, makes
+ * sodagpu_run / sodagpu_init_chains fail with SODAGPU_E_ARG.  One chain only;
+ * call before sodagpu_init_chains (draws == NULL, n == 0 removes the tape). */
+#define SODAGPU_TAPE_W 32
+int sodagpu_set_tape(sodagpu_ctx *ctx, const double *draws, size_t n);
+
 /* Chain initialisation (models.f90:56-128) for all chains. */
 int sodagpu_init_chains(sodagpu_ctx *ctx);
 
@@ -275,8 +297,15 @@ int sodagpu_profile_kernels(sodagpu_ctx *ctx, int32_t iters, double *ms, int32_t
  * array's device address (cudaGetSymbolAddress, with that device current), so
  * make that first call before any stream capture.  All calls share the array
  * and leave their partial sums in it: calls that overlap on the GPU race and
- * must be serialised by the caller.  Errors are reported by the return code
- * only (sodagpu_last_error is not updated). */
+ * must be serialised by the caller.  cudaDeviceReset invalidates the address
+ * looked up for that device: after a reset, do not call this again on that
+ * device in the same process.  The columns are summed in min(32,
+ * SODAGPU_NOALLOC_SCRATCH / nind, nloci) splits: up to nind = 65,536 the same
+ * order as sodagpu_predict, above it the last bits may differ.  Codes outside
+ * 0..2 count as 1 (a missing call, utilities.f90:446-449), where
+ * sodagpu_predict returns SODAGPU_E_ARG.  Errors are reported by the return
+ * code only (sodagpu_last_error is not updated); a launch error the caller
+ * left pending is neither reported nor cleared. */
 #define SODAGPU_NOALLOC_SCRATCH (2 * 1024 * 1024)
 int sodagpu_compute_dgv_noalloc(int32_t nind, int32_t nloci, const int8_t *codes, int32_t ldg,
                                 const double *freq, double mu, const double *effects, double *pred,

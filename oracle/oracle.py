@@ -38,6 +38,9 @@ PROTOTYPES = {
     "oracle_gram": (C.c_int, [_P, _IP, C.c_int32, _DP]),
     "oracle_build_z": (C.c_int, [_P, _IP, C.c_int64, C.c_double, _IP]),
     "oracle_get_z": (C.c_int, [_P, _DP, _DP, _IP]),
+    "oracle_set_z": (C.c_int, [_P, _DP, _DP]),
+    "oracle_set_tape": (C.c_int, [_P, _DP, C.c_int32, C.c_int32]),
+    "oracle_tape_sites": (C.c_int, [_P]),
     "oracle_init_chains": (C.c_int, [_P]),
     "oracle_run": (C.c_int, [_P, C.c_int32, TRACE_CB, _P]),
     "oracle_run_blocks": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
@@ -144,6 +147,27 @@ class Oracle:
         rc = self._lib.oracle_build_z(self._o, None if pv is None else _ip(pv), power_maxit, d_offset, C.byref(nsk))
         _chk(rc, "oracle_build_z")
         return nsk.value
+
+    def record_tape(self, reps: int) -> np.ndarray:
+        """Records the uniforms of every draw site of iterations 0 .. reps-1
+        into a new tape (reps x sites x TAPE_W), filled as the chain runs."""
+        sites = self._lib.oracle_tape_sites(self._o)
+        self._tape = np.zeros(reps * sites * _abi.TAPE_W)
+        _chk(self._lib.oracle_set_tape(self._o, _dp(self._tape), reps, 1), "oracle_set_tape")
+        return self._tape
+
+    def play_tape(self, tape) -> None:
+        """Draw sites take their uniforms from `tape` instead of the RNG."""
+        sites = self._lib.oracle_tape_sites(self._o)
+        self._tape = np.ascontiguousarray(tape, dtype=np.float64)
+        reps = len(self._tape) // (sites * _abi.TAPE_W)
+        _chk(self._lib.oracle_set_tape(self._o, _dp(self._tape), reps, 0), "oracle_set_tape")
+
+    def set_z(self, xa, xxd):
+        """Uses the given Z (identity order, no skipped SNPs) instead of building it."""
+        a = np.asfortranarray(xa, dtype=np.float64)
+        d = np.ascontiguousarray(xxd, dtype=np.float64)
+        _chk(self._lib.oracle_set_z(self._o, a.ctypes.data_as(_DP), _dp(d)), "oracle_set_z")
 
     def z(self):
         xa = np.empty((self.cfg.blocksize, self.p), order="F")

@@ -153,12 +153,27 @@ typedef struct {
     int mode;        /* ORACLE_RNG_* */
     xo_state *xo;    /* reference: the stream in use */
     ctr_rng c;       /* counter */
+    /* injected-draw tape: the record of the current draw site (tmode 1:
+     * the uniforms drawn are written to it, 2: they are read from it instead
+     * of the RNG), tn uniforms used so far */
+    double *tp;
+    int tn, tmode;
 } rng_t;
 
 static inline double rng_u(rng_t *r)
 {
-    return r->mode == ORACLE_RNG_REFERENCE ? u64_to_unit(xo_next(r->xo))
-                                           : u64_to_unit(ctr_next(&r->c));
+    if (r->tmode == 2) {
+        double u = r->tn < SODAGPU_TAPE_W ? r->tp[r->tn] : 0.5;
+        r->tn++;
+        return u;
+    }
+    double u = r->mode == ORACLE_RNG_REFERENCE ? u64_to_unit(xo_next(r->xo))
+                                               : u64_to_unit(ctr_next(&r->c));
+    if (r->tmode == 1) {
+        if (r->tn < SODAGPU_TAPE_W) r->tp[r->tn] = u;
+        r->tn++;
+    }
+    return u;
 }
 
 /* rand_normal (parallelrng.f90:264-277): Box-Muller, sine branch, REAL pi */
@@ -248,6 +263,9 @@ struct oracle_ctx {
     int nskipped, naind, naless;
     int have_geno, have_pheno, have_z, have_chain;
     chain_t *ch;
+    /* injected-draw tape (oracle_set_tape) */
+    double *tape;
+    int tape_reps, tape_sites, tape_play, tape_over;
 };
 
 #define IDX2(i, j, ld) ((size_t)(i) + (size_t)(j) * (size_t)(ld))
@@ -440,6 +458,7 @@ int oracle_permutate(oracle_ctx *o, int32_t *permvec)
         int m = n - i + 1 < s ? n - i + 1 : s;
         rng_t r;
         r.mode = o->rng_mode;
+        r.tmode = 0;
         r.xo = &o->xo[0];
         ctr_init(&r.c, o->cfg.seed, 0, 0, chunk, P_PERM);
         for (int k = 0; k < s; ++k) u[k] = rng_u(&r);
@@ -733,6 +752,7 @@ int oracle_build_z(oracle_ctx *o, const int32_t *permvec, int64_t power_maxit,
         }
         rng_t r;
         r.mode = o->rng_mode;
+        r.tmode = 0;
         r.xo = &o->xo[0];
         ctr_init(&r.c, o->cfg.seed, 0, 0, b, P_POWER);
         for (int i = 0; i < nn; ++i) start[i] = rng_u(&r);
@@ -783,6 +803,27 @@ int oracle_build_z(oracle_ctx *o, const int32_t *permvec, int64_t power_maxit,
     return 0;
 }
 
+/* Takes the augmenting matrix from elsewhere (XA(bs, p) column-major and
+ * xxd(nb), identity SNP order, no skipped SNPs) instead of building it, so
+ * that a sweep can be compared on the same Z.  The factor's conditioning
+ * (its smallest eigenvalue is the 0.001 of soda.f90:485) turns a 1e-12
+ * relative difference in d into ~1e-9 in U, which would otherwise reach
+ * the sweep. */
+int oracle_set_z(oracle_ctx *o, const double *xa, const double *xxd)
+{
+    if (!o || !o->have_geno || !xa || !xxd || o->regular) return SODAGPU_E_STATE;
+    for (int k = 0; k < o->p; ++k) o->perm[k] = k;
+    memcpy(o->XA, xa, sizeof(double) * (size_t)o->bs * o->p);
+    memcpy(o->xxd, xxd, sizeof(double) * o->nb);
+    memset(o->skip, 0, o->p);
+    memset(o->iskipped, 0, sizeof(int32_t) * o->p);
+    o->nskipped = 0;
+    o->naless = 0;
+    o->naind = o->bs;
+    o->have_z = 1;
+    return 0;
+}
+
 int oracle_get_z(oracle_ctx *o, double *xa, double *xxd, int32_t *skip)
 {
     if (!o || !o->have_z) return SODAGPU_E_STATE;
@@ -796,6 +837,43 @@ int oracle_get_z(oracle_ctx *o, double *xa, double *xxd, int32_t *skip)
 /* ------------------------------------------------------------------------ */
 /* Sampler                                                                  */
 /* ------------------------------------------------------------------------ */
+
+/* Injected-draw tape sites (layout of sodagpu_set_tape): 0 mu, 1 sigma2_g,
+ * 2 sigma2_e, 3 + i pi of group i, 3 + ngroup + i ra_i, 3 + ngroup +
+ * blocksize + j SNP j (block draw or single-site draw). */
+static void tape_site(oracle_ctx *o, rng_t *R, int rep, int site)
+{
+    R->tmode = 0;
+    if (!o->tape) return;
+    if (rep >= o->tape_reps) {
+        if (o->tape_play) o->tape_over = 1;   /* playing past the end of the tape */
+        return;
+    }
+    R->tp = o->tape + ((size_t)rep * o->tape_sites + site) * SODAGPU_TAPE_W;
+    R->tn = 0;
+    R->tmode = o->tape_play ? 2 : 1;
+}
+
+static void tape_end(oracle_ctx *o, rng_t *R)
+{
+    if (R->tmode && R->tn > SODAGPU_TAPE_W) o->tape_over = 1;
+    R->tmode = 0;
+}
+
+static int snp_site(const oracle_ctx *o, int snploc) { return 3 + o->ngroup + o->cfg.blocksize + snploc; }
+
+int oracle_set_tape(oracle_ctx *o, double *tape, int32_t reps, int32_t record)
+{
+    if (!o || (tape && reps < 1) || o->nchain != 1) return SODAGPU_E_ARG;
+    o->tape = tape;
+    o->tape_reps = tape ? reps : 0;
+    o->tape_sites = 3 + o->ngroup + o->cfg.blocksize + o->p;
+    o->tape_play = !record;
+    o->tape_over = 0;
+    return 0;
+}
+
+int oracle_tape_sites(const oracle_ctx *o) { return o ? 3 + o->ngroup + o->cfg.blocksize + o->p : 0; }
 
 /* compute_residuals (utilities.f90:609-614) */
 static void compute_residuals(const oracle_ctx *o, chain_t *c)
@@ -811,7 +889,15 @@ static void compute_residuals(const oracle_ctx *o, chain_t *c)
 
 static int is_ab(int m) { return m == SODAGPU_BAYES_A || m == SODAGPU_BAYES_B; }
 
+static int init_chains_(oracle_ctx *o);
+
 int oracle_init_chains(oracle_ctx *o)
+{
+    int rc = init_chains_(o);
+    return rc ? rc : (o->tape_over ? SODAGPU_E_ARG : 0);
+}
+
+static int init_chains_(oracle_ctx *o)
 {
     if (!o || !o->have_geno || !o->have_pheno || !o->have_z) return SODAGPU_E_STATE;
     const int n = o->n, p = o->p, nm = o->nmix, ng = o->ngroup, m = o->method;
@@ -923,14 +1009,19 @@ int oracle_init_chains(oracle_ctx *o)
         double scale = (rr + o->cfg.scale_ve * o->cfg.df_ve) / (nn + o->cfg.df_ve);
         rng_t R;
         R.mode = o->rng_mode;
+        R.tmode = 0;
         R.xo = &o->xo[0];
         ctr_init(&R.c, o->cfg.seed, ci, 0, 0, P_VARE);
+        tape_site(o, &R, 0, 2);
         c->vare = rscinvchi2(nn + o->cfg.df_ve, scale, &R);
+        tape_end(o, &R);
         c->vare_store = 0;
         memset(c->ra, 0, sizeof(double) * o->bs);
         for (int i = 0; i < o->naind; ++i) {
             if (o->rng_mode == ORACLE_RNG_COUNTER) ctr_init(&R.c, o->cfg.seed, ci, 0, i, P_RA);
+            tape_site(o, &R, 0, 3 + o->ngroup + i);
             c->ra[i] = rnorm(0.0, sqrt(c->vare), &R);
+            tape_end(o, &R);
         }
     }
     o->have_chain = 1;
@@ -1144,11 +1235,14 @@ static void sweep_block(oracle_ctx *o, chain_t *c, int ci, int b, int rep)
             static_chunk(N, o->ref_threads, t, &lo, &hi);
             rng_t R;
             R.mode = ORACLE_RNG_REFERENCE;
+            R.tmode = 0;
             R.xo = &o->xo[t];
             for (int jk = lo; jk < hi; ++jk) {
                 int k = ls - 1 + jk;
                 if (o->skip[k]) continue;
+                tape_site(o, &R, rep, snp_site(o, o->perm[k]));
                 draw_in_block(o, c, k, jk, zz, zz_vare, &R);
+                tape_end(o, &R);
             }
         }
     } else {
@@ -1158,9 +1252,12 @@ static void sweep_block(oracle_ctx *o, chain_t *c, int ci, int b, int rep)
             if (o->skip[k]) continue;
             rng_t R;
             R.mode = ORACLE_RNG_COUNTER;
+            R.tmode = 0;
             R.xo = NULL;
             ctr_init(&R.c, o->cfg.seed, ci, rep, o->perm[k], P_SNP);
+            tape_site(o, &R, rep, snp_site(o, o->perm[k]));
             draw_in_block(o, c, k, jk, zz, zz_vare, &R);
+            tape_end(o, &R);
         }
     }
     /* residual update, SNP order within each element (models.f90:164-174) */
@@ -1202,12 +1299,15 @@ static void iterate(oracle_ctx *o, chain_t *c, int ci, int rep, sodagpu_trace_cb
     const double nn = (double)n;
     rng_t R0;
     R0.mode = o->rng_mode;
+    R0.tmode = 0;
     R0.xo = &o->xo[0];
     /* mu (130-132) */
     double s = 0.0;
     for (int i = 0; i < n; ++i) { c->r[i] = c->r[i] + c->mu; s = s + c->r[i]; }
     ctr_init(&R0.c, o->cfg.seed, ci, rep, 0, P_MU);
+    tape_site(o, &R0, rep, 0);
     c->mu = rnorm(s / nn, sqrt(c->vare / nn), &R0);
+    tape_end(o, &R0);
     for (int i = 0; i < n; ++i) c->r[i] = c->r[i] - c->mu;
     /* log_p / vare_gp of the parallel region (198-199, 330-338) */
     if (m != SODAGPU_BAYES_A) {
@@ -1219,7 +1319,9 @@ static void iterate(oracle_ctx *o, chain_t *c, int ci, int rep, sodagpu_trace_cb
     for (int t = 0; t < o->nskipped; ++t) {
         int snploc = o->iskipped[t];
         if (o->rng_mode == ORACLE_RNG_COUNTER) ctr_init(&R0.c, o->cfg.seed, ci, rep, snploc, P_SKIP);
+        tape_site(o, &R0, rep, snp_site(o, snploc));
         draw_skipped(o, c, snploc, &R0);
+        tape_end(o, &R0);
     }
     /* counts and variances (194, 321-325, 496-513) */
     if (m == SODAGPU_BAYES_A) {
@@ -1255,7 +1357,9 @@ static void iterate(oracle_ctx *o, chain_t *c, int ci, int rep, sodagpu_trace_cb
             for (int j = 1; j < nm; ++j) scale = scale + c->varindist[IDX2(i, j, ng)] / o->cfg.mix[j];
         scale = (scale + c->scale_va * o->cfg.df_va) / (o->cfg.df_va + (double)c->included);
         ctr_init(&R0.c, o->cfg.seed, ci, rep, 0, P_VARA);
+        tape_site(o, &R0, rep, 1);
         c->vara = rscinvchi2((double)c->included + o->cfg.df_va, scale, &R0);
+        tape_end(o, &R0);
         for (int j = 0; j < nm; ++j) c->gp[j] = o->cfg.mix[j] * c->vara;
     }
     /* vare (515-516) */
@@ -1263,7 +1367,9 @@ static void iterate(oracle_ctx *o, chain_t *c, int ci, int rep, sodagpu_trace_cb
     for (int i = 0; i < n; ++i) rr = rr + c->r[i] * c->r[i];
     double scale = (rr + o->cfg.scale_ve * o->cfg.df_ve) / (nn + o->cfg.df_ve);
     ctr_init(&R0.c, o->cfg.seed, ci, rep, 0, P_VARE);
+    tape_site(o, &R0, rep, 2);
     c->vare = rscinvchi2(nn + o->cfg.df_ve, scale, &R0);
+    tape_end(o, &R0);
     /* pi (517-522) */
     if (m == SODAGPU_BAYES_CPI || m == SODAGPU_BAYES_R || m == SODAGPU_BAYES_RC) {
         double dirx[SODAGPU_MAXDIST], pi[SODAGPU_MAXDIST];
@@ -1271,14 +1377,18 @@ static void iterate(oracle_ctx *o, chain_t *c, int ci, int rep, sodagpu_trace_cb
             for (int j = 0; j < nm; ++j)
                 dirx[j] = (double)c->snpindist[IDX2(i, j, ng)] + o->cfg.alpha[j];
             ctr_init(&R0.c, o->cfg.seed, ci, rep, i, P_PI);
+            tape_site(o, &R0, rep, 3 + i);
             rdirichlet(nm, dirx, pi, &R0);
+            tape_end(o, &R0);
             for (int j = 0; j < nm; ++j) c->p[IDX2(i, j, ng)] = pi[j];
         }
     }
     /* augmented residual redraw (523-525) */
     for (int i = 0; i < o->naind; ++i) {
         if (o->rng_mode == ORACLE_RNG_COUNTER) ctr_init(&R0.c, o->cfg.seed, ci, rep, i, P_RA);
+        tape_site(o, &R0, rep, 3 + ng + i);
         c->ra[i] = rnorm(0.0, sqrt(c->vare), &R0);
+        tape_end(o, &R0);
     }
     /* accumulators (526-548) */
     if (rep > o->cfg.burnin && rep % o->cfg.thin == 0) {
@@ -1331,7 +1441,7 @@ int oracle_run(oracle_ctx *o, int32_t iters, sodagpu_trace_cb cb, void *user)
             c->rep++;
             iterate(o, c, ci, c->rep, cb, user);
         }
-    return 0;
+    return o->tape_over ? SODAGPU_E_ARG : 0;   /* a draw site used more uniforms than a tape record holds */
 }
 
 /* Timing helper for the CPU baseline: sweeps `nblocks_run` blocks starting at
@@ -1497,6 +1607,7 @@ int oracle_sample(int32_t dist, int32_t mode, int64_t seed, int32_t count, doubl
     xo_streams(seed, 1, &st);
     rng_t R;
     R.mode = mode;
+    R.tmode = 0;
     R.xo = &st;
     ctr_init(&R.c, seed, 0, 0, 0, 0);
     for (int i = 0; i < count; ++i) {

@@ -46,6 +46,13 @@ int oracle_gram(oracle_ctx *o, const int32_t *cols, int32_t ncols, double *A);
 int oracle_build_z(oracle_ctx *o, const int32_t *permvec, int64_t power_maxit,
                    double d_offset, int32_t *nskipped);
 int oracle_get_z(oracle_ctx *o, double *xa, double *xxd, int32_t *skip);
+int oracle_set_z(oracle_ctx *o, const double *xa, const double *xxd);
+/* Injected-draw tape (layout of sodagpu_set_tape, one chain): with record = 1
+ * every draw site of iterations 0 .. reps-1 (0 = chain initialisation) writes
+ * the uniforms it draws into `tape` (reps x sites x SODAGPU_TAPE_W doubles,
+ * owned by the caller); with record = 0 the sites read them from it instead. */
+int oracle_set_tape(oracle_ctx *o, double *tape, int32_t reps, int32_t record);
+int oracle_tape_sites(const oracle_ctx *o);
 int oracle_init_chains(oracle_ctx *o);
 int oracle_run(oracle_ctx *o, int32_t iters, sodagpu_trace_cb cb, void *user);
 int oracle_run_blocks(oracle_ctx *o, int32_t first_block, int32_t nblocks_run,

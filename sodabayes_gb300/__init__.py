@@ -252,6 +252,16 @@ class SodaJob:
                "sodagpu_build_z")
         return nsk.value
 
+    def set_tape(self, tape) -> None:
+        """Injected draws: every draw site of chain 0 takes its uniforms from
+        `tape` (layout of sodagpu_set_tape); None removes it.  Call before
+        init_chains."""
+        if tape is None:
+            _check(self._lib.sodagpu_set_tape(self._ctx, None, 0), "sodagpu_set_tape")
+            return
+        t = np.ascontiguousarray(tape, dtype=np.float64)
+        _check(self._lib.sodagpu_set_tape(self._ctx, _dp(t), t.size), "sodagpu_set_tape")
+
     def init_chains(self) -> None:
         _check(self._lib.sodagpu_init_chains(self._ctx), "sodagpu_init_chains")
 

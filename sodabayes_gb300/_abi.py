@@ -5,6 +5,7 @@ import ctypes as C
 
 MAXDIST = 20
 MAXGRP = 100
+TAPE_W = 32          # uniforms per draw site of an injected-draw tape
 
 BAYES_A, BAYES_B, BAYES_C, BAYES_CPI, BAYES_R, BAYES_RC = 1, 2, 3, 4, 5, 6
 METHODS = {"BayesA": BAYES_A, "BayesB": BAYES_B, "BayesC": BAYES_C, "BayesCpi": BAYES_CPI,
@@ -56,6 +57,7 @@ PROTOTYPES = {
     "sodagpu_set_groups": (C.c_int, [_P, _IP]),
     "sodagpu_build_z": (C.c_int, [_P, _IP, _IP]),
     "sodagpu_set_d_offset": (C.c_int, [_P, C.c_double]),
+    "sodagpu_set_tape": (C.c_int, [_P, _DP, C.c_size_t]),
     "sodagpu_init_chains": (C.c_int, [_P]),
     "sodagpu_run": (C.c_int, [_P, C.c_int32, TRACE_CB, _P]),
     "sodagpu_get_results": (C.c_int, [_P, C.c_int32, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),

@@ -189,6 +189,8 @@ struct sodagpu_ctx {
     double *st_g = nullptr, *st_vs = nullptr, *st_r = nullptr, *st_ra = nullptr, *st_pi = nullptr;
     int32_t *st_cls = nullptr;
     double *rhs_buf = nullptr;
+    double *tape = nullptr;              // injected-draw tape (sodagpu_set_tape)
+    int tape_reps = 0;
     cudaGraphExec_t graph = nullptr;
     double t_build = 0.0, t_run = 0.0, t_run_dev_ms = 0.0;
     Dev D;
@@ -848,12 +850,38 @@ int build_dev(sodagpu_ctx *c)
     D.rasp = c->rasp;
     D.usp = c->usp;
     D.ldu = c->ldu;
+    D.tape = c->tape;
+    D.tape_reps = c->tape_reps;
+    D.tape_snp0 = 3 + c->cfg.ngroup + c->cfg.blocksize;
+    D.tape_sites = D.tape_snp0 + c->p;
     return 0;
 }
 
 }  // namespace
 
 extern "C" {
+
+int sodagpu_set_tape(sodagpu_ctx *c, const double *draws, size_t n)
+{
+    if (!c) return fail(SODAGPU_E_ARG, "null argument");
+    if (c->have_chain) return fail(SODAGPU_E_STATE, "set the tape before sodagpu_init_chains");
+    if (c->C != 1) return fail(SODAGPU_E_UNSUPPORTED, "an injected-draw tape drives one chain");
+    if (c->tape) {
+        c->release(c->tape);
+        c->tape = nullptr;
+        c->tape_reps = 0;
+    }
+    if (!draws && n == 0) return 0;
+    const size_t rec = (size_t)(3 + c->cfg.ngroup + c->cfg.blocksize + c->p) * SODAGPU_TAPE_W;
+    if (!draws || n < rec || n % rec != 0)
+        return fail(SODAGPU_E_ARG, "tape length %zu is not a positive multiple of %zu (sites x SODAGPU_TAPE_W)", n, rec);
+    if (n / rec > (size_t)INT32_MAX) return fail(SODAGPU_E_ARG, "tape too long");
+    TRY(c->alloc(&c->tape, n, false));
+    CUDA_TRY(cudaMemcpyAsync(c->tape, draws, sizeof(double) * n, cudaMemcpyHostToDevice, c->st));
+    CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->tape_reps = (int)(n / rec);
+    return 0;
+}
 
 int sodagpu_init_chains(sodagpu_ctx *c)
 {
@@ -946,6 +974,12 @@ int sodagpu_init_chains(sodagpu_ctx *c)
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(sweep_enqueue_init(c->D, c->cfg.vara0, c->cfg.scale_va, c->sm_count, c->st));
     CUDA_TRY(cudaStreamSynchronize(c->st));
+    {
+        RunCtl hc{};
+        CUDA_TRY(cudaMemcpy(&hc, c->ctl, sizeof hc, cudaMemcpyDeviceToHost));
+        if (hc.err == 19) return fail(SODAGPU_E_ARG, "a draw of the chain initialisation overran the injected-draw tape");
+        if (hc.err) return fail(SODAGPU_E_TIMEOUT, "a bounded device loop gave up (code %d)", hc.err);
+    }
     // capture one iteration of every chain as a CUDA graph
     if (c->graph) {
         cudaGraphExecDestroy(c->graph);
@@ -1002,6 +1036,9 @@ int sodagpu_run(sodagpu_ctx *c, int32_t iters, sodagpu_trace_cb cb, void *user)
     cudaEventDestroy(e1);
     c->t_run_dev_ms = dev_ms;
     c->t_run = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (h.err == 19)
+        return fail(SODAGPU_E_ARG, "a draw overran the injected-draw tape (iteration past its end, or a draw site "
+                                   "needing more than %d uniforms)", SODAGPU_TAPE_W);
     if (h.err) return fail(SODAGPU_E_TIMEOUT, "a bounded device loop gave up (code %d)", h.err);
     if (cb && rows > 0) {
         std::vector<sodagpu_trace_row> hr(rows);
@@ -1251,6 +1288,14 @@ int sodagpu_predict(int32_t nind, int32_t nloci, const void *geno, int32_t layou
             if (e == cudaSuccess) chk(zb_decode_bed(tmp, n, p, G, ldx, st));
         }
     }
+    // codes outside 0..2 are an error, as in sodagpu_load_genotypes: counted on the device (k_freq, into
+    // the xv buffer, which is written again below)
+    int *bad = nullptr, h_bad = 0;
+    chk(cudaMalloc(&bad, sizeof(int)));
+    if (e == cudaSuccess) chk(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    if (e == cudaSuccess) chk(zb_freq(G, n, p, ldx, xv, bad, st));
+    if (e == cudaSuccess) chk(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (e == cudaSuccess) chk(cudaStreamSynchronize(st));
     if (e == cudaSuccess) chk(cudaMemcpyAsync(dfreq, freq, sizeof(double) * p, cudaMemcpyHostToDevice, st));
     if (e == cudaSuccess) chk(cudaMemcpyAsync(deff, effects, sizeof(double) * p, cudaMemcpyHostToDevice, st));
     if (e == cudaSuccess) chk(cudaMemcpyAsync(perm, ident.data(), sizeof(int32_t) * p, cudaMemcpyHostToDevice, st));
@@ -1260,8 +1305,10 @@ int sodagpu_predict(int32_t nind, int32_t nloci, const void *geno, int32_t layou
     if (e == cudaSuccess) chk(cudaStreamSynchronize(st));
     cudaFree(G); cudaFree(dfreq); cudaFree(xv); cudaFree(deff); cudaFree(part); cudaFree(dpred); cudaFree(perm);
     cudaFree(tmp);
+    cudaFree(bad);
     cudaStreamDestroy(st);
     if (e != cudaSuccess) return fail(SODAGPU_E_CUDA, "prediction failed: %s", cudaGetErrorString(e));
+    if (h_bad) return fail(SODAGPU_E_ARG, "%d genotype codes outside 0..2", h_bad);
     return 0;
 }
 

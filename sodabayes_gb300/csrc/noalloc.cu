@@ -16,7 +16,16 @@
 // cudaGetSymbolAddress (with that device current) and caches it; later calls
 // reuse it.  Every call shares the one array: calls that overlap on the GPU
 // (different streams, or different host threads on the same device) race on
-// it and must be serialised by the caller.
+// it and must be serialised by the caller.  cudaDeviceReset destroys the
+// context that holds the array; the cached address is then stale, so a host
+// that resets a device must not call this entry point on it again in the
+// same process.
+//
+// The columns are summed in nsplit = min(32, SCRATCH / nind, nloci) splits,
+// the same 32 as sodagpu_predict up to nind = 65,536; above that the
+// summation order differs and so can the last bits of the result.  Codes
+// outside 0..2 count as 1, the value load_geno gives a missing call
+// (utilities.f90:446-449); sodagpu_predict rejects them instead.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -118,10 +127,26 @@ extern "C" int sodagpu_compute_dgv_noalloc(int32_t nind, int32_t nloci, const in
         }
         scratch = g_scratch_ptr[dev];
     }
+    // cudaLaunchKernel reports a failed launch in its own return value, so an error the caller left
+    // pending from earlier work is neither reported as this call's failure nor cleared
     cudaStream_t st = (cudaStream_t)stream;
-    k_dgv_noalloc_partial<<<dim3((nind + 255) / 256, nsplit), 256, 0, st>>>(codes, ldg, freq, effects, nind, nloci,
-                                                                            nsplit, scratch);
-    k_dgv_noalloc_final<<<(nind + 255) / 256, 256, 0, st>>>(scratch, nind, nsplit, mu, pred);
-    if (cudaGetLastError() != cudaSuccess) return SODAGPU_E_CUDA;
+    {
+        void *args[] = {(void *)&codes, (void *)&ldg, (void *)&freq, (void *)&effects, (void *)&nind,
+                        (void *)&nloci, (void *)&nsplit, (void *)&scratch};
+        if (cudaLaunchKernel((const void *)k_dgv_noalloc_partial, dim3((nind + 255) / 256, nsplit), dim3(256), args,
+                             0, st) != cudaSuccess) {
+            cudaGetLastError();
+            return SODAGPU_E_CUDA;
+        }
+    }
+    {
+        const double *part = scratch;
+        void *args[] = {(void *)&part, (void *)&nind, (void *)&nsplit, (void *)&mu, (void *)&pred};
+        if (cudaLaunchKernel((const void *)k_dgv_noalloc_final, dim3((nind + 255) / 256), dim3(256), args, 0, st) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            return SODAGPU_E_CUDA;
+        }
+    }
     return 0;
 }

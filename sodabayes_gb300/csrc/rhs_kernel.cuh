@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
         else if (MODE == SODAGPU_FP8) xr = xr * inv + x0 * s_rs[c];
         const ChainScal *S = &D.scal[c];
         CRng R;
-        crng_init(R, D.seed, c, cur_rep(D), snp, P_SNP);
+        crng_site(R, D, c, cur_rep(D), snp, P_SNP);
         int err = 0;
         if (MODE == SODAGPU_FP64) {
             delta = draw_snp(D, S, c, cur_rep(D), snp, xr + ur, zz, zz / S->vare, R, &err);

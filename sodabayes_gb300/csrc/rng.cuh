@@ -13,6 +13,7 @@
 //   Dirichlet      normalised gammas                            (parallelrng.f90:445-455)
 #pragma once
 #include <stdint.h>
+#include "../../include/sodagpu.h"
 
 namespace soda {
 
@@ -29,6 +30,11 @@ struct CRng {
     uint32_t k0, k1, c0, c1, c2, c3;
     uint32_t o2, o3;
     int have;
+    // injected draws: the uniforms of this draw site come from a tape record
+    // of SODAGPU_TAPE_W values instead of Philox; tover is set on overrun
+    const double *tape;
+    int tpos;
+    int *tover;
 };
 
 __host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b)
@@ -63,6 +69,18 @@ __host__ __device__ __forceinline__ void crng_init(CRng &s, uint64_t seed, int c
     s.c2 = (uint32_t)purpose;
     s.c3 = (uint32_t)chain << 20;
     s.have = 0;
+    s.tape = nullptr;
+    s.tpos = 0;
+    s.tover = nullptr;
+}
+
+__device__ __forceinline__ double crng_tape_next(CRng &s)
+{
+    double v = 0.5;
+    if (s.tpos < SODAGPU_TAPE_W) v = s.tape[s.tpos];
+    else if (s.tover) *s.tover = 1;
+    ++s.tpos;
+    return v;
 }
 
 __host__ __device__ __forceinline__ uint64_t crng_u64(CRng &s)
@@ -82,6 +100,9 @@ __host__ __device__ __forceinline__ uint64_t crng_u64(CRng &s)
 
 __host__ __device__ __forceinline__ double crng_unit(CRng &s)
 {
+#if defined(__CUDA_ARCH__)
+    if (s.tape) return crng_tape_next(s);
+#endif
     const uint64_t bits = 0x3FF0000000000000ULL | (crng_u64(s) >> 12);
 #if defined(__CUDA_ARCH__)
     return __longlong_as_double((long long)bits) - 1.0;
@@ -151,6 +172,7 @@ __device__ __forceinline__ double d_rscinvchi2(double dof, double scale, CRng &s
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float crng_unit_f(CRng &s)
 {
+    if (s.tape) return (float)crng_tape_next(s);
     return ((float)(uint32_t)(crng_u64(s) >> 40) + 0.5f) * 5.9604644775390625e-8f;
 }
 

@@ -128,6 +128,11 @@ struct Dev {
     // (chain c, subset SNP jl) to rhs_out[c * bs + jl] (exactly the value its
     // draw would consume) and draws nothing
     double *rhs_out;
+    // injected-draw tape (sodagpu_set_tape): tape_reps iterations of
+    // tape_sites records of SODAGPU_TAPE_W uniforms; SNP records start at
+    // site tape_snp0 (3 + ngroup + the configured blocksize)
+    const double *tape;
+    int tape_reps, tape_sites, tape_snp0;
 };
 
 constexpr int RHS_KSPLIT_MAX = 16;

@@ -86,6 +86,34 @@ __device__ __forceinline__ void flag_err(const Dev &D, int code)
     atomicExch(&D.ctl->err, code);
 }
 
+// Device error code of an injected-draw tape that a draw overran (a site
+// needing more uniforms than its record holds, or an iteration past the tape).
+constexpr int ERR_TAPE = 19;
+
+// The draw stream of one site: Philox keyed by (seed, chain, rep, slot,
+// purpose), or, with an injected-draw tape, the site's record (chain 0; site
+// numbering of sodagpu_set_tape).
+__device__ __forceinline__ void crng_site(CRng &R, const Dev &D, int c, int rep, int slot, int purpose)
+{
+    crng_init(R, D.seed, c, rep, slot, purpose);
+    if (!D.tape) return;
+    int site;
+    switch (purpose) {
+    case P_MU: site = 0; break;
+    case P_VARA: site = 1; break;
+    case P_VARE: site = 2; break;
+    case P_PI: site = 3 + slot; break;
+    case P_RA: site = 3 + D.ngroup + slot; break;
+    default: site = D.tape_snp0 + slot; break;   // P_SNP, P_SKIP: by SNP id
+    }
+    R.tover = &D.ctl->err;
+    if (rep >= 0 && rep < D.tape_reps && site < D.tape_sites) {
+        R.tape = D.tape + ((size_t)rep * D.tape_sites + site) * SODAGPU_TAPE_W;
+    } else {
+        flag_err(D, ERR_TAPE);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Per-SNP conditional draw inside a subset.  Returns delta = g_old - g_new.
 // Restates models.f90:146-161 (BayesA), 211-255 (BayesB), 350-412 (C/Cpi/R/Rc).
@@ -379,7 +407,7 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
         double tot = 0.0;
         for (int t = 0; t < D.nr_ctas; ++t) tot += D.rpart[(size_t)c * D.nr_ctas + t];
         CRng R;
-        crng_init(R, D.seed, c, rep, 0, P_MU);
+        crng_site(R, D, c, rep, 0, P_MU);
         const double nn = (double)D.n;
         const double mu = d_rnorm(tot / nn, sqrt(S->vare / nn), R);
         s_mu = mu;
@@ -469,7 +497,7 @@ __device__ __forceinline__ double single_site_draw(const Dev &D, ChainScal *S, i
         }
         if (lane == 0) {
             CRng R;
-            crng_init(R, D.seed, c, rep, snploc, P_SKIP);
+            crng_site(R, D, c, rep, snploc, P_SKIP);
             const double u = crng_unit(R);
             double ssculm = 0.0;
             int flag = 1;
@@ -504,7 +532,7 @@ __device__ __forceinline__ double single_site_draw(const Dev &D, ChainScal *S, i
         const double gk = D.g[o];
         double gt = 0.0;
         CRng R;
-        crng_init(R, D.seed, c, rep, snploc, P_SKIP);
+        crng_site(R, D, c, rep, snploc, P_SKIP);
         if (m == SODAGPU_BAYES_A) {
             rhs = rhs + zz * gk;
             const double v1 = zz + vare / D.vara_s[o];
@@ -671,7 +699,7 @@ __global__ void __launch_bounds__(128) k_hyper(Dev D)
                 for (int j = 1; j < nm; ++j) scale = scale + S->varindist[i + j * ng] / D.mix[j];
             scale = (scale + S->scale_va * D.df_va) / (D.df_va + (double)S->included);
             CRng R;
-            crng_init(R, D.seed, c, rep, 0, P_VARA);
+            crng_site(R, D, c, rep, 0, P_VARA);
             S->vara = d_rscinvchi2((double)S->included + D.df_va, scale, R, &err);
             for (int j = 0; j < nm; ++j) S->gp[j] = D.mix[j] * S->vara;
         }
@@ -680,7 +708,7 @@ __global__ void __launch_bounds__(128) k_hyper(Dev D)
         const double nn = (double)D.n;
         const double scale = (rr + D.scale_ve * D.df_ve) / (nn + D.df_ve);
         CRng R;
-        crng_init(R, D.seed, c, rep, 0, P_VARE);
+        crng_site(R, D, c, rep, 0, P_VARE);
         S->vare = d_rscinvchi2(nn + D.df_ve, scale, R, &err);
         s_vara = S->vara;
     }
@@ -689,7 +717,7 @@ __global__ void __launch_bounds__(128) k_hyper(Dev D)
     if (m == SODAGPU_BAYES_CPI || m == SODAGPU_BAYES_R || m == SODAGPU_BAYES_RC) {
         for (int i = threadIdx.x; i < ng; i += blockDim.x) {
             CRng R;
-            crng_init(R, D.seed, c, rep, i, P_PI);
+            crng_site(R, D, c, rep, i, P_PI);
             double x[MAXDIST], sx = 0.0;
             for (int j = 0; j < nm; ++j)
                 x[j] = d_rgamma((double)S->snpindist[i + j * ng] + D.alpha[j], 1.0, R, &err);
@@ -754,7 +782,7 @@ __global__ void __launch_bounds__(256) k_post(Dev D)
     const double sd = sqrt(S->vare);
     for (int i = t0; i < D.naind; i += stride) {
         CRng R;
-        crng_init(R, D.seed, c, rep, i, P_RA);
+        crng_site(R, D, c, rep, i, P_RA);
         store_ra(D, c, i, d_rnorm(0.0, sd, R));
     }
     if (!S->keep) return;
@@ -877,7 +905,7 @@ __global__ void __launch_bounds__(256) k_init_chain(Dev D, double vara0, double 
         for (int j = 0; j < nm; ++j) S->gp[j] = D.mix[j] * S->vara;
         const double scale = (rr + D.scale_ve * D.df_ve) / (nn + D.df_ve);
         CRng R;
-        crng_init(R, D.seed, c, 0, 0, P_VARE);
+        crng_site(R, D, c, 0, 0, P_VARE);
         int err = 0;
         S->vare = d_rscinvchi2(nn + D.df_ve, scale, R, &err);
         if (err) flag_err(D, 1);
@@ -892,7 +920,7 @@ __global__ void __launch_bounds__(256) k_init_chain(Dev D, double vara0, double 
         double v = 0.0;
         if (i < D.naind) {
             CRng R;
-            crng_init(R, D.seed, c, 0, i, P_RA);
+            crng_site(R, D, c, 0, i, P_RA);
             v = d_rnorm(0.0, sd, R);
         }
         store_ra(D, c, i, v);

@@ -674,7 +674,8 @@ __global__ void __launch_bounds__(256) k_dgv_partial(const int8_t *G, int ldx, c
     for (int k = k0; k < k1; ++k) {
         const double e = eff[perm ? perm[k] : k];
         if (e == 0.0) continue;
-        acc = acc + xv[(size_t)k * 4 + G[(size_t)k * ldx + i]] * e;
+        const int code = G[(size_t)k * ldx + i];
+        acc = acc + xv[(size_t)k * 4 + ((unsigned)code <= 2u ? code : 1)] * e;   // codes are validated on entry
     }
     part[(size_t)s * ldx + i] = acc;
 }

@@ -2,6 +2,8 @@
 example files (run once where the reference checkout is available; the
 fixtures are committed, the tests never read the reference).
 
+Usage: python tests/golden/make_golden.py <reference checkout>
+
 pred_kat.npz — prediction known-answer test.  The reference's prediction
     mode (SODABayes.f90:145-148 -> setup_prediction, xscale, compute_dgv,
     write_dgv) applied to examples/data/simdata1_pred.bed with the shipped
@@ -21,9 +23,8 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
-EX = os.path.join(REF, "examples")
+EX = ""   # <reference checkout>/examples, set from the command line
 NKEEP = 100
 NIND, NLOCI = 900, 9346
 
@@ -96,4 +97,7 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout (the directory holding examples/)>")
+    EX = os.path.join(sys.argv[1], "examples")
     main()

@@ -55,3 +55,21 @@ def test_gpu_prediction_matches_oracle(gpu_lib, oracle_mod, kat):
         want = oracle_mod.predict(codes, kat["freq"], kat["mu"][s], kat["eff"][s])
         got = sg.predict(codes=codes, freq=kat["freq"], mu=kat["mu"][s], effects=kat["eff"][s])
         assert np.allclose(got, want, rtol=1e-12, atol=1e-10)
+
+
+@pytest.mark.gpu
+def test_gpu_prediction_rejects_codes_outside_0_to_2(gpu_lib, kat):
+    """Codes other than 0/1/2 are an argument error in prediction mode, as
+    when loading genotypes (the centring table has three values per SNP)."""
+    import sodabayes_gb300 as sg
+    n, p = 50, 40
+    codes = np.ones((n, p), dtype=np.int8)
+    freq = np.full(p, 0.5)
+    eff = np.ones(p)
+    assert np.allclose(sg.predict(codes=codes, freq=freq, mu=1.0, effects=eff), 1.0)
+    for bad in (-1, 3, -9):
+        c2 = codes.copy()
+        c2[7, 3] = bad
+        with pytest.raises(sg.SodaGpuError) as ei:
+            sg.predict(codes=c2, freq=freq, mu=1.0, effects=eff)
+        assert ei.value.code == -1

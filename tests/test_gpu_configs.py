@@ -86,23 +86,31 @@ def _c2_opts(prec):
 
 
 @pytest.fixture(scope="module")
-def c2_oracle(oracle_mod, c2):
-    """Oracle states after one and three iterations of config 2 (the FP64 Z build takes about a minute)."""
+def c2_oracle(gpu_lib, oracle_mod, c2):
+    """Oracle states after one and three iterations of config 2 on the GPU's Z.  The sweep is compared
+    on one Z: its factor has the smallest eigenvalue 0.001 (soda.f90:485), so the 1e-12 relative
+    difference between the GPU's Lanczos d and the oracle's power-method d moves U by ~1e-9, which
+    would reach the draws.  The Z build itself is compared with the oracle's at config 1."""
     G, y = c2
-    oracle_mod.set_threads(os.cpu_count() or 1)
     cfg = make_config(G.shape[0], G.shape[1], JobOptions(**_c2_opts("fp64")))
+    with SodaJob(cfg) as job:
+        job.load_genotypes(G)
+        job.load_pheno(y)
+        assert job.build_z() == 0
+        xa, xxd, _ = job.z()
+    oracle_mod.set_threads(os.cpu_count() or 1)
     o = oracle_mod.Oracle(cfg)
     o.load_genotypes(G)
     o.load_pheno(y)
-    nsk = o.build_z()
-    _, xxd, _ = o.z()
+    o.set_z(xa, xxd)
+    del xa
     o.init_chains()
     o.run(1)
     s1 = o.state()
     o.run(2)
     s3 = o.state()
     o.close()
-    return {"nskipped": nsk, "xxd": xxd, 1: s1, 3: s3}
+    return {"xxd": xxd, 1: s1, 3: s3}
 
 
 def test_config2_bayesr_fp64_against_oracle(gpu_lib, c2, c2_oracle):
@@ -111,8 +119,8 @@ def test_config2_bayesr_fp64_against_oracle(gpu_lib, c2, c2_oracle):
     with SodaJob(cfg) as job:
         job.load_genotypes(G)
         job.load_pheno(y)
-        assert job.build_z() == c2_oracle["nskipped"]
-        assert _rel(job.z()[1], c2_oracle["xxd"]) <= 1e-12
+        assert job.build_z() == 0
+        assert np.array_equal(job.z()[1], c2_oracle["xxd"])   # the Z build is deterministic
         job.init_chains()
         job.run(1)
         _same(job.state(), c2_oracle[1], 1e-10)
