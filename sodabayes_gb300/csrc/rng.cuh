@@ -26,6 +26,9 @@ enum Purpose : uint32_t {
 // parallelrng.f90:20 declares pi as a default REAL literal: float(pi) widened.
 #define SODA_REF_PI 3.1415927410125732
 
+// Device error code of a draw that overran its injected-draw tape record.
+constexpr int CRNG_TAPE_OVERRUN = 19;
+
 struct CRng {
     uint32_t k0, k1, c0, c1, c2, c3;
     uint32_t o2, o3;
@@ -78,7 +81,7 @@ __device__ __forceinline__ double crng_tape_next(CRng &s)
 {
     double v = 0.5;
     if (s.tpos < SODAGPU_TAPE_W) v = s.tape[s.tpos];
-    else if (s.tover) *s.tover = 1;
+    else if (s.tover) *s.tover = CRNG_TAPE_OVERRUN;
     ++s.tpos;
     return v;
 }

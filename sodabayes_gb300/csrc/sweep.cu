@@ -86,9 +86,9 @@ __device__ __forceinline__ void flag_err(const Dev &D, int code)
     atomicExch(&D.ctl->err, code);
 }
 
-// Device error code of an injected-draw tape that a draw overran (a site
-// needing more uniforms than its record holds, or an iteration past the tape).
-constexpr int ERR_TAPE = 19;
+// A draw past the end of an injected-draw tape sets the same error code as a
+// site needing more uniforms than its record holds.
+constexpr int ERR_TAPE = CRNG_TAPE_OVERRUN;
 
 // The draw stream of one site: Philox keyed by (seed, chain, rep, slot,
 // purpose), or, with an injected-draw tape, the site's record (chain 0; site

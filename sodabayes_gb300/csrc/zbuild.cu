@@ -175,14 +175,19 @@ __global__ void __launch_bounds__(256) k_gram(const int8_t *G, int ldx, const in
             const int k = tj * GT + tx * 4 + r;
             if (k >= N) continue;
             const double fk = freq[perm[ls + k]];
-            const double qj = __dsub_rn(1.0, fj), qk = __dsub_rn(1.0, fk);
+            // the scaling takes the frequency of the later position first, like xxproduct's
+            // (jj, kk) with kk <= jj (soda.f90:474-481, 553-554): products of doubles are not
+            // associative, and in a diagonal tile the two threads holding (j, k) and (k, j) both
+            // write both entries, so they must compute the same value
+            const double fa = k > j ? fk : fj, fb = k > j ? fj : fk;
+            const double qa = __dsub_rn(1.0, fa), qb = __dsub_rn(1.0, fb);
             double res;
-            if (fj <= ep || qj <= ep || fk <= ep || qk <= ep) {
+            if (fa <= ep || qa <= ep || fb <= ep || qb <= ep) {
                 res = 0.0;
             } else {
-                const double pj = __dmul_rn(fj, 2.0), pk = __dmul_rn(fk, 2.0);
-                const double t1 = __dmul_rn(__dmul_rn((double)n, pj), pk);
-                const double den = sqrt(__dmul_rn(__dmul_rn(__dmul_rn(pj, pk), qj), qk));
+                const double pa = __dmul_rn(fa, 2.0), pb = __dmul_rn(fb, 2.0);
+                const double t1 = __dmul_rn(__dmul_rn((double)n, pa), pb);
+                const double den = sqrt(__dmul_rn(__dmul_rn(__dmul_rn(pa, pb), qa), qb));
                 res = __ddiv_rn(__dsub_rn((double)acc[q][r], t1), den);
             }
             Wb[(size_t)j + (size_t)k * N] = res;

@@ -112,21 +112,24 @@ def test_reference_streams_fed_to_the_gpu(gpu_lib, oracle_mod, data, method):
     z = zjob.z()[:2]
     zjob.close()
     o = _oracle(oracle_mod, cfg, G, y, oracle_mod.RNG_REFERENCE, z)
-    tape = o.record_tape(4)
+    tape = o.record_tape(4)      # filled as the oracle runs: run it first
     o.init_chains()
+    want = [o.state()]
+    o.run(1)
+    want.append(o.state())
+    o.run(2)
+    want.append(o.state())
+    o.close()
     job = _gpu(cfg, G, y, tape)
     try:
-        _same(job.state(), o.state(), 1e-12)        # chain initialisation (sigma2_e, yAadj)
+        _same(job.state(), want[0], 1e-12)        # chain initialisation (sigma2_e, yAadj)
         job.run(1)
-        o.run(1)
-        _same(job.state(), o.state(), 1e-10)
+        _same(job.state(), want[1], 1e-10)
         job.run(2)
-        o.run(2)
-        _same(job.state(), o.state(), 1e-9)
+        _same(job.state(), want[2], 1e-9)
         # past the tape's four iterations (0 .. 3) the GPU refuses to draw
         from sodabayes_gb300 import SodaGpuError
         with pytest.raises(SodaGpuError):
             job.run(1)
     finally:
         job.close()
-        o.close()
