@@ -60,22 +60,6 @@ CUresult make_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, const void *base, 
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
 
-// 3-D tile map over the tiled codes (blocks of 128 positions x 256
-// individuals, one contiguous [128][256] byte array each), loaded in boxes of
-// b0 individuals x b1 positions of one block.
-CUresult make_tmap_codes(CUtensorMap *m, const void *base, long long nblocks, uint32_t b0, uint32_t b1,
-                         CUtensorMapSwizzle sw)
-{
-    PFN_cuTensorMapEncodeTiled_v12000 fn = tmap_encoder();
-    if (!fn) return CUDA_ERROR_NOT_SUPPORTED;
-    const cuuint64_t dims[3] = {256, 128, (cuuint64_t)nblocks};
-    const cuuint64_t strides[2] = {256, 256 * 128};
-    const cuuint32_t box[3] = {b0, b1, 1};
-    const cuuint32_t es[3] = {1, 1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<void *>(base), dims, strides, box, es,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-}
-
 thread_local std::string g_last_error;
 
 int fail(int code, const char *fmt, ...)
@@ -175,13 +159,13 @@ struct sodagpu_ctx {
     bool usp_ready = false;
     double *k0part = nullptr;
     float *vpart = nullptr;              // residual-update partial sums
-    unsigned long long *ugrid = nullptr;
+    unsigned *uticket = nullptr;         // per-tile tickets of the residual update
     TcMaps maps{};
     std::vector<int32_t> h_rtab;         // work table of the tensor-core rhs
     int32_t *rtab = nullptr;
     std::vector<int32_t> h_qoff;         // first code block of each subset (tiled codes)
     int32_t *qoff = nullptr;
-    int8_t *Gt = nullptr;                // tiled codes: [blocks][128][256]
+    uint8_t *Gt = nullptr;               // packed codes: [blocks][TC_PACKED_BLOCK]
     long long ncblk = 0;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
@@ -841,7 +825,8 @@ int build_dev(sodagpu_ctx *c)
     D.dsplit = c->dsplit;
     D.k0part = c->k0part;
     D.vpart = c->vpart;
-    D.ugrid = c->ugrid;
+    D.uticket = c->uticket;
+    D.gpk = c->Gt;
     D.nvt = sweep_tc_update_tiles(c->n);
     D.rtab = c->rtab;
     D.qoff = c->qoff;
@@ -918,7 +903,7 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             TRY(c->alloc(&c->dsplit, (size_t)sweep_tc_rows(C) * c->ldd));
             TRY(c->alloc(&c->k0part, (((size_t)c->ldd * C + 255) / 256) * C));
             TRY(c->alloc(&c->vpart, sweep_tc_vpart_floats(c->n, c->bs, C, c->sm_count), false));
-            TRY(c->alloc(&c->ugrid, 1));
+            TRY(c->alloc(&c->uticket, sweep_tc_update_all_tiles(c->n, c->bs)));
             const int NB = sweep_tc_rows(C);
             c->ldu = (int)round_up((size_t)c->bs, 8);
             TRY(c->alloc(&c->rsp, (size_t)NB * c->ldr));
@@ -935,17 +920,13 @@ int sodagpu_init_chains(sodagpu_ctx *c)
                        sweep_tc_update_tiles(c->n);
             TRY(c->alloc(&c->qoff, c->h_qoff.size(), false));
             CUDA_TRY(cudaMemcpyAsync(c->qoff, c->h_qoff.data(), c->h_qoff.size() * 4, cudaMemcpyHostToDevice, c->st));
-            TRY(c->alloc(&c->Gt, (size_t)c->ncblk * TC_CODE_BLOCK, false));
+            TRY(c->alloc(&c->Gt, (size_t)c->ncblk * TC_PACKED_BLOCK, false));
         }
     }
     build_dev(c);
     if (c->tc) {
         const int NB = sweep_tc_rows(C);
-        CUresult r = make_tmap_codes(&c->maps.codes128, c->Gt, c->ncblk, 128, 128, CU_TENSOR_MAP_SWIZZLE_128B);
-        if (r == CUDA_SUCCESS)
-            r = make_tmap_codes(&c->maps.codes256, c->Gt, c->ncblk, 256, 64, CU_TENSOR_MAP_SWIZZLE_NONE);
-        if (r == CUDA_SUCCESS)
-            r = make_tmap_2d(&c->maps.rsp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->rsp, c->ldr, NB, (uint64_t)c->ldr * 2,
+        CUresult r = make_tmap_2d(&c->maps.rsp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->rsp, c->ldr, NB, (uint64_t)c->ldr * 2,
                              64, NB, CU_TENSOR_MAP_SWIZZLE_128B);
         if (r == CUDA_SUCCESS)
             r = make_tmap_2d(&c->maps.rasp, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, c->rasp, c->ldra, NB,

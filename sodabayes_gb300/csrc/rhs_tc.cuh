@@ -16,21 +16,26 @@
 // draw kernel.  A CTA owns one M tile and a contiguous range of its stages
 // (genotype stages first) and runs a warp-specialised pipeline synchronised
 // by mbarriers:
-//   warp 16 (one thread) TMA: each stage's A tile (codes: 128 x 128 bytes,
-//           half of one 32 KB block of the tiled copy, so 128-byte rows 256
-//           bytes apart; U terms: 128 x 64 bf16) and B tile, all 128-byte
-//           swizzled, into a raw buffer (NS buffers in flight);
-//   warps 0-15 convert a genotype stage's codes into one of four bf16
-//           operands in tensor memory (lane = SNP, tcgen05.st);
+//   warp 16 (one thread) TMA: each stage's B tile (the residual split) and,
+//           for U stages, its A tile (128 x 64 bf16), 128-byte swizzled, into
+//           a raw buffer (NS buffers in flight);
+//   warps 0-15 load the genotype codes of a stage 2-bit packed from global
+//           memory (8 bytes = 32 codes per thread, several stages ahead; the
+//           codes are written once, before the sweep, so the first loads are
+//           issued before the dependency wait) and widen them into one of four
+//           bf16 operands in tensor memory (lane = SNP, tcgen05.st); they take
+//           no part in the raw buffers' hand-offs;
 //   warp 17 (one thread) issues the stage's MMAs (A from tensor memory or,
 //           for U stages, from the raw buffer; B always from the raw buffer)
-//           and commits their completion, which frees the buffers.
+//           once the operands are in place, and commits their completion,
+//           which frees the buffers.
 // With programmatic dependent launch the prologue (barriers, tensor memory,
-// the first A tiles, which are constant) overlaps the previous kernel; the
-// residual splits are read after it completes.  Each thread lets the draw
-// kernel launch only after its own dependency wait, so that the draw's
-// prologue may read what the previous residual update wrote.  The accumulator rows go to
-// rpx as FP32 partial sums, one slot per K split, added by k_draw.
+// the first U tiles, which are constant, and the first code words) overlaps
+// the previous kernel; the residual splits are read after it completes.  Each
+// thread lets the draw kernel launch only after its own dependency wait, so
+// that the draw's prologue may read what the previous residual update wrote.
+// The accumulator rows go to rpx as FP32 partial sums, one slot per K split,
+// added by k_draw.
 #pragma once
 #include <cuda.h>
 
@@ -43,15 +48,16 @@ constexpr int TC_THREADS = 576;  // 16 converter warps, the TMA warp, the MMA wa
 constexpr int TC_CONV = 512;     // converter threads
 constexpr int TC_CONV_WARPS = TC_CONV / 32;   // each converter warp arrives once per stage
 constexpr int TC_NOB = 4;        // bf16 codes operands in tensor memory (converters run up to 4 stages ahead)
+constexpr int TC_PF = 4;         // packed code words each converter thread holds in flight
 constexpr int TC_WARP_TMA = 16, TC_WARP_MMA = 17;
 
 template <int CT>
 struct RhsTc {
     static constexpr int NB = ((3 * CT + 15) / 16) * 16;   // MMA N: hi, mid, lo per chain
-    static constexpr int RAW_A = TC_TM * TC_KC;            // codes box 128 x 128 bytes, or U box 128 x 64 bf16
+    static constexpr int RAW_A = TC_TM * TC_KU * 2;        // U box 128 x 64 bf16 (U stages)
     static constexpr int RAW_B = NB * TC_KC * 2;           // residual split: two 64-wide K regions
     static constexpr int RAW = RAW_A + RAW_B;
-    static constexpr uint32_t TX_G = RAW;                  // bytes a genotype stage loads
+    static constexpr uint32_t TX_G = RAW_B;                // bytes a genotype stage loads
     static constexpr uint32_t TX_U = RAW_A + NB * TC_KU * 2;   // bytes an augmenting stage loads
     static constexpr int NS_FIT = (220 * 1024 - 1024) / RAW;
     static constexpr int NS = NS_FIT > 8 ? 8 : NS_FIT;     // raw buffers in flight
@@ -84,8 +90,8 @@ __host__ __device__ inline int rhs_tc_split(int nG, int T, int ks, int ksplit)
 
 template <int CT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_rhs_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_rsp,
-             const __grid_constant__ CUtensorMap tm_usp, const __grid_constant__ CUtensorMap tm_rasp, Dev D, int b)
+    k_rhs_tc(const __grid_constant__ CUtensorMap tm_rsp, const __grid_constant__ CUtensorMap tm_usp,
+             const __grid_constant__ CUtensorMap tm_rasp, Dev D, int b)
 {
     using T = RhsTc<CT>;
     constexpr int NB = T::NB, NS = T::NS;
@@ -116,7 +122,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) {
             tc::mbar_init(&s_full[i], 1);
-            tc::mbar_init(&s_empty[i], TC_CONV_WARPS + 1);   // converter warps + the MMAs reading B (and U's A)
+            tc::mbar_init(&s_empty[i], 1);   // the MMAs reading B (and a U stage's A)
         }
         for (int i = 0; i < TC_NOB; ++i) {
             tc::mbar_init(&s_conv[i], TC_CONV_WARPS);
@@ -134,31 +140,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     if (warp == TC_WARP_TMA) {
         if (lane == 0) {
-            tc::tma_prefetch_desc(&tm_codes);
             tc::tma_prefetch_desc(&tm_rsp);
             tc::tma_prefetch_desc(&tm_usp);
             tc::tma_prefetch_desc(&tm_rasp);
-            // A tiles (codes, U terms) do not depend on the previous kernel; B tiles do.  Codes:
-            // half t % 2 of the tiled block (tile mt of the subset, individuals 256 (t / 2) ..)
-            const int cblk = (D.qoff[b] + mt) * D.nvt;
+            // U stages' A tiles do not depend on the previous kernel; B tiles do
             auto load_a = [&](int s) {
                 const int t = t0 + s;
+                if (t < nG) return;   // genotype stages: the converters load the codes
                 unsigned char *rw = raw0 + (size_t)(s % NS) * T::RAW;
                 uint64_t *bar = &s_full[s % NS];
-                if (t < nG) {
-                    tc::mbar_expect_tx(bar, T::TX_G);
-                    tc::tma_load_3d(rw, &tm_codes, (t & 1) * TC_KC, 0, cblk + (t >> 1), bar);
-                } else {
-                    const int u = t - nG;
-                    tc::mbar_expect_tx(bar, T::TX_U);
-                    tc::tma_load_2d(rw, &tm_usp, (u / 3) * TC_KU, (u % 3) * D.p + ls + j0, bar);
-                }
+                const int u = t - nG;
+                tc::mbar_expect_tx(bar, T::TX_U);
+                tc::tma_load_2d(rw, &tm_usp, (u / 3) * TC_KU, (u % 3) * D.p + ls + j0, bar);
             };
             auto load_b = [&](int s) {
                 const int t = t0 + s;
                 unsigned char *rw = raw0 + (size_t)(s % NS) * T::RAW + T::RAW_A;
                 uint64_t *bar = &s_full[s % NS];
                 if (t < nG) {
+                    tc::mbar_expect_tx(bar, T::TX_G);
                     tc::tma_load_2d(rw, &tm_rsp, t * TC_KC, 0, bar);
                     tc::tma_load_2d(rw + NB * 128, &tm_rsp, t * TC_KC + 64, 0, bar);
                 } else {
@@ -179,6 +179,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 load_a(s);
                 load_b(s);
             }
+            // no copy may still be in flight into this CTA's shared memory when it exits
+            for (int s = max(0, ns - NS); s < ns; ++s)
+                if (!tc::mbar_wait(&s_full[s % NS], (s / NS) & 1)) s_err = 1;
         } else {
             tc::pdl_wait();
             tc::pdl_trigger();
@@ -193,7 +196,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t rb = tc::smem_u32(raw0 + (size_t)buf * T::RAW);
                 if (s < nck) {
                     const int ob = s % TC_NOB;
-                    if (!tc::mbar_wait(&s_conv[ob], (s / TC_NOB) & 1)) {
+                    if (!tc::mbar_wait(&s_conv[ob], (s / TC_NOB) & 1) || !tc::mbar_wait(&s_full[buf], (s / NS) & 1)) {
                         s_err = 1;
                         break;
                     }
@@ -222,46 +225,54 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc::mma_commit(&s_done);
         }
     } else {
+        // converters: thread (SNP m of the tile, individuals 32 s4 .. 32 s4 + 31 of each stage) loads
+        // 8 bytes of packed codes per genotype stage, TC_PF stages ahead, and widens them into one of
+        // four bf16 operands in tensor memory; they take no part in the raw buffers' hand-offs
+        const int m = 32 * (warp & 3) + lane, s4 = warp >> 2;
+        // a packed block is [4 groups of 64 individuals][128 positions][16 bytes]; stage t covers
+        // individuals 128 (t % 2) .. of tile t / 2, so this thread's 8 bytes are half s4 % 2 of the
+        // 16-byte word (group 2 (t % 2) + s4 / 2, position m)
+        const uint64_t *cw = reinterpret_cast<const uint64_t *>(D.gpk) + 2 * ((s4 >> 1) * TC_TM + m) + (s4 & 1);
+        const size_t blk0 = (size_t)(D.qoff[b] + mt) * D.nvt;
+        auto code_word = [&](int s) -> uint64_t {
+            const int t = t0 + s;
+            const uint64_t *p = cw + (blk0 + (t >> 1)) * (TC_PACKED_BLOCK / 8) + (t & 1) * (4 * TC_TM);
+            uint64_t v;
+            asm volatile("ld.global.nc.L1::no_allocate.u64 %0, [%1];" : "=l"(v) : "l"(p));
+            return v;
+        };
+        uint64_t pf[TC_PF];
+#pragma unroll
+        for (int i = 0; i < TC_PF; ++i) pf[i] = i < nck ? code_word(i) : 0ull;
         tc::pdl_wait();
         tc::pdl_trigger();
-        // converters: genotype stages -> bf16 codes in tensor memory; augmenting stages
-        // need no conversion (they only release the buffer after its TMA completed)
-        for (int s = 0; s < ns; ++s) {
-            const int buf = s % NS, ob = s % TC_NOB;
-            bool ok = tc::mbar_wait(&s_full[buf], (s / NS) & 1);
-            if (s < nck) {
-                // the operand buffer was last read by the MMAs of stage s - TC_NOB
-                if (ok && s >= TC_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
-                ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
-                if (!ok) {
-                    s_err = 1;
-                    break;
-                }
-                const unsigned char *ra_ = raw0 + (size_t)buf * T::RAW;
-                // warp w writes lanes 32*(w%4).. (SNP rows), 32 codes of K (columns 16*(w/4) .. +15)
-                const int m = 32 * (warp & 3) + lane, s4 = warp >> 2;
-                const uint4 wa = *reinterpret_cast<const uint4 *>(ra_ + m * 128 + (((2 * s4) ^ (m & 7)) << 4));
-                const uint4 wb = *reinterpret_cast<const uint4 *>(ra_ + m * 128 + (((2 * s4 + 1) ^ (m & 7)) << 4));
-                uint32_t v[16];
-                tc::codes_to_bf16x4(wa.x, v[0], v[1]);
-                tc::codes_to_bf16x4(wa.y, v[2], v[3]);
-                tc::codes_to_bf16x4(wa.z, v[4], v[5]);
-                tc::codes_to_bf16x4(wa.w, v[6], v[7]);
-                tc::codes_to_bf16x4(wb.x, v[8], v[9]);
-                tc::codes_to_bf16x4(wb.y, v[10], v[11]);
-                tc::codes_to_bf16x4(wb.z, v[12], v[13]);
-                tc::codes_to_bf16x4(wb.w, v[14], v[15]);
-                tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 64 * ob + 16 * s4, v);
-                tc::tmem_wait_st();
-                tc::fence_before_sync();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
-            } else if (!__all_sync(0xffffffffu, ok)) {
+        for (int s = 0; s < nck; ++s) {
+            const int ob = s % TC_NOB;
+            // the operand buffer was last read by the MMAs of stage s - TC_NOB
+            bool ok = s < TC_NOB || tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
+            ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
+            if (!ok) {
                 s_err = 1;
                 break;
             }
+            const uint64_t w = pf[0];
+#pragma unroll
+            for (int i = 0; i + 1 < TC_PF; ++i) pf[i] = pf[i + 1];
+            pf[TC_PF - 1] = s + TC_PF < nck ? code_word(s + TC_PF) : 0ull;
+            // word ww of the 8 bytes: individuals 16 ww + 4 q + e at bits 8 e + 2 q
+            uint32_t v[16];
+#pragma unroll
+            for (int ww = 0; ww < 2; ++ww) {
+                const uint32_t x = (uint32_t)(w >> (32 * ww));
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    tc::codes_to_bf16x4((x >> (2 * q)) & 0x03030303u, v[8 * ww + 2 * q], v[8 * ww + 2 * q + 1]);
+            }
+            tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 64 * ob + 16 * s4, v);
+            tc::tmem_wait_st();
+            tc::fence_before_sync();
             __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&s_empty[buf]);
+            if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
         }
         if (ns > 0 && !tc::mbar_wait(&s_done, 0)) s_err = 1;
     }

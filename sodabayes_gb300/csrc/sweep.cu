@@ -996,8 +996,8 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
     cudaError_t e;
     {
         ProfScope ps(prof, st, PROF_RHS);
-        e = launch_pdl(k_rhs_tc<CT>, dim3(nrhs), dim3(TC_THREADS), RhsTc<CT>::SMEM, st, maps->codes128, maps->rsp,
-                       maps->usp, maps->rasp, D, b);
+        e = launch_pdl(k_rhs_tc<CT>, dim3(nrhs), dim3(TC_THREADS), RhsTc<CT>::SMEM, st, maps->rsp, maps->usp,
+                       maps->rasp, D, b);
     }
     if (e != cudaSuccess) return e;
     {
@@ -1009,7 +1009,7 @@ static cudaError_t launch_block_tc(const Dev &D, int b, int nblk_snps, int sm_co
     {
         ProfScope ps(prof, st, PROF_UPDATE);
         e = launch_pdl(k_update_tc<CT>, dim3(std::min(sm_count, TV_MAXG)), dim3(TV_THREADS), UpdTc<CT>::SMEM, st,
-                       maps->codes256, maps->d, maps->usp64, D, b);
+                       maps->d, maps->usp64, D, b);
 
     }
     if (e != cudaSuccess) return e;
@@ -1176,6 +1176,8 @@ size_t sweep_tc_vpart_floats(int n, int bs, int chains, int sm_count)
 
 int sweep_tc_rows(int chains) { return ((3 * chains + 15) / 16) * 16; }
 
+int sweep_tc_update_all_tiles(int n, int bs) { return sweep_tc_update_tiles(n) + (bs + TV_N - 1) / TV_N; }
+
 __global__ void __launch_bounds__(256) k_tc_prepare(int8_t *G, Dev D, uint16_t *usp)
 {
     for (int k = blockIdx.x; k < D.p; k += gridDim.x) {
@@ -1216,13 +1218,18 @@ int sweep_tc_code_blocks(const int *blk_sizes, int nb, int32_t *qoff)
     return tot;
 }
 
-// Code block (q2, t) = positions 128 (q2 - qoff[b]) .. of subset b x individuals 256 t .., one
-// contiguous [128][256] byte array; positions past the subset and individuals past n hold 0.
-// A warp copies two rows per pass (16-byte chunks), so reads and writes are coalesced.
-__global__ void __launch_bounds__(256) k_tile_codes(const int8_t *G, Dev D, int8_t *Gt, long long nblocks)
+// Packed code block (q2, t): positions 128 (q2 - qoff[b]) .. of subset b x individuals 256 t .. (see
+// TC_PACKED_BLOCK); positions past the subset and individuals past n hold 0.  One thread per 16-byte word
+// (group g of 64 individuals, position k): four 16-byte loads of the position's column of G (64 bytes never
+// straddle ldx, a multiple of 128), each folded into one 32-bit word.
+__global__ void __launch_bounds__(256) k_tile_codes(const int8_t *G, Dev D, uint8_t *Gt, long long nblocks)
 {
-    const int ch = threadIdx.x & 15;
-    for (long long blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+    constexpr int WORDS = TC_PACKED_BLOCK / 16;
+    const long long total = nblocks * WORDS;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long blk = idx / WORDS;
+        const int wi = (int)(idx - blk * WORDS), g = wi / TC_TM, k = wi - g * TC_TM;
         const int q2 = (int)(blk / D.nvt), t = (int)(blk - (long long)q2 * D.nvt);
         int lo = 0, hi = D.nb - 1;   // the subset: last b with qoff[b] <= q2
         while (lo < hi) {
@@ -1230,27 +1237,29 @@ __global__ void __launch_bounds__(256) k_tile_codes(const int8_t *G, Dev D, int8
             if (D.qoff[mid] <= q2) lo = mid;
             else hi = mid - 1;
         }
-        const int ls = D.blk_ls[lo], N = D.blk_ls[lo + 1] - ls, r0 = (q2 - D.qoff[lo]) * TC_TM;
-        const int i0 = t * TV_N + 16 * ch;
-        for (int row = threadIdx.x >> 4; row < TC_TM; row += 16) {
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (r0 + row < N && i0 < D.n) {
-                v = *reinterpret_cast<const uint4 *>(G + (size_t)(ls + r0 + row) * D.ldx + i0);
-                if (i0 + 16 > D.n) {
-                    uint8_t *bv = reinterpret_cast<uint8_t *>(&v);
-                    for (int e = D.n - i0; e < 16; ++e) bv[e] = 0;
-                }
+        const int ls = D.blk_ls[lo], N = D.blk_ls[lo + 1] - ls, r = (q2 - D.qoff[lo]) * TC_TM + k;
+        const int i0 = t * TV_N + 64 * g;
+        uint32_t out[4] = {0u, 0u, 0u, 0u};
+        if (r < N && i0 + 64 <= D.ldx) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(G + (size_t)(ls + r) * D.ldx + i0);
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                const uint4 v = src[w];   // individuals 16 w + 4 b + j: byte j of word b
+                out[w] = (v.x & 0x03030303u) | ((v.y & 0x03030303u) << 2) | ((v.z & 0x03030303u) << 4) |
+                         ((v.w & 0x03030303u) << 6);
             }
-            *reinterpret_cast<uint4 *>(Gt + (size_t)blk * (TC_TM * TV_N) + row * TV_N + 16 * ch) = v;
         }
+        *reinterpret_cast<uint4 *>(Gt + blk * TC_PACKED_BLOCK + (size_t)wi * 16) =
+            make_uint4(out[0], out[1], out[2], out[3]);
     }
 }
 
-cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, int8_t *Gt, long long nblocks, int sm_count,
+cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, uint8_t *Gt, long long nblocks, int sm_count,
                                 cudaStream_t st)
 {
     if (!Gt || !D.qoff || nblocks <= 0) return cudaErrorInvalidValue;
-    const long long grid = std::min<long long>(nblocks, 8LL * sm_count);
+    const long long words = nblocks * (TC_PACKED_BLOCK / 16);
+    const long long grid = std::min<long long>((words + 255) / 256, 16LL * sm_count);
     k_tile_codes<<<(unsigned)grid, 256, 0, st>>>(G, D, Gt, nblocks);
     return cudaGetLastError();
 }

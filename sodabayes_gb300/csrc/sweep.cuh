@@ -12,10 +12,12 @@ cudaError_t sweep_prepare(int bs);
 // (3 * chains rounded up to 16).
 int sweep_tc_supported(int precision, int chains, int bs);
 int sweep_tc_rows(int chains);
-// The residual update's row tiles (256 individuals) and the floats of its
-// partial-sum slots (one per tile segment: tiles + CTAs slots of 3C x 256).
+// The residual update's row tiles (256 individuals), the floats of its
+// partial-sum slots (one per tile segment: tiles + CTAs slots of C x 256) and
+// its tiles (row tiles and ra tiles, one ticket each).
 int sweep_tc_update_tiles(int n);
 size_t sweep_tc_vpart_floats(int n, int bs, int chains, int sm_count);
+int sweep_tc_update_all_tiles(int n, int bs);
 // Work tables of the tensor-core rhs (host side), per subset b of blk_sizes:
 // rtab[b*stride + m] = first rhs CTA of 128-SNP tile m, rtab[b*stride + tiles]
 // = rhs CTAs; tiles get K splits in proportion to their pipeline stages
@@ -27,17 +29,22 @@ void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count
 // sd_k = 1 where 1/sd_k is 0) and zeroes the codes of those columns in G (their
 // x values are all 0, so no product changes).
 cudaError_t sweep_tc_prepare(int8_t *G, const Dev &D, cudaStream_t st);
-// Tiled copy of the codes for the tensor-core kernels: per subset b, code
+// Packed copy of the codes for the tensor-core kernels: per subset b, code
 // blocks qoff[b] .. qoff[b+1]-1 of 128 positions (the last one zero-padded);
-// block (q2, t) of 128 positions x 256 individuals is one contiguous
-// [128][256] byte array at Gt + (q2 * D.nvt + t) * 32768, so every TMA box
-// the kernels load is a contiguous 16 KB (update) or half of a 32 KB block
-// (rhs).  sweep_tc_code_blocks fills qoff[0..nb] and returns the block rows;
+// block (q2, t) covers 128 positions x 256 individuals (individuals past n
+// hold 0) as TC_PACKED_BLOCK bytes at Gt + (q2 * D.nvt + t) * TC_PACKED_BLOCK:
+// [4 groups of 64 individuals][128 positions][16 bytes], 2 bits per code, and
+// in each 32-bit word of a 16-byte entry the code of individual 16 w + 4 b + j
+// of the group (w the word) sits at bits 8 j + 2 b, so that
+// (word >> 2b) & 0x03030303 holds four consecutive codes as bytes.  An update
+// unit (64 positions of one block) is 4 KB, one word per converter thread; an
+// rhs stage (128 positions x 128 individuals) is 8 bytes per converter thread.
+// sweep_tc_code_blocks fills qoff[0..nb] and returns the block rows;
 // sweep_tc_tile_codes writes all nblocks = rows * D.nvt blocks from G (after
 // sweep_tc_prepare, on the same stream).
-constexpr int TC_CODE_BLOCK = 128 * 256;   // bytes of one code block
+constexpr int TC_PACKED_BLOCK = 4 * 128 * 16;   // bytes of one packed code block
 int sweep_tc_code_blocks(const int *blk_sizes, int nb, int32_t *qoff);
-cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, int8_t *Gt, long long nblocks, int sm_count,
+cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, uint8_t *Gt, long long nblocks, int sm_count,
                                 cudaStream_t st);
 // Optional per-launch event recording (eager profiling, never inside a graph):
 // before/after every launch an event pair is recorded and its kernel class
@@ -49,14 +56,11 @@ struct ProfHook {
     int n, cap;
 };
 
-// TMA descriptors of the tensor-core sweep: the tiled genotype codes in
-// 128 x 128 x 1 (individuals x positions x block, 128-byte swizzle) and
-// 256 x 64 x 1 (unswizzled) boxes; the
-// bf16 splits of delta, r and ra in 64 x rows boxes; the bf16 U terms in
-// 64 x 128 and 64 x 64 (U rows x SNPs) boxes (all 128-byte swizzle); and the
-// host copy of the rhs work table.
+// TMA descriptors of the tensor-core sweep: the bf16 splits of delta, r and
+// ra in 64 x rows boxes; the bf16 U terms in 64 x 128 and 64 x 64 (U rows x
+// SNPs) boxes (all 128-byte swizzle); and the host copy of the rhs work table.
 struct TcMaps {
-    CUtensorMap codes128, codes256, d;  // tiled codes (128 x 128 and 256 x 64 boxes), delta split
+    CUtensorMap d;                      // delta split
     CUtensorMap rsp, usp, usp64, rasp;  // residual split, U-term split (two box heights), ra split
     const int32_t *h_rtab;              // host copy of D.rtab
 };

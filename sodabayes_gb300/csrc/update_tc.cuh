@@ -10,34 +10,42 @@
 //     by the draws (delta itself for columns with sd = 0, whose codes are
 //     zero): rows term * chains + c (3 * chains of the M = 64 rows are
 //     used), K = subset positions, 64 per stage;
-//   B (N = 256) = for r, the genotype codes of 256 individuals, loaded by TMA
-//     from the tiled copy of the codes as one contiguous 16 KB (64 positions
-//     x 256 bytes; SNP-major rows n bytes apart load at about half the
-//     bandwidth when every SM streams) and widened to bf16 by
-//     the converter warps into an MN-major operand (individuals contiguous);
-//     for ra, one bf16 term of sd * U (256 rows of U), loaded by TMA straight
-//     into an MN-major operand (the factor is stored column by column);
+//   B (N = 256) = for r, the genotype codes of 256 individuals: the
+//     converter warps load them 2-bit packed (4 KB per unit) straight from
+//     global memory into registers, several units ahead, and widen them to a
+//     bf16 MN-major operand (individuals contiguous); for ra, one bf16 term of
+//     sd * U (256 rows of U), loaded by TMA straight into an MN-major operand
+//     (the factor is stored column by column);
 //   D = 64 x 256 FP32 in tensor memory (rows 16q .. in lanes 32q ..),
 //     double-buffered.
 // A tcgen05.mma costs about the same for any N up to 256, so the codes sit on
 // the N = 256 side: one instruction consumes 4 KB of codes.
 //
-// Work units: (row tile of 256 individuals, active stage) and, for ra,
-// (tile of 256 rows of U, active stage, U term); stages whose 64 positions
-// have no non-zero delta in any chain are inactive, and an upper-triangular
-// factor meets a row tile only from its first row on.  The units are laid
-// out row tiles first and split evenly over the CTAs (one per SM); a CTA's
+// Work units: (row tile of 256 individuals, stage of 64 positions) and, for
+// ra, (tile of 256 rows of U, stage, U term); an upper-triangular factor meets
+// an ra tile only from its first row on.  The plan depends on the subset's
+// shape alone, so it is made, and the first code words are loaded, before
+// the draws of this subset complete.  The units are laid out row tiles first
+// and split evenly over the CTAs (stream-K, one CTA per SM); a CTA's
 // consecutive units of one tile form a segment, whose accumulator rows go to
-// vpart as FP32 partial sums.  After a grid-wide barrier (one CTA per SM, all
-// resident; the wait is bounded) every CTA takes an equal share of the
-// (128-element half tile, chain) pairs: it adds the pair's segments in
-// segment order (deterministic) and applies hi + mid + lo and the centring
-// term sum_j x0_j delta_j (FP64) to the FP64 residuals.
+// vpart as FP32 partial sums (hi + mid + lo per chain).  Each CTA then takes
+// a ticket for the segment's tile; the CTA that holds a tile's last segment
+// completes it once its own work is done, with all its warps: it adds the
+// tile's segments in segment order (deterministic), the centring term
+// sum_j x0_j delta_j (FP64), and writes the FP64 residuals.  No CTA waits for
+// another.
 //
 // Warp roles (mbarrier hand-offs, every wait bounded): warp 8 issues the TMA
 // loads, warps 0-7 widen the codes, warp 9 issues the MMAs, warps 10-13
-// reduce the centring term and move finished accumulators to vpart; all
-// warps then take part in the reductions.
+// reduce the centring term and move finished accumulators to vpart.  Per
+// unit s (A slot s % TV_NA, B slot s % TV_NOB):
+//   producer: wait A slot free (MMAs of s - TV_NA) and B slot free (MMAs of
+//     s - TV_NOB); load A (+ tx); for an ra unit load B (+ tx) on fullb, for
+//     a row unit arrive on fullb (the slot is the converters' to write);
+//   converters: wait fullb; row unit: write B from the codes; arrive on conv;
+//   MMA: wait conv and fulla; 4 MMAs; commit to opfree and emptya.
+// Every wait is at most one phase behind its barrier, so the parity waits are
+// exact (checked by a CPU model of this protocol in the tests).
 #pragma once
 
 namespace soda {
@@ -46,13 +54,14 @@ constexpr int TV_N = 256;          // individuals per row tile / rows of U per r
 constexpr int TV_K = 64;           // subset positions per stage
 constexpr int TV_M = 64;           // MMA M (the 3 * chains <= 48 rows of the delta split)
 constexpr int TV_NA = 4;           // delta-split tiles (operand A) in flight
-constexpr int TV_NC = 4;           // code tiles in flight
-constexpr int TV_NOB = 2;          // B operands
+constexpr int TV_NOB = 4;          // B operands
+constexpr int TV_PF = 4;           // packed code words each converter thread holds in flight
 constexpr int TV_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
 constexpr int TV_MAXRA = 64;       // ra tiles per subset
 constexpr int TV_THREADS = 448;    // 8 converter warps, TMA, MMA, 4 epilogue warps
+constexpr int TV_NW = TV_THREADS / 32;
 constexpr int TV_MAXG = 512;       // CTAs (one per SM)
-constexpr int TV_WROW = 1, TV_WRA = 1;   // unit weights of the split (row / ra units)
+constexpr int TV_MAXPEND = 8;      // tiles a CTA completes after its roles
 constexpr int TV_CONV = 256;
 constexpr int TV_CONV_WARPS = TV_CONV / 32;   // each converter warp arrives once per unit
 constexpr int TV_WARP_TMA = 8, TV_WARP_MMA = 9, TV_WARP_EPI = 10;
@@ -66,27 +75,26 @@ struct UpdTc {
     // the MMA reads is the target of a TMA load in flight (rows past NB are never written)
     static constexpr int ASTRIDE = TV_M * 128;
     static constexpr int AREG = TV_NA * ASTRIDE;
-    static constexpr int RAW_C = TV_K * TV_N;          // codes: 64 positions x 256 individuals, unswizzled
-    static constexpr int C0 = AREG;
     static constexpr int BOP = TV_K * TV_N * 2;        // B operand: 64 x 256 bf16
-    static constexpr int BOP0 = C0 + TV_NC * RAW_C;
+    static constexpr int BOP0 = AREG;
     // epilogue staging: the accumulator rows in use, all 256 columns (row stride 257 floats)
     static constexpr int STG0 = BOP0 + TV_NOB * BOP;
     static constexpr int STG = ((ROWS * (TV_N + 1) * 4 + 1023) / 1024) * 1024;
     static constexpr size_t SMEM = 1024 + (size_t)STG0 + (size_t)STG;
-    static_assert(RAW_A % 1024 == 0 && AREG % 1024 == 0 && RAW_C % 1024 == 0, "buffer alignment");
+    static_assert(RAW_A % 1024 == 0 && AREG % 1024 == 0 && BOP % 1024 == 0, "buffer alignment");
     static_assert(NB <= TV_M, "delta split rows exceed the MMA's M");
+    static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 
 // Units of one subset, as every role decodes them.
 struct UnitPlan {
-    int nact, nvt, nra, R, W;        // active stages, row tiles, ra tiles, row units, all units
-    int qs[TV_MAXRA];                // first active stage of each ra tile
+    int nq, nvt, nra, R, W;          // stages, row tiles, ra tiles, row units, all units
+    int qs[TV_MAXRA];                // first stage of each ra tile
     int pref[TV_MAXRA + 1];          // first ra unit of each ra tile (relative to R)
 };
 
 struct Unit {
-    int kind, tile, q, term;         // kind 0: r, 1: ra; tile; index into the active stages; U term
+    int kind, tile, q, term;         // kind 0: r, 1: ra; tile; stage; U term
 };
 
 __device__ __forceinline__ Unit decode_unit(const UnitPlan &P, int u, int &ra_hint)
@@ -94,8 +102,8 @@ __device__ __forceinline__ Unit decode_unit(const UnitPlan &P, int u, int &ra_hi
     Unit x;
     if (u < P.R) {
         x.kind = 0;
-        x.tile = u / P.nact;
-        x.q = u - x.tile * P.nact;
+        x.tile = u / P.nq;
+        x.q = u - x.tile * P.nq;
         x.term = 0;
         return x;
     }
@@ -118,8 +126,8 @@ __device__ __forceinline__ Unit decode_unit_bs(const UnitPlan &P, int u)
     Unit x;
     if (u < P.R) {
         x.kind = 0;
-        x.tile = u / P.nact;
-        x.q = u - x.tile * P.nact;
+        x.tile = u / P.nq;
+        x.q = u - x.tile * P.nq;
         x.term = 0;
         return x;
     }
@@ -138,14 +146,10 @@ __device__ __forceinline__ Unit decode_unit_bs(const UnitPlan &P, int u)
     return x;
 }
 
-// First unit of CTA q when the units are split over G CTAs in equal shares of
-// weight (row units TV_WROW, ra units TV_WRA).
+// First unit of CTA q when the W units are split over G CTAs in equal shares.
 __device__ __forceinline__ int split_bound(const UnitPlan &P, int q, int G)
 {
-    const long long wt = (long long)TV_WROW * P.R + (long long)TV_WRA * (P.W - P.R);
-    const long long x = ((long long)q * wt) / G;
-    if (x <= (long long)TV_WROW * P.R) return (int)((x + TV_WROW - 1) / TV_WROW);
-    return P.R + (int)((x - (long long)TV_WROW * P.R + TV_WRA - 1) / TV_WRA);
+    return (int)(((long long)q * P.W) / G);
 }
 
 // CTA holding unit u: the last q with bnd[q] <= u.
@@ -188,173 +192,163 @@ __device__ __forceinline__ void update_k0(const Dev &D, int b, int t, double *s_
         for (int q = 0; q < PARTS; ++q) s += s_k0p[t * PARTS + q];
         s_k0[t] = s;
     }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
 }
 
 // Units [u0, u1) of global tile tg (row tiles, then ra tiles).
-__device__ __forceinline__ void tile_units(const UnitPlan &P, int tg, long long &u0, long long &u1)
+__device__ __forceinline__ void tile_units(const UnitPlan &P, int tg, int &u0, int &u1)
 {
     if (tg < P.nvt) {
-        u0 = (long long)tg * P.nact;
-        u1 = u0 + P.nact;
+        u0 = tg * P.nq;
+        u1 = u0 + P.nq;
     } else {
         u0 = P.R + P.pref[tg - P.nvt];
         u1 = P.R + P.pref[tg - P.nvt + 1];
     }
 }
 
-// One (128-element half tile, chain) pair of the reductions: global tile tg
-// (row tiles, then ra tiles), half h, chain c, the CTAs sl..sh whose segments
-// cover the tile (sl > sh: no unit touched it, nothing changes) and the old
-// values (r or ra) of the half, lane l holding elements l + 32k.  Everything
-// here is known before the grid barrier: nothing else writes those values
-// during the update.
-struct PairJob {
-    int tg, h, c, sl, sh;
-    double rold[4];
+// A tile this CTA completes: global tile tg, and the CTAs sl .. sh whose
+// segments cover it (those holding units; when there are fewer units than
+// CTAs some hold none and have no segment).
+struct PendTile {
+    int tg, sl, sh;
 };
 
-template <int CT>
-__device__ __forceinline__ void pair_prepare(const Dev &D, const UnitPlan &P, const int *bnd, int G, int pr, int npair,
-                                             int N, PairJob &j)
-{
-    j.tg = j.h = j.c = 0;
-    j.sl = 1;
-    j.sh = 0;
-    if (pr >= npair) return;
-    const int hh = pr / CT;
-    j.c = pr - hh * CT;
-    j.tg = hh >> 1;
-    j.h = hh & 1;
-    long long u0, u1;
-    tile_units(P, j.tg, u0, u1);
-    if (u1 <= u0) return;
-    j.sl = unit_cta(bnd, (int)u0, G);
-    j.sh = unit_cta(bnd, (int)u1 - 1, G);
-    const int lane = threadIdx.x & 31;
-    const bool is_r = j.tg < P.nvt;
-    const int tile = is_r ? j.tg : j.tg - P.nvt;
-    const int lim = is_r ? D.n : min(N, D.bs);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int i = tile * TV_N + j.h * 128 + lane + 32 * k;
-        j.rold[k] = 0.0;
-        if (i < lim) j.rold[k] = is_r ? __ldcg(D.r + (size_t)j.c * D.ldr + i) : __ldcg(D.ra + (size_t)j.c * D.ldra + i);
-    }
-}
+// Completes the pending tiles: every (tile, 128-element half, chain) triple
+// is one job; warps w0 .. w0 + nw - 1 of the CTA take TV_JPW jobs at a time
+// (one round for a tile of 16 chains on 14 warps), with the loads of all of
+// them (old residuals, the segments in vpart) in flight together.  Lane l
+// adds elements l + 32k of the segments in segment order and applies them:
+// r, its bf16 split and the 128-row partial sum of r for a row tile, ra and
+// its split for an ra tile.
+constexpr int TV_JPW = 3;
 
-// The segments of job j from CTA q0 + u (u < 4) of its range: loads only.
 template <int CT>
-__device__ __forceinline__ void pair_load4(const Dev &D, const int *bnd, const PairJob &j, int q0, float (&v)[4][4])
+__device__ __forceinline__ void tiles_complete(const Dev &D, const UnitPlan &P, const int *bnd, const PendTile *pend,
+                                               int npend, const double *s_k0, int N, int w0, int nw)
 {
-    const int lane = threadIdx.x & 31;
+    constexpr int JOBS = 2 * CT;   // per tile
+    const int lane = threadIdx.x & 31, ew = (threadIdx.x >> 5) - w0;
+    const int njob = npend * JOBS;
+    for (int j0 = TV_JPW * ew; j0 < njob; j0 += TV_JPW * nw) {
+        double rold[TV_JPW][4];
+        float acc[TV_JPW][4];
+        int tg[TV_JPW], c[TV_JPW], h[TV_JPW], lim[TV_JPW], sl[TV_JPW], sh[TV_JPW];
+        bool isr[TV_JPW], live[TV_JPW];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int q = q0 + u;
-        const bool ok = q <= j.sh && bnd[q] < bnd[q + 1];   // CTAs without units have no slot
-        const float *pp = D.vpart + ((size_t)(j.tg + q) * CT + j.c) * TV_N + j.h * 128 + lane;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) v[u][k] = ok ? __ldcg(pp + 32 * k) : 0.0f;
-    }
-}
-
-// Applies the update of job j from its segment sum acc: r, its bf16 split and
-// the 128-row partial sum of r for a row tile, ra and its split for an ra tile.
-template <int CT>
-__device__ __forceinline__ void pair_finish(const Dev &D, const UnitPlan &P, const PairJob &j, const float (&acc)[4],
-                                            const double *s_k0, int N)
-{
-    const int lane = threadIdx.x & 31;
-    const bool is_r = j.tg < P.nvt;
-    const int tile = is_r ? j.tg : j.tg - P.nvt;
-    const int lim = is_r ? D.n : min(N, D.bs);
-    float part = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int i = tile * TV_N + j.h * 128 + lane + 32 * k;
-        if (is_r) {
-            const double rn = j.rold[k] + ((double)acc[k] + s_k0[j.c]);
-            if (i < lim) {
-                const size_t o = (size_t)j.c * D.ldr + i;
-                D.r[o] = rn;
-                split_store(D.rsp, o, (size_t)D.chains * D.ldr, (float)rn);
-                part += (float)rn;
-            }
-        } else if (i < lim) {
-            store_ra(D, j.c, i, j.rold[k] + (double)acc[k]);
-        }
-    }
-    if (is_r) {
-        const float ws = warp_sumf(part);
-        if (lane == 0 && 2 * tile + j.h < D.nr_ctas) D.rsum[(size_t)j.c * D.nr_ctas + 2 * tile + j.h] = (double)ws;
-    }
-}
-
-// Two jobs of one warp: the segments of each are added in segment order (the
-// same order for any grouping), with the loads of both jobs issued together.
-template <int CT>
-__device__ __forceinline__ void pair_reduce2(const Dev &D, const UnitPlan &P, const int *bnd, const PairJob &ja,
-                                             const PairJob &jb, const double *s_k0, int N)
-{
-    float aa[4] = {0.0f, 0.0f, 0.0f, 0.0f}, ab[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    const int na = ja.sh - ja.sl + 1, nb_ = jb.sh - jb.sl + 1, nmax = max(na, nb_);
-    for (int q0 = 0; q0 < nmax; q0 += 4) {
-        float va[4][4], vb[4][4];
-        pair_load4<CT>(D, bnd, ja, ja.sl + q0, va);
-        pair_load4<CT>(D, bnd, jb, jb.sl + q0, vb);
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int e = 0; e < TV_JPW; ++e) {
+            const int j = j0 + e;
+            live[e] = j < njob;
+            const PendTile pt = pend[live[e] ? j / JOBS : 0];
+            const int pr = j % JOBS;
+            tg[e] = pt.tg;
+            sl[e] = pt.sl;
+            sh[e] = live[e] ? pt.sh : pt.sl - 1;
+            h[e] = pr / CT;
+            c[e] = pr - h[e] * CT;
+            isr[e] = tg[e] < P.nvt;
+            lim[e] = isr[e] ? D.n : min(N, D.bs);
+            const int tile = isr[e] ? tg[e] : tg[e] - P.nvt;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                aa[k] += va[u][k];
-                ab[k] += vb[u][k];
+                const int i = tile * TV_N + h[e] * 128 + lane + 32 * k;
+                rold[e][k] = 0.0;
+                acc[e][k] = 0.0f;
+                if (live[e] && i < lim[e])
+                    rold[e][k] = isr[e] ? __ldcg(D.r + (size_t)c[e] * D.ldr + i)
+                                        : __ldcg(D.ra + (size_t)c[e] * D.ldra + i);
             }
+        }
+        // the segments, two per job loaded together (a tile rarely spans more than two CTAs)
+        int span = 0;
+#pragma unroll
+        for (int e = 0; e < TV_JPW; ++e) span = max(span, sh[e] - sl[e] + 1);
+        for (int d = 0; d < span; d += 2) {
+            float v[TV_JPW][2][4];
+#pragma unroll
+            for (int e = 0; e < TV_JPW; ++e)
+#pragma unroll
+                for (int dd = 0; dd < 2; ++dd) {
+                    const int q = sl[e] + d + dd;
+                    const bool ok = q <= sh[e] && bnd[q] < bnd[q + 1];
+                    const float *pp = D.vpart + ((size_t)(tg[e] + q) * CT + c[e]) * TV_N + h[e] * 128 + lane;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) v[e][dd][k] = ok ? __ldcg(pp + 32 * k) : 0.0f;
+                }
+#pragma unroll
+            for (int e = 0; e < TV_JPW; ++e)
+#pragma unroll
+                for (int dd = 0; dd < 2; ++dd)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) acc[e][k] += v[e][dd][k];
+        }
+#pragma unroll
+        for (int e = 0; e < TV_JPW; ++e) {
+            if (!live[e]) break;
+            const int tile = isr[e] ? tg[e] : tg[e] - P.nvt;
+            float part = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int i = tile * TV_N + h[e] * 128 + lane + 32 * k;
+                if (isr[e]) {
+                    const double rn = rold[e][k] + ((double)acc[e][k] + s_k0[c[e]]);
+                    if (i < lim[e]) {
+                        const size_t o = (size_t)c[e] * D.ldr + i;
+                        D.r[o] = rn;
+                        split_store(D.rsp, o, (size_t)D.chains * D.ldr, (float)rn);
+                        part += (float)rn;
+                    }
+                } else if (i < lim[e]) {
+                    store_ra(D, c[e], i, rold[e][k] + (double)acc[e][k]);
+                }
+            }
+            if (isr[e]) {
+                const float ws = warp_sumf(part);
+                if (lane == 0 && 2 * tile + h[e] < D.nr_ctas)
+                    D.rsum[(size_t)c[e] * D.nr_ctas + 2 * tile + h[e]] = (double)ws;
+            }
+        }
     }
-    if (na > 0) pair_finish<CT>(D, P, ja, aa, s_k0, N);
-    if (nb_ > 0) pair_finish<CT>(D, P, jb, ab, s_k0, N);
 }
 
-// Grid-wide barrier of the G CTAs of one launch on a monotonic counter (each
-// launch adds G); bounded by %globaltimer (20 ms), false on time-out.
-__device__ __forceinline__ bool update_grid_sync(unsigned long long *ctr, unsigned G)
+// Packed code word of a converter thread for row unit u: positions of stage q
+// of row tile `tile`; the thread takes position k = tid % 64 and individuals
+// 64 j .. 64 j + 63, j = tid / 64, of the tile (16 bytes: 64 codes of 2 bits).
+__device__ __forceinline__ uint4 update_code_word(const Dev &D, const UnitPlan &P, int cblk, int u, int tid)
 {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned long long old = atomicAdd(ctr, 1ull);
-        const unsigned long long target = (old / G + 1) * G;
-        const uint64_t t0 = tc::globaltimer_ns();
-        int ok = 1;
-        for (;;) {
-            unsigned long long v;
-            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ctr) : "memory");
-            if (v >= target) break;
-            if (tc::globaltimer_ns() - t0 > 20000000ull) {
-                ok = 0;
-                break;
-            }
-            __nanosleep(64);
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
+    const int tile = u / P.nq, q = u - tile * P.nq;
+    const int k = tid & 63, j = tid >> 6;
+    const size_t blk = (size_t)(cblk + (q >> 1)) * P.nvt + tile;
+    const uint4 *w = reinterpret_cast<const uint4 *>(D.gpk + blk * TC_PACKED_BLOCK) + j * TC_TM + 64 * (q & 1) + k;
+    uint4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(w));
+    return v;
+}
+
+// Widens one 32-bit word of 16 packed codes (individuals 4b + j at bits
+// 8j + 2b) into the bf16 of two 16-byte operand chunks (individuals 0-7, 8-15).
+__device__ __forceinline__ void unpack16(uint32_t w, uint4 &lo, uint4 &hi)
+{
+    uint32_t o[8];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) tc::codes_to_bf16x4((w >> (2 * b)) & 0x03030303u, o[2 * b], o[2 * b + 1]);
+    lo = make_uint4(o[0], o[1], o[2], o[3]);
+    hi = make_uint4(o[4], o[5], o[6], o[7]);
 }
 
 template <int CT>
 __global__ void __launch_bounds__(TV_THREADS, 1)
-    k_update_tc(const __grid_constant__ CUtensorMap tm_codes, const __grid_constant__ CUtensorMap tm_d,
-                const __grid_constant__ CUtensorMap tm_u, Dev D, int b)
+    k_update_tc(const __grid_constant__ CUtensorMap tm_d, const __grid_constant__ CUtensorMap tm_u, Dev D, int b)
 {
     using T = UpdTc<CT>;
-    constexpr int NW = TV_THREADS / 32;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
-    __shared__ uint64_t s_fulla[TV_NA], s_emptya[TV_NA], s_fullc[TV_NC], s_emptyc[TV_NC];
-    __shared__ uint64_t s_conv[TV_NOB], s_opfree[TV_NOB], s_segdone[2], s_dfree[2];
+    __shared__ uint64_t s_fulla[TV_NA], s_emptya[TV_NA], s_fullb[TV_NOB], s_conv[TV_NOB], s_opfree[TV_NOB];
+    __shared__ uint64_t s_segdone[2], s_dfree[2];
     __shared__ uint32_t s_tmem;
-    __shared__ int s_err, s_wcnt[NW];
-    __shared__ int s_act[TV_MAXQ];
+    __shared__ int s_err, s_last, s_npend;
+    __shared__ PendTile s_pend[TV_MAXPEND];
     __shared__ UnitPlan s_plan;
     __shared__ double s_k0p[128], s_k0[CT];
     __shared__ int s_bnd[TV_MAXG + 1];
@@ -366,87 +360,51 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     const int nq = (N + TV_K - 1) / TV_K;
     const bool pd = D.blk_pd[b] != 0;
     const int cblk = D.qoff[b];   // the subset's first code block row (set up before the sweep)
-    tc::pdl_trigger();
-    tc::pdl_wait();   // the draws of this subset are complete
 
-    // active stages in subset order (nq <= 256), and the unit plan
-    {
-        bool f = false;
-        if (tid < nq) {
-            const int jb = tid * TV_K, e = min(N, jb + TV_K);
-            if (e - jb == TV_K) {   // full stage: four 16-byte loads
-                const uint4 *q = reinterpret_cast<const uint4 *>(D.nzflag + jb);
-                const uint4 a = q[0], bq = q[1], c2 = q[2], d2 = q[3];
-                f = ((a.x | a.y | a.z | a.w) | (bq.x | bq.y | bq.z | bq.w) | (c2.x | c2.y | c2.z | c2.w) |
-                     (d2.x | d2.y | d2.z | d2.w)) != 0u;
-            } else {
-                uint32_t o = 0;
-                for (int jk = jb; jk < e; ++jk) o |= D.nzflag[jk];
-                f = o != 0u;
-            }
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) s_wcnt[warp] = __popc(m);
-        __syncthreads();
-        int before = 0, nact = 0;
-        for (int q = 0; q < NW; ++q) {
-            if (q < warp) before += s_wcnt[q];
-            nact += s_wcnt[q];
-        }
-        if (f) s_act[before + __popc(m & ((1u << lane) - 1u))] = tid;
-        __syncthreads();
-        if (warp == 0) {
-            // ra tile a (<= 64 of them, two per lane): its first active stage (upper triangular: rows
-            // 256a .. meet positions from 256a on, stages >= 4a) and an exclusive scan of its units
-            UnitPlan &P = s_plan;
-            const int nra = (N + TV_N - 1) / TV_N;
-            int cnt[2], qs[2];
+    // the unit plan: the subset's shape only (set up before the sweep), so it overlaps the draws
+    if (warp == 0) {
+        // ra tile a (<= 64 of them, two per lane): its first stage (upper triangular: rows 256a ..
+        // meet positions from 256a on, stages >= 4a) and an exclusive scan of its units
+        UnitPlan &P = s_plan;
+        const int nra = (N + TV_N - 1) / TV_N;
+        int cnt[2], qs[2];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int a = 2 * lane + h;
-                int lo = 0, hi = nact;
-                if (pd) {
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (s_act[mid] < 4 * a) lo = mid + 1;
-                        else hi = mid;
-                    }
-                }
-                qs[h] = lo;
-                cnt[h] = a < nra ? 3 * (nact - lo) : 0;
-            }
-            const int pair = cnt[0] + cnt[1];
-            int incl = pair;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            const int excl = incl - pair;
-            if (2 * lane < TV_MAXRA) {
-                P.qs[2 * lane] = qs[0];
-                P.pref[2 * lane] = excl;
-                P.qs[2 * lane + 1] = qs[1];
-                P.pref[2 * lane + 1] = excl + cnt[0];
-            }
-            const int total = __shfl_sync(0xffffffffu, incl, 31);
-            if (lane == 0) {
-                P.nact = nact;
-                P.nvt = D.nvt;
-                P.nra = nra;
-                P.R = P.nvt * nact;
-                P.pref[TV_MAXRA] = total;
-                P.pref[nra] = total;
-                P.W = P.R + total;
-                s_err = 0;
-            }
+        for (int h = 0; h < 2; ++h) {
+            const int a = 2 * lane + h;
+            qs[h] = pd ? min(4 * a, nq) : 0;
+            cnt[h] = a < nra ? 3 * (nq - qs[h]) : 0;
         }
-        __syncthreads();
+        const int pair = cnt[0] + cnt[1];
+        int incl = pair;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int excl = incl - pair;
+        P.qs[2 * lane] = qs[0];
+        P.pref[2 * lane] = excl;
+        P.qs[2 * lane + 1] = qs[1];
+        P.pref[2 * lane + 1] = excl + cnt[0];
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (lane == 0) {
+            P.nq = nq;
+            P.nvt = D.nvt;
+            P.nra = nra;
+            P.R = D.nvt * nq;
+            P.pref[TV_MAXRA] = total;
+            P.pref[nra] = total;
+            P.W = P.R + total;
+            s_err = 0;
+            s_npend = 0;
+        }
     }
+    __syncthreads();
     const UnitPlan &P = s_plan;
     const int G = gridDim.x;
     for (int q = tid; q <= G; q += TV_THREADS) s_bnd[q] = split_bound(P, q, G);
     __syncthreads();
+    tc::pdl_trigger();
     const int u_begin = s_bnd[blockIdx.x], u_end = s_bnd[blockIdx.x + 1];
     const int nu = u_end - u_begin;
     if (nu > 0) {
@@ -455,11 +413,8 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 tc::mbar_init(&s_fulla[i], 1);
                 tc::mbar_init(&s_emptya[i], 1);   // the MMAs reading the tile
             }
-            for (int i = 0; i < TV_NC; ++i) {
-                tc::mbar_init(&s_fullc[i], 1);
-                tc::mbar_init(&s_emptyc[i], TV_CONV_WARPS);   // the converter warps
-            }
             for (int i = 0; i < TV_NOB; ++i) {
+                tc::mbar_init(&s_fullb[i], 1);    // the producer: U tile landed, or slot handed to the converters
                 tc::mbar_init(&s_conv[i], TV_CONV_WARPS);
                 tc::mbar_init(&s_opfree[i], 1);
             }
@@ -477,30 +432,22 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
 
         if (warp == TV_WARP_TMA) {
             // the warp decodes 32 units at a time into registers (lane l: unit s0 + l); lane 0 issues
-            // their loads, taking each unit's coordinates by shuffle, so that no chain of shared-memory
-            // loads sits between two issues
+            // their loads, taking each unit's coordinates by shuffle
             if (lane == 0) {
-                tc::tma_prefetch_desc(&tm_codes);
                 tc::tma_prefetch_desc(&tm_d);
                 tc::tma_prefetch_desc(&tm_u);
             }
+            tc::pdl_wait();   // the A tiles are the draws' delta split
             bool ok = true;
+            int issued = 0;
             for (int s0 = 0; s0 < nu && ok; s0 += 32) {
                 int kind = 0, ax = 0, cy = 0, cz = 0;
                 if (s0 + lane < nu) {
                     const Unit x = decode_unit_bs(P, u_begin + s0 + lane);
-                    const int st = s_act[x.q];
                     kind = x.kind;
-                    ax = st * TV_K;
-                    if (x.kind == 0) {
-                        // one contiguous 16 KB: half st % 2 of code block (st / 2, tile)
-                        cy = (st & 1) * TV_K;
-                        cz = (cblk + (st >> 1)) * P.nvt + x.tile;
-                    } else {
-                        // four boxes of 64 rows of U x 64 positions from row 256 tile, term's plane
-                        cy = x.tile * TV_N;
-                        cz = x.term * D.p + ls + ax;
-                    }
+                    ax = x.q * TV_K;
+                    cy = x.tile * TV_N;                 // ra: four boxes of 64 rows of U x 64 positions
+                    cz = x.term * D.p + ls + ax;        //     from row 256 tile, term's plane
                 }
                 const int m = min(32, nu - s0);
                 for (int i = 0; i < m; ++i) {
@@ -508,41 +455,39 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     const int kd = __shfl_sync(0xffffffffu, kind, i), k0 = __shfl_sync(0xffffffffu, ax, i);
                     const int y = __shfl_sync(0xffffffffu, cy, i), z = __shfl_sync(0xffffffffu, cz, i);
                     if (lane == 0) {
-                        const int a = s % TV_NA, cb = s % TV_NC, ob = s % TV_NOB;
-                        // the slots' previous tiles are consumed: A by the MMAs of unit s - TV_NA, the
-                        // code tile by the converters of unit s - TV_NC and, for an ra unit (whose B
-                        // operand TMA writes), B by the MMAs of unit s - TV_NOB
+                        const int a = s % TV_NA, ob = s % TV_NOB;
+                        // the slots' previous tiles are consumed: A by the MMAs of unit s - TV_NA, B by
+                        // the MMAs of unit s - TV_NOB
                         ok = s < TV_NA || tc::mbar_wait(&s_emptya[a], ((s / TV_NA) - 1) & 1);
-                        if (ok && s >= TV_NC) ok = tc::mbar_wait(&s_emptyc[cb], ((s / TV_NC) - 1) & 1);
-                        if (ok && kd == 1 && s >= TV_NOB) {
-                            // a parity wait for the MMAs of unit s - NOB is only sound once those of
-                            // s - 2 NOB are complete (else the barrier may be a whole phase behind);
-                            // with more A slots than 2 NOB nothing else guarantees that, so wait for
-                            // them on their A slot first
-                            if (TV_NA > 2 * TV_NOB && s >= 2 * TV_NOB)
-                                ok = tc::mbar_wait(&s_emptya[(s - 2 * TV_NOB) % TV_NA], ((s - 2 * TV_NOB) / TV_NA) & 1);
-                            if (ok) ok = tc::mbar_wait(&s_opfree[ob], ((s - TV_NOB) / TV_NOB) & 1);
-                        }
+                        if (ok && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s / TV_NOB) - 1) & 1);
                         if (!ok) {
                             s_err = 11;
                         } else {
                             tc::mbar_expect_tx(&s_fulla[a], T::RAW_A);
                             tc::tma_load_2d(raw0 + (size_t)a * T::ASTRIDE, &tm_d, k0, 0, &s_fulla[a]);
-                            if (kd == 0) {
-                                tc::mbar_expect_tx(&s_fullc[cb], T::RAW_C);
-                                tc::tma_load_3d(raw0 + T::C0 + (size_t)cb * T::RAW_C, &tm_codes, 0, y, z, &s_fullc[cb]);
-                            } else {
+                            if (kd == 1) {
                                 unsigned char *bo = bop0 + (size_t)ob * T::BOP;   // MN atoms 8 KB apart
-                                tc::mbar_expect_tx(&s_fullc[cb], T::BOP);
-    #pragma unroll
+                                tc::mbar_expect_tx(&s_fullb[ob], T::BOP);
+#pragma unroll
                                 for (int h = 0; h < 4; ++h)
-                                    tc::tma_load_2d(bo + h * 8192, &tm_u, y + 64 * h, z, &s_fullc[cb]);
+                                    tc::tma_load_2d(bo + h * 8192, &tm_u, y + 64 * h, z, &s_fullb[ob]);
+                            } else {
+                                tc::mbar_arrive(&s_fullb[ob]);
                             }
+                            issued = s + 1;
                         }
                     }
                     ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
                     if (!ok) break;
                 }
+            }
+            // no copy may still be in flight into this CTA's shared memory when it exits: wait (bounded)
+            // for the last loads issued into every slot (already complete unless a wait above gave up)
+            if (lane == 0 && issued > 0) {
+                for (int s = max(0, issued - TV_NA); s < issued; ++s)
+                    if (!tc::mbar_wait(&s_fulla[s % TV_NA], (s / TV_NA) & 1)) s_err = 21;
+                for (int s = max(0, issued - TV_NOB); s < issued; ++s)
+                    if (!tc::mbar_wait(&s_fullb[s % TV_NOB], (s / TV_NOB) & 1)) s_err = 21;
             }
         } else if (warp == TV_WARP_MMA) {
             if (lane == 0) {
@@ -570,14 +515,12 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         ok = tc::mbar_wait(&s_fulla[a], (s / TV_NA) & 1);
                         if (!ok) s_err = 18;
                     }
-                    if (!ok) {
-                        break;
-                    }
+                    if (!ok) break;
                     tc::fence_after_sync();
                     const uint32_t a0 = tc::smem_u32(raw0 + (size_t)a * T::ASTRIDE);
                     const uint32_t b0 = tc::smem_u32(bop0 + (size_t)ob * T::BOP);
                     const uint32_t dt = tm + 256 * (seg & 1);
-    #pragma unroll
+#pragma unroll
                     for (int kk = 0; kk < TV_K / 16; ++kk) {
                         // codes operand: K groups of four atoms (4096 bytes), atoms 1024 apart;
                         // U operand: atoms of eight K groups (8192 bytes), K groups 1024 apart
@@ -591,59 +534,56 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
             }
         } else if (warp < TV_WARP_TMA) {
-            // converters: 16-byte chunk (position k, individuals 16c .. 16c+15) -> 32 bytes of bf16 in
-            // the MN-major operand: K group k/8 (4096 bytes: four atoms of 64 individuals), row k%8,
-            // chunks 2(c%4), 2(c%4)+1 of atom c/4, XOR-swizzled by the row
-            int hint = 0;
+            // converters.  Row units come first in the unit order, so this CTA's row units are
+            // u_begin .. min(u_end, R) - 1; the thread keeps the packed words of the next TV_PF of
+            // them in registers (the codes are not written by any kernel of the sweep, so the first
+            // ones are loaded while the draws still run).  Thread tid writes position k = tid % 64
+            // (K group k / 8, row k % 8) of atom j = tid / 64 (individuals 64 j ..): eight 16-byte
+            // chunks, chunk cc at (cc ^ row) in the 128-byte swizzled row.
+            const int nrow = max(0, min(u_end, P.R) - u_begin);
+            uint4 pf[TV_PF];
+#pragma unroll
+            for (int i = 0; i < TV_PF; ++i)
+                pf[i] = i < nrow ? update_code_word(D, P, cblk, u_begin + i, tid) : make_uint4(0u, 0u, 0u, 0u);
+            const int k = tid & 63, j = tid >> 6, row = k & 7;
             for (int s = 0; s < nu; ++s) {
-                const int cb = s % TV_NC, ob = s % TV_NOB;
-                const Unit x = decode_unit(P, u_begin + s, hint);
-                bool ok = tc::mbar_wait(&s_fullc[cb], (s / TV_NC) & 1);
-                if (x.kind == 0) {
-                    if (ok && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s - TV_NOB) / TV_NOB) & 1);
-                    ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
-                    if (!ok) {
-                        s_err = 13;
-                        break;
-                    }
-                    const unsigned char *rc = raw0 + T::C0 + (size_t)cb * T::RAW_C;
-                    unsigned char *bo = bop0 + (size_t)ob * T::BOP;
-    #pragma unroll
-                    for (int h4 = 0; h4 < 4; ++h4) {
-                        const int q = tid + TV_CONV * h4, k = q >> 4, c = q & 15;
-                        const uint4 w = *reinterpret_cast<const uint4 *>(rc + k * TV_N + 16 * c);
-                        uint32_t o[8];
-                        tc::codes_to_bf16x4(w.x, o[0], o[1]);
-                        tc::codes_to_bf16x4(w.y, o[2], o[3]);
-                        tc::codes_to_bf16x4(w.z, o[4], o[5]);
-                        tc::codes_to_bf16x4(w.w, o[6], o[7]);
-                        // lanes with c % 8 >= 4 store their two chunks in the other order, so that the
-                        // eight lanes of each store phase meet eight different 16-byte bank groups
-                        const int r = k & 7, j0 = 2 * (c & 3), sw = (c >> 2) & 1;
-                        unsigned char *ob_ = bo + (k >> 3) * 4096 + (c >> 2) * 1024 + r * 128;
-                        const uint4 w0 = make_uint4(o[0], o[1], o[2], o[3]), w1 = make_uint4(o[4], o[5], o[6], o[7]);
-                        *reinterpret_cast<uint4 *>(ob_ + (((j0 + sw) ^ r) << 4)) = sw ? w1 : w0;
-                        *reinterpret_cast<uint4 *>(ob_ + (((j0 + 1 - sw) ^ r) << 4)) = sw ? w0 : w1;
-                    }
-                    tc::fence_async_smem();
-                } else if (!__all_sync(0xffffffffu, ok)) {
-                    s_err = 14;
+                const int ob = s % TV_NOB;
+                bool ok = tc::mbar_wait(&s_fullb[ob], (s / TV_NOB) & 1);
+                ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
+                if (!ok) {
+                    s_err = 13;
                     break;
                 }
-                __syncwarp();
-                if (lane == 0) {
-                    tc::mbar_arrive(&s_emptyc[cb]);
-                    tc::mbar_arrive(&s_conv[ob]);
+                if (s < nrow) {
+                    const uint4 w = pf[0];
+#pragma unroll
+                    for (int i = 0; i + 1 < TV_PF; ++i) pf[i] = pf[i + 1];
+                    pf[TV_PF - 1] = s + TV_PF < nrow ? update_code_word(D, P, cblk, u_begin + s + TV_PF, tid)
+                                                     : make_uint4(0u, 0u, 0u, 0u);
+                    unsigned char *orow = bop0 + (size_t)ob * T::BOP + (k >> 3) * 4096 + j * 1024 + row * 128;
+                    const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        uint4 c0, c1;
+                        unpack16(ww[q], c0, c1);
+                        *reinterpret_cast<uint4 *>(orow + (((2 * q) ^ row) << 4)) = c0;
+                        *reinterpret_cast<uint4 *>(orow + (((2 * q + 1) ^ row) << 4)) = c1;
+                    }
+                    tc::fence_async_smem();
                 }
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
             }
         } else {
             // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. for all 256
-            // columns (an M = 64 accumulator keeps rows 16q .. 16q+15 in lanes 32q .. 32q+15) and stores
-            // rows < 3 * chains to the segment's slot of vpart
+            // columns (an M = 64 accumulator keeps rows 16q .. 16q+15 in lanes 32q .. 32q+15), stores
+            // hi + mid + lo per chain to the segment's slot of vpart, and takes the tile's ticket; a
+            // tile whose last segment this CTA holds is completed after the roles
+            tc::pdl_wait();   // the draws' centring sums; r of the previous update
+            const int t = tid - 32 * TV_WARP_EPI;
             const int qd = warp & 3, row = lane < 16 ? 16 * qd + lane : T::ROWS;
             float *stg = reinterpret_cast<float *>(raw0 + T::STG0);
-            // the centring term first: the reductions need it, the first segment takes several units
-            update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);
+            update_k0<CT>(D, b, t, s_k0p, s_k0);
             int hint = 0, seg = -1, pkind = -1, ptile = -1;
             for (int s = 0; s <= nu; ++s) {
                 Unit x;
@@ -660,20 +600,19 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     // all 256 columns of the rows in use to the staging buffer (32 at a time), then
                     // hi + mid + lo per chain to the slot in one coalesced pass
                     float *dst = D.vpart + (size_t)(tg + blockIdx.x) * CT * TV_N;
-                    const int t = tid - 32 * TV_WARP_EPI;
                     const uint32_t ta = tm + 256 * (seg & 1) + ((uint32_t)(32 * qd) << 16);
                     if (ok && 16 * qd < T::ROWS) {
-    #pragma unroll 1
-                        for (int j = 0; j < TV_N / 32; ++j) {
+#pragma unroll 1
+                        for (int jj = 0; jj < TV_N / 32; ++jj) {
                             float v0[8], v1[8], v2[8], v3[8];
-                            tc::tmem_ld8(ta + 32 * j, v0);
-                            tc::tmem_ld8(ta + 32 * j + 8, v1);
-                            tc::tmem_ld8(ta + 32 * j + 16, v2);
-                            tc::tmem_ld8(ta + 32 * j + 24, v3);
+                            tc::tmem_ld8(ta + 32 * jj, v0);
+                            tc::tmem_ld8(ta + 32 * jj + 8, v1);
+                            tc::tmem_ld8(ta + 32 * jj + 16, v2);
+                            tc::tmem_ld8(ta + 32 * jj + 24, v3);
                             tc::tmem_wait_ld();
                             if (row < T::ROWS) {
-                                float *sr = stg + row * (TV_N + 1) + 32 * j;
-    #pragma unroll
+                                float *sr = stg + row * (TV_N + 1) + 32 * jj;
+#pragma unroll
                                 for (int e = 0; e < 8; ++e) {
                                     sr[e] = v0[e];
                                     sr[8 + e] = v1[e];
@@ -683,16 +622,46 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                             }
                         }
                     }
+                    tc::fence_before_sync();
                     asm volatile("bar.sync 1, 128;" ::: "memory");
+                    // the accumulator is free once every lane has read it
+                    if (t == 0) tc::mbar_arrive(&s_dfree[seg & 1]);
                     for (int idx = t; idx < CT * TV_N; idx += 128) {
                         const int cc = idx >> 8, col = idx & (TV_N - 1);
                         dst[cc * TV_N + col] = (stg[cc * (TV_N + 1) + col] + stg[(CT + cc) * (TV_N + 1) + col]) +
                                                stg[(2 * CT + cc) * (TV_N + 1) + col];
                     }
-                    __threadfence();   // the slot is read after the grid barrier
-                    tc::fence_before_sync();
+                    // the segment is in vpart: take the tile's ticket
+                    int u0, u1;
+                    tile_units(P, tg, u0, u1);
+                    const int sl = unit_cta(s_bnd, u0, G), sh = unit_cta(s_bnd, u1 - 1, G);
+                    __threadfence();
                     asm volatile("bar.sync 1, 128;" ::: "memory");
-                    if (warp == TV_WARP_EPI && lane == 0) tc::mbar_arrive(&s_dfree[seg & 1]);
+                    if (t == 0) {
+                        unsigned nseg = 0;   // the CTAs holding units of the tile, one segment each
+                        for (int q = sl; q <= sh; ++q) nseg += s_bnd[q] < s_bnd[q + 1] ? 1u : 0u;
+                        const unsigned old = atomicAdd(D.uticket + tg, 1u);
+                        s_last = old + 1 == nseg;
+                        if (s_last && ok && s_npend < TV_MAXPEND) {
+                            s_pend[s_npend].tg = tg;
+                            s_pend[s_npend].sl = sl;
+                            s_pend[s_npend].sh = sh;
+                            ++s_npend;
+                            s_last = 0;
+                        }
+                    }
+                    asm volatile("bar.sync 1, 128;" ::: "memory");
+                    if (s_last && ok) {
+                        // more tiles than the pending list holds: complete this one here
+                        __threadfence();
+                        PendTile one;
+                        one.tg = tg;
+                        one.sl = sl;
+                        one.sh = sh;
+                        tiles_complete<CT>(D, P, s_bnd, &one, 1, s_k0, N, TV_WARP_EPI, 4);
+                        if (t == 0) D.uticket[tg] = 0u;   // for the next launch (stream-ordered after this one)
+                    }
+                    asm volatile("bar.sync 1, 128;" ::: "memory");
                 }
                 if (s == nu) break;
                 ++seg;
@@ -705,29 +674,15 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             tc::fence_after_sync();
             tc::tmem_dealloc(tm, 512);
         }
-    } else if (warp >= TV_WARP_EPI) {
-        update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);   // the centring term
-    }
-    // this warp's first two pairs (pr0 and pr0 + stride) prepared while the other CTAs finish
-    const int npair = 2 * (P.nvt + P.nra) * CT;
-    const int pr0 = blockIdx.x * NW + warp, stride = G * NW;
-    PairJob ja, jb;
-    pair_prepare<CT>(D, P, s_bnd, G, pr0, npair, N, ja);
-    pair_prepare<CT>(D, P, s_bnd, G, pr0 + stride, npair, N, jb);
-    // every segment is in vpart once all CTAs are here; then the reductions, an equal share of the
-    // (half tile, chain) pairs per CTA, one pair per warp at a time
-    if (!update_grid_sync(D.ugrid, (unsigned)G)) s_err = 16;
-    if (s_err) {
-        if (tid == 0) flag_err(D, s_err);
-        return;
-    }
-    for (int pr = pr0; pr < npair; pr += 2 * stride) {
-        if (pr != pr0) {
-            pair_prepare<CT>(D, P, s_bnd, G, pr, npair, N, ja);
-            pair_prepare<CT>(D, P, s_bnd, G, pr + stride, npair, N, jb);
+        // the tiles whose last segment this CTA holds, by all warps
+        if (s_npend > 0 && !s_err) {
+            __threadfence();
+            tiles_complete<CT>(D, P, s_bnd, s_pend, s_npend, s_k0, N, 0, TV_NW);
+            if (tid < s_npend) D.uticket[s_pend[tid].tg] = 0u;   // for the next launch
         }
-        pair_reduce2<CT>(D, P, s_bnd, ja, jb, s_k0, N);
     }
+    __syncthreads();
+    if (s_err && tid == 0) flag_err(D, s_err);
 }
 
 }  // namespace soda

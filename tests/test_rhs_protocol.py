@@ -2,19 +2,22 @@
 sodabayes_gb300/csrc/rhs_tc.cuh), as a model run on the CPU, like
 test_update_protocol.py for the residual update.
 
-Roles: the TMA thread loads each stage's A and B tiles into raw buffer
-s % NS (one barrier phase per stage); the converter warps widen a genotype
-stage's codes into tensor-memory operand s % NOB; the MMA thread reads that
-operand and the stage's B tile (genotype stages) or both raw tiles (U stages,
-which follow the genotype stages).  A raw buffer is free once the converters
-and the MMAs of its stage are done (one barrier, converter warps + MMA
-commit); an operand once the MMAs of its stage completed.
+Roles: the TMA thread loads each stage's B tile, and a U stage's A tile,
+into raw buffer s % NS (one barrier phase per stage); the converter warps
+load a genotype stage's codes from global memory and widen them into
+tensor-memory operand s % NOB and take no part in the raw buffers; the MMA
+thread reads that operand and the stage's B tile (genotype stages: it waits
+for both) or both raw tiles (U stages, which follow the genotype stages).  A
+raw buffer is free once the MMAs of its stage are done (MMA commit); an
+operand once the MMAs of its stage completed.
 
 Checked for every number of stages and genotype/U split, for the kernel's
 NS (computed from its buffer sizes for 4, 8 and 16 chains) and NOB, under
 random interleavings: no parity wait returns a phase early, and no raw
 buffer or operand is overwritten while a reader of its previous contents is
-pending."""
+pending.  Two mistakes planted in the model must be caught: converters that
+do not wait for the MMAs of the operand's previous stage, and an MMA thread
+that takes a genotype stage without waiting for its B tile."""
 import os
 import random
 import re
@@ -28,10 +31,11 @@ def _consts():
     nob = int(re.search(r"constexpr int TC_NOB = (\d+);", txt).group(1))
     tm = int(re.search(r"constexpr int TC_TM = (\d+);", txt).group(1))
     kc = int(re.search(r"constexpr int TC_KC = (\d+);", txt).group(1))
+    ku = int(re.search(r"constexpr int TC_KU = (\d+);", txt).group(1))
     ns = {}
     for ct in (4, 8, 16):
         nb = ((3 * ct + 15) // 16) * 16
-        raw = tm * kc + nb * kc * 2
+        raw = tm * ku * 2 + nb * kc * 2
         ns[ct] = min(8, (220 * 1024 - 1024) // raw)
     return nob, ns
 
@@ -45,29 +49,24 @@ class Bar:
         self.k = 0
 
     def ready(self, i):
+        if self.k >= i + 2:
+            raise Unsound("parity wait for phase %d asked with %d phases complete" % (i, self.k))
         ok = (self.k & 1) != (i & 1)
-        if ok and self.k < i + 1:
+        if ok and self.k != i + 1:
             raise Unsound("parity wait for phase %d returned with %d phases complete" % (i, self.k))
         return ok
 
 
-def run(ns_total, nck, NS, NOB, seed, skip_opfree=False):
+def run(ns_total, nck, NS, NOB, seed, skip_opfree=False, skip_bwait=False):
     rnd = random.Random(seed)
     full = [Bar() for _ in range(NS)]
-    empty = [Bar() for _ in range(NS)]   # converters + MMA commit: the model counts two arrivals per phase
-    empty_arr = [0] * NS
+    empty = [Bar() for _ in range(NS)]   # MMA commit
     conv = [Bar() for _ in range(NOB)]
     opfree = [Bar() for _ in range(NOB)]
     raw_owner = [None] * NS
     op_owner = [None] * NOB
-    conv_done, mma_done = set(), set()
+    mma_done, landed = set(), set()
     pending = []
-
-    def empty_arrive(buf):
-        empty_arr[buf] += 1
-        if empty_arr[buf] == 2:
-            empty_arr[buf] = 0
-            empty[buf].k += 1
 
     def producer():
         for s in range(ns_total):
@@ -75,39 +74,43 @@ def run(ns_total, nck, NS, NOB, seed, skip_opfree=False):
             if s >= NS:
                 yield empty[buf], s // NS - 1
             prev = raw_owner[buf]
-            if prev is not None and not (prev in conv_done and prev in mma_done):
+            if prev is not None and prev not in mma_done:
                 raise Unsound("raw buffer %d overwritten by stage %d while stage %d is read" % (buf, s, prev))
             raw_owner[buf] = s
-            pending.append(lambda buf=buf: setattr(full[buf], "k", full[buf].k + 1))
+
+            def land(s=s, buf=buf):
+                landed.add(s)
+                full[buf].k += 1
+            pending.append(land)
 
     def converter():
-        for s in range(ns_total):
-            buf, ob = s % NS, s % NOB
-            yield full[buf], s // NS
-            if s < nck:
-                if s >= NOB and not skip_opfree:
-                    yield opfree[ob], (s - NOB) // NOB
-                prev = op_owner[ob]
-                if prev is not None and prev not in mma_done:
-                    raise Unsound("operand %d overwritten by stage %d while stage %d's MMAs read it" % (ob, s, prev))
-                op_owner[ob] = s
-                conv[ob].k += 1
-            conv_done.add(s)
-            empty_arrive(buf)
+        for s in range(nck):
+            ob = s % NOB
+            if s >= NOB and not skip_opfree:
+                yield opfree[ob], (s - NOB) // NOB
+            prev = op_owner[ob]
+            if prev is not None and prev not in mma_done:
+                raise Unsound("operand %d overwritten by stage %d while stage %d's MMAs read it" % (ob, s, prev))
+            op_owner[ob] = s
+            conv[ob].k += 1
 
     def mma():
         for s in range(ns_total):
             buf, ob = s % NS, s % NOB
             if s < nck:
                 yield conv[ob], s // NOB
+                if not skip_bwait:
+                    yield full[buf], s // NS
             else:
                 yield full[buf], s // NS
+            if s not in landed:
+                raise Unsound("the MMAs of stage %d read a B tile still in flight" % s)
 
             def commit(s=s, buf=buf, ob=ob):
                 mma_done.add(s)
                 if s < nck:
                     opfree[ob].k += 1
-                empty_arrive(buf)
+                empty[buf].k += 1
             pending.append(commit)
 
     roles = [producer(), converter(), mma()]
@@ -152,6 +155,22 @@ def test_rhs_protocol_model_catches_a_missing_wait():
         total = rnd.randint(nob + 1, 48)
         try:
             run(total, total, ns[16], nob, seed=t, skip_opfree=True)
+        except Unsound:
+            caught += 1
+    assert caught > 0
+
+
+def test_rhs_protocol_model_catches_an_mma_before_its_b_tile():
+    """An MMA thread that takes a genotype stage once its codes are converted,
+    without waiting for the stage's B tile (the converters no longer wait for
+    the raw buffer), must be caught."""
+    nob, ns = _consts()
+    rnd = random.Random(9)
+    caught = 0
+    for t in range(200):
+        total = rnd.randint(1, 48)
+        try:
+            run(total, total, ns[16], nob, seed=t, skip_bwait=True)
         except Unsound:
             caught += 1
     assert caught > 0
