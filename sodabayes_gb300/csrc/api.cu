@@ -159,7 +159,7 @@ struct sodagpu_ctx {
     bool usp_ready = false;
     double *k0part = nullptr;
     float *vpart = nullptr;              // residual-update partial sums
-    unsigned *uticket = nullptr;         // per-tile tickets of the residual update
+    unsigned long long *ugrid = nullptr; // grid-barrier counter of the residual update
     TcMaps maps{};
     std::vector<int32_t> h_rtab;         // work table of the tensor-core rhs
     int32_t *rtab = nullptr;
@@ -825,7 +825,7 @@ int build_dev(sodagpu_ctx *c)
     D.dsplit = c->dsplit;
     D.k0part = c->k0part;
     D.vpart = c->vpart;
-    D.uticket = c->uticket;
+    D.ugrid = c->ugrid;
     D.gpk = c->Gt;
     D.nvt = sweep_tc_update_tiles(c->n);
     D.rtab = c->rtab;
@@ -903,7 +903,7 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             TRY(c->alloc(&c->dsplit, (size_t)sweep_tc_rows(C) * c->ldd));
             TRY(c->alloc(&c->k0part, (((size_t)c->ldd * C + 255) / 256) * C));
             TRY(c->alloc(&c->vpart, sweep_tc_vpart_floats(c->n, c->bs, C, c->sm_count), false));
-            TRY(c->alloc(&c->uticket, sweep_tc_update_all_tiles(c->n, c->bs)));
+            TRY(c->alloc(&c->ugrid, 1));
             const int NB = sweep_tc_rows(C);
             c->ldu = (int)round_up((size_t)c->bs, 8);
             TRY(c->alloc(&c->rsp, (size_t)NB * c->ldr));

@@ -115,7 +115,7 @@ struct Dev {
     uint16_t *dsplit;          // [round_up(3C,16)][ldd] bf16 hi/mid/lo of delta/sd per chain
     double *k0part;            // [draw CTAs][C] per-CTA sums of x0_j delta_j
     float *vpart;              // [tiles + update CTAs][C][256] update partial sums, one slot per segment
-    unsigned *uticket;         // [row tiles + ra tiles] segments of each tile the update has finished (0 between launches)
+    unsigned long long *ugrid; // grid-barrier counter of the update (each launch adds its CTA count)
     const uint8_t *gpk;        // 2-bit packed code blocks (see TC_PACKED_BLOCK)
     int nvt;                   // row tiles of 256 individuals of the update
     const int32_t *qoff;       // [nb+1] first 128-position code block of each subset (tiled codes)

@@ -1176,8 +1176,6 @@ size_t sweep_tc_vpart_floats(int n, int bs, int chains, int sm_count)
 
 int sweep_tc_rows(int chains) { return ((3 * chains + 15) / 16) * 16; }
 
-int sweep_tc_update_all_tiles(int n, int bs) { return sweep_tc_update_tiles(n) + (bs + TV_N - 1) / TV_N; }
-
 __global__ void __launch_bounds__(256) k_tc_prepare(int8_t *G, Dev D, uint16_t *usp)
 {
     for (int k = blockIdx.x; k < D.p; k += gridDim.x) {

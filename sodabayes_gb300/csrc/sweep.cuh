@@ -12,12 +12,10 @@ cudaError_t sweep_prepare(int bs);
 // (3 * chains rounded up to 16).
 int sweep_tc_supported(int precision, int chains, int bs);
 int sweep_tc_rows(int chains);
-// The residual update's row tiles (256 individuals), the floats of its
-// partial-sum slots (one per tile segment: tiles + CTAs slots of C x 256) and
-// its tiles (row tiles and ra tiles, one ticket each).
+// The residual update's row tiles (256 individuals) and the floats of its
+// partial-sum slots (one per tile segment: tiles + CTAs slots of C x 256).
 int sweep_tc_update_tiles(int n);
 size_t sweep_tc_vpart_floats(int n, int bs, int chains, int sm_count);
-int sweep_tc_update_all_tiles(int n, int bs);
 // Work tables of the tensor-core rhs (host side), per subset b of blk_sizes:
 // rtab[b*stride + m] = first rhs CTA of 128-SNP tile m, rtab[b*stride + tiles]
 // = rhs CTAs; tiles get K splits in proportion to their pipeline stages

@@ -28,16 +28,19 @@
 // the draws of this subset complete.  The units are laid out row tiles first
 // and split evenly over the CTAs (stream-K, one CTA per SM); a CTA's
 // consecutive units of one tile form a segment, whose accumulator rows go to
-// vpart as FP32 partial sums (hi + mid + lo per chain).  Each CTA then takes
-// a ticket for the segment's tile; the CTA that holds a tile's last segment
-// completes it once its own work is done, with all its warps: it adds the
-// tile's segments in segment order (deterministic), the centring term
-// sum_j x0_j delta_j (FP64), and writes the FP64 residuals.  No CTA waits for
-// another.
+// vpart as FP32 partial sums (hi + mid + lo per chain).  After a grid-wide
+// barrier (one CTA per SM, all resident; the wait is bounded) every CTA takes
+// an equal share of the (128-element half tile, chain) pairs, whose old
+// residuals it loaded before the barrier: it adds the pair's segments in
+// segment order (deterministic) and the centring term sum_j x0_j delta_j, and
+// writes the FP64 residuals.  Spreading this over every SM matters: GB300
+// runs FP64 at a small fraction of its FP32 rate, and a tile's residuals take
+// about as long on one SM's FP64 pipe as a third of the unit loop.
 //
 // Warp roles (mbarrier hand-offs, every wait bounded): warp 8 issues the TMA
 // loads, warps 0-7 widen the codes, warp 9 issues the MMAs, warps 10-13
-// reduce the centring term and move finished accumulators to vpart.  Per
+// reduce the centring term and move finished accumulators to vpart; all warps
+// then take part in the reductions.  Per
 // unit s (A slot s % TV_NA, B slot s % TV_NOB):
 //   producer: wait A slot free (MMAs of s - TV_NA) and B slot free (MMAs of
 //     s - TV_NOB); load A (+ tx); for an ra unit load B (+ tx) on fullb, for
@@ -61,7 +64,6 @@ constexpr int TV_MAXRA = 64;       // ra tiles per subset
 constexpr int TV_THREADS = 448;    // 8 converter warps, TMA, MMA, 4 epilogue warps
 constexpr int TV_NW = TV_THREADS / 32;
 constexpr int TV_MAXG = 512;       // CTAs (one per SM)
-constexpr int TV_MAXPEND = 8;      // tiles a CTA completes after its roles
 constexpr int TV_CONV = 256;
 constexpr int TV_CONV_WARPS = TV_CONV / 32;   // each converter warp arrives once per unit
 constexpr int TV_WARP_TMA = 8, TV_WARP_MMA = 9, TV_WARP_EPI = 10;
@@ -207,108 +209,148 @@ __device__ __forceinline__ void tile_units(const UnitPlan &P, int tg, int &u0, i
     }
 }
 
-// A tile this CTA completes: global tile tg, and the CTAs sl .. sh whose
-// segments cover it (those holding units; when there are fewer units than
-// CTAs some hold none and have no segment).
-struct PendTile {
-    int tg, sl, sh;
+// One (128-element half tile, chain) pair of the reductions: global tile tg
+// (row tiles, then ra tiles), half h, chain c, the CTAs sl..sh whose segments
+// cover the tile (sl > sh: no unit touched it, nothing changes) and the old
+// values (r or ra) of the half, lane l holding elements l + 32k.  Everything
+// here is known before the grid barrier: nothing else writes those values
+// during the update.
+struct PairJob {
+    int tg, h, c, sl, sh;
+    double rold[4];
 };
 
-// Completes the pending tiles: every (tile, 128-element half, chain) triple
-// is one job; warps w0 .. w0 + nw - 1 of the CTA take TV_JPW jobs at a time
-// (one round for a tile of 16 chains on 14 warps), with the loads of all of
-// them (old residuals, the segments in vpart) in flight together.  Lane l
-// adds elements l + 32k of the segments in segment order and applies them:
-// r, its bf16 split and the 128-row partial sum of r for a row tile, ra and
-// its split for an ra tile.
-constexpr int TV_JPW = 3;
-
 template <int CT>
-__device__ __forceinline__ void tiles_complete(const Dev &D, const UnitPlan &P, const int *bnd, const PendTile *pend,
-                                               int npend, const double *s_k0, int N, int w0, int nw)
+__device__ __forceinline__ void pair_prepare(const Dev &D, const UnitPlan &P, const int *bnd, int G, int pr, int npair,
+                                             int N, PairJob &j)
 {
-    constexpr int JOBS = 2 * CT;   // per tile
-    const int lane = threadIdx.x & 31, ew = (threadIdx.x >> 5) - w0;
-    const int njob = npend * JOBS;
-    for (int j0 = TV_JPW * ew; j0 < njob; j0 += TV_JPW * nw) {
-        double rold[TV_JPW][4];
-        float acc[TV_JPW][4];
-        int tg[TV_JPW], c[TV_JPW], h[TV_JPW], lim[TV_JPW], sl[TV_JPW], sh[TV_JPW];
-        bool isr[TV_JPW], live[TV_JPW];
+    j.tg = j.h = j.c = 0;
+    j.sl = 1;
+    j.sh = 0;
+    if (pr >= npair) return;
+    const int hh = pr / CT;
+    j.c = pr - hh * CT;
+    j.tg = hh >> 1;
+    j.h = hh & 1;
+    int u0, u1;
+    tile_units(P, j.tg, u0, u1);
+    if (u1 <= u0) return;
+    j.sl = unit_cta(bnd, u0, G);
+    j.sh = unit_cta(bnd, u1 - 1, G);
+    const int lane = threadIdx.x & 31;
+    const bool is_r = j.tg < P.nvt;
+    const int tile = is_r ? j.tg : j.tg - P.nvt;
+    const int lim = is_r ? D.n : min(N, D.bs);
 #pragma unroll
-        for (int e = 0; e < TV_JPW; ++e) {
-            const int j = j0 + e;
-            live[e] = j < njob;
-            const PendTile pt = pend[live[e] ? j / JOBS : 0];
-            const int pr = j % JOBS;
-            tg[e] = pt.tg;
-            sl[e] = pt.sl;
-            sh[e] = live[e] ? pt.sh : pt.sl - 1;
-            h[e] = pr / CT;
-            c[e] = pr - h[e] * CT;
-            isr[e] = tg[e] < P.nvt;
-            lim[e] = isr[e] ? D.n : min(N, D.bs);
-            const int tile = isr[e] ? tg[e] : tg[e] - P.nvt;
+    for (int k = 0; k < 4; ++k) {
+        const int i = tile * TV_N + j.h * 128 + lane + 32 * k;
+        j.rold[k] = 0.0;
+        if (i < lim) j.rold[k] = is_r ? __ldcg(D.r + (size_t)j.c * D.ldr + i) : __ldcg(D.ra + (size_t)j.c * D.ldra + i);
+    }
+}
+
+// The segments of job j from CTA q0 + u (u < 4) of its range: loads only.
+template <int CT>
+__device__ __forceinline__ void pair_load4(const Dev &D, const int *bnd, const PairJob &j, int q0, float (&v)[4][4])
+{
+    const int lane = threadIdx.x & 31;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int i = tile * TV_N + h[e] * 128 + lane + 32 * k;
-                rold[e][k] = 0.0;
-                acc[e][k] = 0.0f;
-                if (live[e] && i < lim[e])
-                    rold[e][k] = isr[e] ? __ldcg(D.r + (size_t)c[e] * D.ldr + i)
-                                        : __ldcg(D.ra + (size_t)c[e] * D.ldra + i);
+    for (int u = 0; u < 4; ++u) {
+        const int q = q0 + u;
+        const bool ok = q <= j.sh && bnd[q] < bnd[q + 1];   // CTAs without units have no slot
+        const float *pp = D.vpart + ((size_t)(j.tg + q) * CT + j.c) * TV_N + j.h * 128 + lane;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[u][k] = ok ? __ldcg(pp + 32 * k) : 0.0f;
+    }
+}
+
+// Applies the update of job j from its segment sum acc: r, its bf16 split and
+// the 128-row partial sum of r for a row tile, ra and its split for an ra
+// tile.  The centring term is added to the FP32 segment sum (it is of the
+// size of the other terms), leaving one FP64 conversion and one FP64
+// addition per element.
+template <int CT>
+__device__ __forceinline__ void pair_finish(const Dev &D, const UnitPlan &P, const PairJob &j, const float (&acc)[4],
+                                            const float *s_k0f, int N)
+{
+    const int lane = threadIdx.x & 31;
+    const bool is_r = j.tg < P.nvt;
+    const int tile = is_r ? j.tg : j.tg - P.nvt;
+    const int lim = is_r ? D.n : min(N, D.bs);
+    float part = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = tile * TV_N + j.h * 128 + lane + 32 * k;
+        if (is_r) {
+            const double rn = j.rold[k] + (double)(acc[k] + s_k0f[j.c]);
+            if (i < lim) {
+                const size_t o = (size_t)j.c * D.ldr + i;
+                const float rf = (float)rn;
+                D.r[o] = rn;
+                split_store(D.rsp, o, (size_t)D.chains * D.ldr, rf);
+                part += rf;
             }
-        }
-        // the segments, two per job loaded together (a tile rarely spans more than two CTAs)
-        int span = 0;
-#pragma unroll
-        for (int e = 0; e < TV_JPW; ++e) span = max(span, sh[e] - sl[e] + 1);
-        for (int d = 0; d < span; d += 2) {
-            float v[TV_JPW][2][4];
-#pragma unroll
-            for (int e = 0; e < TV_JPW; ++e)
-#pragma unroll
-                for (int dd = 0; dd < 2; ++dd) {
-                    const int q = sl[e] + d + dd;
-                    const bool ok = q <= sh[e] && bnd[q] < bnd[q + 1];
-                    const float *pp = D.vpart + ((size_t)(tg[e] + q) * CT + c[e]) * TV_N + h[e] * 128 + lane;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) v[e][dd][k] = ok ? __ldcg(pp + 32 * k) : 0.0f;
-                }
-#pragma unroll
-            for (int e = 0; e < TV_JPW; ++e)
-#pragma unroll
-                for (int dd = 0; dd < 2; ++dd)
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) acc[e][k] += v[e][dd][k];
-        }
-#pragma unroll
-        for (int e = 0; e < TV_JPW; ++e) {
-            if (!live[e]) break;
-            const int tile = isr[e] ? tg[e] : tg[e] - P.nvt;
-            float part = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int i = tile * TV_N + h[e] * 128 + lane + 32 * k;
-                if (isr[e]) {
-                    const double rn = rold[e][k] + ((double)acc[e][k] + s_k0[c[e]]);
-                    if (i < lim[e]) {
-                        const size_t o = (size_t)c[e] * D.ldr + i;
-                        D.r[o] = rn;
-                        split_store(D.rsp, o, (size_t)D.chains * D.ldr, (float)rn);
-                        part += (float)rn;
-                    }
-                } else if (i < lim[e]) {
-                    store_ra(D, c[e], i, rold[e][k] + (double)acc[e][k]);
-                }
-            }
-            if (isr[e]) {
-                const float ws = warp_sumf(part);
-                if (lane == 0 && 2 * tile + h[e] < D.nr_ctas)
-                    D.rsum[(size_t)c[e] * D.nr_ctas + 2 * tile + h[e]] = (double)ws;
-            }
+        } else if (i < lim) {
+            store_ra(D, j.c, i, j.rold[k] + (double)acc[k]);
         }
     }
+    if (is_r) {
+        const float ws = warp_sumf(part);
+        if (lane == 0 && 2 * tile + j.h < D.nr_ctas) D.rsum[(size_t)j.c * D.nr_ctas + 2 * tile + j.h] = (double)ws;
+    }
+}
+
+// Two jobs of one warp: the segments of each are added in segment order (the
+// same order for any grouping), with the loads of both jobs issued together.
+template <int CT>
+__device__ __forceinline__ void pair_reduce2(const Dev &D, const UnitPlan &P, const int *bnd, const PairJob &ja,
+                                             const PairJob &jb, const float *s_k0f, int N)
+{
+    float aa[4] = {0.0f, 0.0f, 0.0f, 0.0f}, ab[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const int na = ja.sh - ja.sl + 1, nb_ = jb.sh - jb.sl + 1, nmax = max(na, nb_);
+    for (int q0 = 0; q0 < nmax; q0 += 4) {
+        float va[4][4], vb[4][4];
+        pair_load4<CT>(D, bnd, ja, ja.sl + q0, va);
+        pair_load4<CT>(D, bnd, jb, jb.sl + q0, vb);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                aa[k] += va[u][k];
+                ab[k] += vb[u][k];
+            }
+    }
+    if (na > 0) pair_finish<CT>(D, P, ja, aa, s_k0f, N);
+    if (nb_ > 0) pair_finish<CT>(D, P, jb, ab, s_k0f, N);
+}
+
+// Grid-wide barrier of the G CTAs of one launch on a monotonic counter (each
+// launch adds G); bounded by %globaltimer (20 ms), false on time-out.
+__device__ __forceinline__ bool update_grid_sync(unsigned long long *ctr, unsigned G)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long old = atomicAdd(ctr, 1ull);
+        const unsigned long long target = (old / G + 1) * G;
+        const uint64_t t0 = tc::globaltimer_ns();
+        int ok = 1;
+        for (;;) {
+            unsigned long long v;
+            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ctr) : "memory");
+            if (v >= target) break;
+            if (tc::globaltimer_ns() - t0 > 20000000ull) {
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
 }
 
 // Packed code word of a converter thread for row unit u: positions of stage q
@@ -347,10 +389,10 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     __shared__ uint64_t s_fulla[TV_NA], s_emptya[TV_NA], s_fullb[TV_NOB], s_conv[TV_NOB], s_opfree[TV_NOB];
     __shared__ uint64_t s_segdone[2], s_dfree[2];
     __shared__ uint32_t s_tmem;
-    __shared__ int s_err, s_last, s_npend;
-    __shared__ PendTile s_pend[TV_MAXPEND];
+    __shared__ int s_err;
     __shared__ UnitPlan s_plan;
     __shared__ double s_k0p[128], s_k0[CT];
+    __shared__ float s_k0f[CT];
     __shared__ int s_bnd[TV_MAXG + 1];
     unsigned char *raw0 = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
     unsigned char *bop0 = raw0 + T::BOP0;
@@ -396,7 +438,6 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             P.pref[nra] = total;
             P.W = P.R + total;
             s_err = 0;
-            s_npend = 0;
         }
     }
     __syncthreads();
@@ -576,9 +617,8 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             }
         } else {
             // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. for all 256
-            // columns (an M = 64 accumulator keeps rows 16q .. 16q+15 in lanes 32q .. 32q+15), stores
-            // hi + mid + lo per chain to the segment's slot of vpart, and takes the tile's ticket; a
-            // tile whose last segment this CTA holds is completed after the roles
+            // columns (an M = 64 accumulator keeps rows 16q .. 16q+15 in lanes 32q .. 32q+15) and
+            // stores hi + mid + lo per chain to the segment's slot of vpart
             tc::pdl_wait();   // the draws' centring sums; r of the previous update
             const int t = tid - 32 * TV_WARP_EPI;
             const int qd = warp & 3, row = lane < 16 ? 16 * qd + lane : T::ROWS;
@@ -631,36 +671,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         dst[cc * TV_N + col] = (stg[cc * (TV_N + 1) + col] + stg[(CT + cc) * (TV_N + 1) + col]) +
                                                stg[(2 * CT + cc) * (TV_N + 1) + col];
                     }
-                    // the segment is in vpart: take the tile's ticket
-                    int u0, u1;
-                    tile_units(P, tg, u0, u1);
-                    const int sl = unit_cta(s_bnd, u0, G), sh = unit_cta(s_bnd, u1 - 1, G);
-                    __threadfence();
-                    asm volatile("bar.sync 1, 128;" ::: "memory");
-                    if (t == 0) {
-                        unsigned nseg = 0;   // the CTAs holding units of the tile, one segment each
-                        for (int q = sl; q <= sh; ++q) nseg += s_bnd[q] < s_bnd[q + 1] ? 1u : 0u;
-                        const unsigned old = atomicAdd(D.uticket + tg, 1u);
-                        s_last = old + 1 == nseg;
-                        if (s_last && ok && s_npend < TV_MAXPEND) {
-                            s_pend[s_npend].tg = tg;
-                            s_pend[s_npend].sl = sl;
-                            s_pend[s_npend].sh = sh;
-                            ++s_npend;
-                            s_last = 0;
-                        }
-                    }
-                    asm volatile("bar.sync 1, 128;" ::: "memory");
-                    if (s_last && ok) {
-                        // more tiles than the pending list holds: complete this one here
-                        __threadfence();
-                        PendTile one;
-                        one.tg = tg;
-                        one.sl = sl;
-                        one.sh = sh;
-                        tiles_complete<CT>(D, P, s_bnd, &one, 1, s_k0, N, TV_WARP_EPI, 4);
-                        if (t == 0) D.uticket[tg] = 0u;   // for the next launch (stream-ordered after this one)
-                    }
+                    __threadfence();   // the slot is read after the grid barrier
                     asm volatile("bar.sync 1, 128;" ::: "memory");
                 }
                 if (s == nu) break;
@@ -674,15 +685,33 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             tc::fence_after_sync();
             tc::tmem_dealloc(tm, 512);
         }
-        // the tiles whose last segment this CTA holds, by all warps
-        if (s_npend > 0 && !s_err) {
-            __threadfence();
-            tiles_complete<CT>(D, P, s_bnd, s_pend, s_npend, s_k0, N, 0, TV_NW);
-            if (tid < s_npend) D.uticket[s_pend[tid].tg] = 0u;   // for the next launch
-        }
+    } else if (warp >= TV_WARP_EPI) {
+        tc::pdl_wait();
+        update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);   // the centring term
     }
-    __syncthreads();
-    if (s_err && tid == 0) flag_err(D, s_err);
+    __syncthreads();   // s_k0 is complete
+    if (tid < CT) s_k0f[tid] = (float)s_k0[tid];   // read after the grid barrier's __syncthreads
+    // this warp's first two pairs (pr0 and pr0 + stride) prepared while the other CTAs finish
+    tc::pdl_wait();   // r and ra of the previous update (every warp reads them below)
+    const int npair = 2 * (P.nvt + P.nra) * CT;
+    const int pr0 = blockIdx.x * TV_NW + warp, stride = G * TV_NW;
+    PairJob ja, jb;
+    pair_prepare<CT>(D, P, s_bnd, G, pr0, npair, N, ja);
+    pair_prepare<CT>(D, P, s_bnd, G, pr0 + stride, npair, N, jb);
+    // every segment is in vpart once all CTAs are here; then the reductions, an equal share of the
+    // (half tile, chain) pairs per CTA, one pair per warp at a time
+    if (!update_grid_sync(D.ugrid, (unsigned)G)) s_err = 16;
+    if (s_err) {
+        if (tid == 0) flag_err(D, s_err);
+        return;
+    }
+    for (int pr = pr0; pr < npair; pr += 2 * stride) {
+        if (pr != pr0) {
+            pair_prepare<CT>(D, P, s_bnd, G, pr, npair, N, ja);
+            pair_prepare<CT>(D, P, s_bnd, G, pr + stride, npair, N, jb);
+        }
+        pair_reduce2<CT>(D, P, s_bnd, ja, jb, s_k0f, N);
+    }
 }
 
 }  // namespace soda
