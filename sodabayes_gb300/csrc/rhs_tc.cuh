@@ -246,33 +246,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int i = 0; i < TC_PF; ++i) pf[i] = i < nck ? code_word(i) : 0ull;
         tc::pdl_wait();
         tc::pdl_trigger();
-        for (int s = 0; s < nck; ++s) {
-            const int ob = s % TC_NOB;
-            // the operand buffer was last read by the MMAs of stage s - TC_NOB
-            bool ok = s < TC_NOB || tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
-            ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
-            if (!ok) {
-                s_err = 1;
-                break;
+        // stage s uses pf[s % TC_PF] and reloads it for stage s + TC_PF: the loop is unrolled by
+        // TC_PF so that every slot stays in its own registers (a shift of the slots would wait for
+        // each load one stage after issuing it)
+        bool stop = false;
+        for (int s0 = 0; s0 < nck && !stop; s0 += TC_PF) {
+#pragma unroll
+            for (int i = 0; i < TC_PF; ++i) {
+                const int s = s0 + i;
+                if (s >= nck || stop) break;
+                const int ob = s % TC_NOB;
+                // the operand buffer was last read by the MMAs of stage s - TC_NOB
+                bool ok = s < TC_NOB || tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
+                ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
+                if (!ok) {
+                    s_err = 1;
+                    stop = true;
+                    break;
+                }
+                const uint64_t w = pf[i];
+                pf[i] = s + TC_PF < nck ? code_word(s + TC_PF) : 0ull;
+                // word ww of the 8 bytes: individuals 16 ww + 4 q + e at bits 8 e + 2 q
+                uint32_t v[16];
+#pragma unroll
+                for (int ww = 0; ww < 2; ++ww) {
+                    const uint32_t x = (uint32_t)(w >> (32 * ww));
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        tc::codes_to_bf16x4((x >> (2 * q)) & 0x03030303u, v[8 * ww + 2 * q], v[8 * ww + 2 * q + 1]);
+                }
+                tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 64 * ob + 16 * s4, v);
+                tc::tmem_wait_st();
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
             }
-            const uint64_t w = pf[0];
-#pragma unroll
-            for (int i = 0; i + 1 < TC_PF; ++i) pf[i] = pf[i + 1];
-            pf[TC_PF - 1] = s + TC_PF < nck ? code_word(s + TC_PF) : 0ull;
-            // word ww of the 8 bytes: individuals 16 ww + 4 q + e at bits 8 e + 2 q
-            uint32_t v[16];
-#pragma unroll
-            for (int ww = 0; ww < 2; ++ww) {
-                const uint32_t x = (uint32_t)(w >> (32 * ww));
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    tc::codes_to_bf16x4((x >> (2 * q)) & 0x03030303u, v[8 * ww + 2 * q], v[8 * ww + 2 * q + 1]);
-            }
-            tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 64 * ob + 16 * s4, v);
-            tc::tmem_wait_st();
-            tc::fence_before_sync();
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
         }
         if (ns > 0 && !tc::mbar_wait(&s_done, 0)) s_err = 1;
     }

@@ -40,13 +40,15 @@
 // Warp roles (mbarrier hand-offs, every wait bounded): warp 8 issues the TMA
 // loads, warps 0-7 widen the codes, warp 9 issues the MMAs, warps 10-13
 // reduce the centring term and move finished accumulators to vpart; all warps
-// then take part in the reductions.  Per
-// unit s (A slot s % TV_NA, B slot s % TV_NOB):
-//   producer: wait A slot free (MMAs of s - TV_NA) and B slot free (MMAs of
-//     s - TV_NOB); load A (+ tx); for an ra unit load B (+ tx) on fullb, for
-//     a row unit arrive on fullb (the slot is the converters' to write);
-//   converters: wait fullb; row unit: write B from the codes; arrive on conv;
-//   MMA: wait conv and fulla; 4 MMAs; commit to opfree and emptya.
+// then take part in the reductions.  A CTA's row units come before its ra
+// units.  Unit s uses slot s % TV_NS of both operands, and one commit of its
+// MMAs frees both:
+//   producer: wait free (MMAs of s - TV_NS); load A (+ tx) on fulla; for an
+//     ra unit also load B (+ tx) on fullb;
+//   converters (row units only): wait free; write B from the codes; arrive
+//     on conv;
+//   MMA: wait conv (row unit) or fullb (ra unit), and fulla; 4 MMAs; commit
+//     to free.
 // Every wait is at most one phase behind its barrier, so the parity waits are
 // exact (checked by a CPU model of this protocol in the tests).
 #pragma once
@@ -56,8 +58,7 @@ namespace soda {
 constexpr int TV_N = 256;          // individuals per row tile / rows of U per ra tile (MMA N)
 constexpr int TV_K = 64;           // subset positions per stage
 constexpr int TV_M = 64;           // MMA M (the 3 * chains <= 48 rows of the delta split)
-constexpr int TV_NA = 4;           // delta-split tiles (operand A) in flight
-constexpr int TV_NOB = 4;          // B operands
+constexpr int TV_NS = 4;           // operand slots: delta-split tile (A) and B operand
 constexpr int TV_PF = 4;           // packed code words each converter thread holds in flight
 constexpr int TV_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
 constexpr int TV_MAXRA = 64;       // ra tiles per subset
@@ -76,11 +77,11 @@ struct UpdTc {
     // an M = 64 MMA reads 64 rows (8 KB) from A's start: each A slot owns 8 KB, so that no byte
     // the MMA reads is the target of a TMA load in flight (rows past NB are never written)
     static constexpr int ASTRIDE = TV_M * 128;
-    static constexpr int AREG = TV_NA * ASTRIDE;
+    static constexpr int AREG = TV_NS * ASTRIDE;
     static constexpr int BOP = TV_K * TV_N * 2;        // B operand: 64 x 256 bf16
     static constexpr int BOP0 = AREG;
     // epilogue staging: the accumulator rows in use, all 256 columns (row stride 257 floats)
-    static constexpr int STG0 = BOP0 + TV_NOB * BOP;
+    static constexpr int STG0 = BOP0 + TV_NS * BOP;
     static constexpr int STG = ((ROWS * (TV_N + 1) * 4 + 1023) / 1024) * 1024;
     static constexpr size_t SMEM = 1024 + (size_t)STG0 + (size_t)STG;
     static_assert(RAW_A % 1024 == 0 && AREG % 1024 == 0 && BOP % 1024 == 0, "buffer alignment");
@@ -119,6 +120,14 @@ __device__ __forceinline__ Unit decode_unit(const UnitPlan &P, int u, int &ra_hi
     x.q = P.qs[a] + w / 3;
     x.term = w % 3;
     return x;
+}
+
+// Phase index of fullb of slot s % TV_NS for ra unit s: the slot's earlier
+// units less its row units (the CTA's nrow row units come first).
+__device__ __forceinline__ int ra_phase(int s, int nrow)
+{
+    const int sl = s % TV_NS;
+    return s / TV_NS - (nrow > sl ? (nrow - 1 - sl) / TV_NS + 1 : 0);
 }
 
 // decode_unit without a hint (binary search over the ra tiles), for lanes that
@@ -386,7 +395,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
 {
     using T = UpdTc<CT>;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
-    __shared__ uint64_t s_fulla[TV_NA], s_emptya[TV_NA], s_fullb[TV_NOB], s_conv[TV_NOB], s_opfree[TV_NOB];
+    __shared__ uint64_t s_fulla[TV_NS], s_fullb[TV_NS], s_conv[TV_NS], s_free[TV_NS];
     __shared__ uint64_t s_segdone[2], s_dfree[2];
     __shared__ uint32_t s_tmem;
     __shared__ int s_err;
@@ -450,14 +459,11 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     const int nu = u_end - u_begin;
     if (nu > 0) {
         if (tid == 0) {
-            for (int i = 0; i < TV_NA; ++i) {
-                tc::mbar_init(&s_fulla[i], 1);
-                tc::mbar_init(&s_emptya[i], 1);   // the MMAs reading the tile
-            }
-            for (int i = 0; i < TV_NOB; ++i) {
-                tc::mbar_init(&s_fullb[i], 1);    // the producer: U tile landed, or slot handed to the converters
+            for (int i = 0; i < TV_NS; ++i) {
+                tc::mbar_init(&s_fulla[i], 1);    // A tile landed
+                tc::mbar_init(&s_fullb[i], 1);    // U tile of an ra unit landed
                 tc::mbar_init(&s_conv[i], TV_CONV_WARPS);
-                tc::mbar_init(&s_opfree[i], 1);
+                tc::mbar_init(&s_free[i], 1);     // the MMAs reading the slot are complete
             }
             for (int i = 0; i < 2; ++i) {
                 tc::mbar_init(&s_segdone[i], 1);
@@ -496,24 +502,20 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     const int kd = __shfl_sync(0xffffffffu, kind, i), k0 = __shfl_sync(0xffffffffu, ax, i);
                     const int y = __shfl_sync(0xffffffffu, cy, i), z = __shfl_sync(0xffffffffu, cz, i);
                     if (lane == 0) {
-                        const int a = s % TV_NA, ob = s % TV_NOB;
-                        // the slots' previous tiles are consumed: A by the MMAs of unit s - TV_NA, B by
-                        // the MMAs of unit s - TV_NOB
-                        ok = s < TV_NA || tc::mbar_wait(&s_emptya[a], ((s / TV_NA) - 1) & 1);
-                        if (ok && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob], ((s / TV_NOB) - 1) & 1);
+                        const int sl = s % TV_NS;
+                        // the slot's previous operands are consumed by the MMAs of unit s - TV_NS
+                        ok = s < TV_NS || tc::mbar_wait(&s_free[sl], ((s / TV_NS) - 1) & 1);
                         if (!ok) {
                             s_err = 11;
                         } else {
-                            tc::mbar_expect_tx(&s_fulla[a], T::RAW_A);
-                            tc::tma_load_2d(raw0 + (size_t)a * T::ASTRIDE, &tm_d, k0, 0, &s_fulla[a]);
+                            tc::mbar_expect_tx(&s_fulla[sl], T::RAW_A);
+                            tc::tma_load_2d(raw0 + (size_t)sl * T::ASTRIDE, &tm_d, k0, 0, &s_fulla[sl]);
                             if (kd == 1) {
-                                unsigned char *bo = bop0 + (size_t)ob * T::BOP;   // MN atoms 8 KB apart
-                                tc::mbar_expect_tx(&s_fullb[ob], T::BOP);
+                                unsigned char *bo = bop0 + (size_t)sl * T::BOP;   // MN atoms 8 KB apart
+                                tc::mbar_expect_tx(&s_fullb[sl], T::BOP);
 #pragma unroll
                                 for (int h = 0; h < 4; ++h)
-                                    tc::tma_load_2d(bo + h * 8192, &tm_u, y + 64 * h, z, &s_fullb[ob]);
-                            } else {
-                                tc::mbar_arrive(&s_fullb[ob]);
+                                    tc::tma_load_2d(bo + h * 8192, &tm_u, y + 64 * h, z, &s_fullb[sl]);
                             }
                             issued = s + 1;
                         }
@@ -525,18 +527,20 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             // no copy may still be in flight into this CTA's shared memory when it exits: wait (bounded)
             // for the last loads issued into every slot (already complete unless a wait above gave up)
             if (lane == 0 && issued > 0) {
-                for (int s = max(0, issued - TV_NA); s < issued; ++s)
-                    if (!tc::mbar_wait(&s_fulla[s % TV_NA], (s / TV_NA) & 1)) s_err = 21;
-                for (int s = max(0, issued - TV_NOB); s < issued; ++s)
-                    if (!tc::mbar_wait(&s_fullb[s % TV_NOB], (s / TV_NOB) & 1)) s_err = 21;
+                const int nrow = max(0, min(u_end, P.R) - u_begin);
+                for (int s = max(0, issued - TV_NS); s < issued; ++s) {
+                    if (!tc::mbar_wait(&s_fulla[s % TV_NS], (s / TV_NS) & 1)) s_err = 21;
+                    if (s >= nrow && !tc::mbar_wait(&s_fullb[s % TV_NS], ra_phase(s, nrow) & 1)) s_err = 21;
+                }
             }
         } else if (warp == TV_WARP_MMA) {
             if (lane == 0) {
                 const uint32_t idesc = tc::idesc_bf16_bmn(TV_M, TV_N);
+                const int nrow = max(0, min(u_end, P.R) - u_begin);
                 int hint = 0, seg = -1, pkind = -1, ptile = -1;
                 bool ok = true;
                 for (int s = 0; s < nu && ok; ++s) {
-                    const int a = s % TV_NA, ob = s % TV_NOB;
+                    const int sl = s % TV_NS;
                     const Unit x = decode_unit(P, u_begin + s, hint);
                     const bool first = x.kind != pkind || x.tile != ptile;
                     if (first) {
@@ -549,17 +553,19 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         if (!ok) s_err = 17;
                     }
                     if (ok) {
-                        ok = tc::mbar_wait(&s_conv[ob], (s / TV_NOB) & 1);
+                        // B: widened codes of a row unit, or the U tile of an ra unit
+                        ok = s < nrow ? tc::mbar_wait(&s_conv[sl], (s / TV_NS) & 1)
+                                      : tc::mbar_wait(&s_fullb[sl], ra_phase(s, nrow) & 1);
                         if (!ok) s_err = 12;
                     }
                     if (ok) {
-                        ok = tc::mbar_wait(&s_fulla[a], (s / TV_NA) & 1);
+                        ok = tc::mbar_wait(&s_fulla[sl], (s / TV_NS) & 1);
                         if (!ok) s_err = 18;
                     }
                     if (!ok) break;
                     tc::fence_after_sync();
-                    const uint32_t a0 = tc::smem_u32(raw0 + (size_t)a * T::ASTRIDE);
-                    const uint32_t b0 = tc::smem_u32(bop0 + (size_t)ob * T::BOP);
+                    const uint32_t a0 = tc::smem_u32(raw0 + (size_t)sl * T::ASTRIDE);
+                    const uint32_t b0 = tc::smem_u32(bop0 + (size_t)sl * T::BOP);
                     const uint32_t dt = tm + 256 * (seg & 1);
 #pragma unroll
                     for (int kk = 0; kk < TV_K / 16; ++kk) {
@@ -569,8 +575,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                                                         : tc::desc_sw128_mn(b0 + kk * 2048, 8192, 1024);
                         tc::mma_bf16(dt, tc::desc_sw128(a0 + kk * 32, 1024), bd, idesc, (first && kk == 0) ? 0u : 1u);
                     }
-                    tc::mma_commit(&s_opfree[ob]);
-                    tc::mma_commit(&s_emptya[a]);
+                    tc::mma_commit(&s_free[sl]);
                 }
                 if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
             }
@@ -587,33 +592,42 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             for (int i = 0; i < TV_PF; ++i)
                 pf[i] = i < nrow ? update_code_word(D, P, cblk, u_begin + i, tid) : make_uint4(0u, 0u, 0u, 0u);
             const int k = tid & 63, j = tid >> 6, row = k & 7;
-            for (int s = 0; s < nu; ++s) {
-                const int ob = s % TV_NOB;
-                bool ok = tc::mbar_wait(&s_fullb[ob], (s / TV_NOB) & 1);
-                ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
-                if (!ok) {
-                    s_err = 13;
-                    break;
-                }
-                if (s < nrow) {
-                    const uint4 w = pf[0];
+            // unit s uses pf[s % TV_PF] and reloads it for unit s + TV_PF: the loop is unrolled by
+            // TV_PF so that every slot stays in its own registers (a shift of the slots would wait
+            // for each load one unit after issuing it)
+            bool stop = false;
+            for (int s0 = 0; s0 < nrow && !stop; s0 += TV_PF) {
 #pragma unroll
-                    for (int i = 0; i + 1 < TV_PF; ++i) pf[i] = pf[i + 1];
-                    pf[TV_PF - 1] = s + TV_PF < nrow ? update_code_word(D, P, cblk, u_begin + s + TV_PF, tid)
-                                                     : make_uint4(0u, 0u, 0u, 0u);
-                    unsigned char *orow = bop0 + (size_t)ob * T::BOP + (k >> 3) * 4096 + j * 1024 + row * 128;
-                    const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        uint4 c0, c1;
-                        unpack16(ww[q], c0, c1);
-                        *reinterpret_cast<uint4 *>(orow + (((2 * q) ^ row) << 4)) = c0;
-                        *reinterpret_cast<uint4 *>(orow + (((2 * q + 1) ^ row) << 4)) = c1;
+                for (int i = 0; i < TV_PF; ++i) {
+                    const int s = s0 + i;
+                    if (s >= nrow || stop) break;
+                    const int ob = s % TV_NS;
+                    // the B operand was last read by the MMAs of unit s - TV_NS
+                    bool ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);
+                    ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
+                    if (!ok) {
+                        s_err = 13;
+                        stop = true;
+                        break;
                     }
-                    tc::fence_async_smem();
+                    {
+                        const uint4 w = pf[i];
+                        pf[i] = s + TV_PF < nrow ? update_code_word(D, P, cblk, u_begin + s + TV_PF, tid)
+                                                 : make_uint4(0u, 0u, 0u, 0u);
+                        unsigned char *orow = bop0 + (size_t)ob * T::BOP + (k >> 3) * 4096 + j * 1024 + row * 128;
+                        const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            uint4 c0, c1;
+                            unpack16(ww[q], c0, c1);
+                            *reinterpret_cast<uint4 *>(orow + (((2 * q) ^ row) << 4)) = c0;
+                            *reinterpret_cast<uint4 *>(orow + (((2 * q + 1) ^ row) << 4)) = c1;
+                        }
+                        tc::fence_async_smem();
+                    }
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
                 }
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
             }
         } else {
             // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. for all 256

@@ -5,19 +5,20 @@ The kernel's roles hand buffers to one another through mbarriers waited on by
 phase parity: a wait for phase i returns as soon as the barrier's completed
 phase count k has the other parity than i.  It is therefore sound only if it
 is never asked while k <= i - 1 (it would return at once, a phase early) and
-never when k >= i + 2 (a whole phase was missed).  Per unit s the producer
-waits for its A slot (MMAs of s - NA) and its B slot (MMAs of s - NOB), loads
-A, and for an ra unit loads B by TMA (fullb completes on arrival) or for a
-row unit arrives on fullb at once; the converters wait on fullb, widen the
-codes of a row unit into B, and arrive on conv; the MMA thread waits on conv
-and fulla and commits to opfree and emptya.  The model runs the roles and
-the asynchronous completions (TMA arrival, MMA commit) under random
-interleavings, with the slot counts read from the kernel's source, and
-checks that every wait that returns has exactly its phase completed and that
-no buffer is written while a reader of its previous contents is pending, for
-random mixes of row units and ra units.  The mistake planted in the model,
-a producer that waits for the B slot only before ra units, is harmless when
-NA == NOB (the A-slot wait implies it) and must be caught with more A slots."""
+never when k >= i + 2 (a whole phase was missed).  A CTA's row units come
+before its ra units; unit s uses operand slot s % NS.  The producer waits for
+the slot (the MMAs of unit s - NS), loads A, and for an ra unit also loads B
+by TMA (fullb completes on arrival); the converters, for row units only, wait
+for the slot themselves, widen the codes into B and arrive on conv; the MMA
+thread waits on conv (row unit) or on fullb (ra unit: phase = the slot's
+earlier units less its row units) and on fulla, and commits once to free.
+The model runs the roles and the asynchronous completions (TMA arrival, MMA
+commit) under random interleavings, with the slot count read from the
+kernel's source, and checks that every wait that returns has exactly its
+phase completed and that no buffer is written while a reader of its previous
+contents is pending.  Planted mistakes it must catch: converters that do not
+wait for the slot, a fullb phase that forgets the row units, and ra units
+placed before row units."""
 import os
 import random
 import re
@@ -28,14 +29,15 @@ SRC = os.path.join(ROOT, "sodabayes_gb300", "csrc", "update_tc.cuh")
 
 def _consts():
     txt = open(SRC).read()
-    out = {}
-    for name in ("TV_NA", "TV_NOB"):
-        m = re.search(r"constexpr int %s = (\d+);" % name, txt)
-        assert m, name
-        out[name] = int(m.group(1))
-    # the producer waits for the B slot before every unit, row or ra
-    out["bwait_all"] = "if (ok && s >= TV_NOB) ok = tc::mbar_wait(&s_opfree[ob]" in txt
-    return out
+    m = re.search(r"constexpr int TV_NS = (\d+);", txt)
+    assert m, "TV_NS"
+    return {
+        "TV_NS": int(m.group(1)),
+        # the converters wait for the slot before writing B
+        "conv_wait": "bool ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);" in txt,
+        # the MMA thread's fullb phase discounts the slot's row units
+        "ra_phase": "tc::mbar_wait(&s_fullb[sl], ra_phase(s, nrow) & 1)" in txt,
+    }
 
 
 class Unsound(AssertionError):
@@ -57,77 +59,77 @@ class Bar:
         return ok
 
 
-def run(kinds, NA, NOB, bwait_all, seed):
+def ra_phase(s, nrow, NS):
+    sl = s % NS
+    return s // NS - ((nrow - 1 - sl) // NS + 1 if nrow > sl else 0)
+
+
+def run(kinds, NS, seed, conv_wait=True, naive_ra_phase=False):
     rnd = random.Random(seed)
     nu = len(kinds)
-    fulla = [Bar() for _ in range(NA)]
-    emptya = [Bar() for _ in range(NA)]
-    fullb = [Bar() for _ in range(NOB)]
-    conv = [Bar() for _ in range(NOB)]
-    opfree = [Bar() for _ in range(NOB)]
-    a_owner = [None] * NA        # unit whose A tile is in the slot, until its MMAs complete
-    b_owner = [None] * NOB       # unit whose B operand is in the buffer, until its MMAs complete
+    nrow = 0
+    while nrow < nu and kinds[nrow] == 0:
+        nrow += 1
+    fulla = [Bar() for _ in range(NS)]
+    fullb = [Bar() for _ in range(NS)]
+    conv = [Bar() for _ in range(NS)]
+    free = [Bar() for _ in range(NS)]
+    a_owner = [None] * NS        # unit whose A tile is in the slot, until its MMAs complete
+    b_owner = [None] * NS        # unit whose B operand is in the slot, until its MMAs complete
     mma_done = set()
     landed_a, landed_b = set(), set()
 
-    def write_a(s):
-        a = s % NA
-        if a_owner[a] is not None and a_owner[a] not in mma_done:
-            raise Unsound("A slot %d overwritten by unit %d while unit %d's MMAs read it" % (a, s, a_owner[a]))
-        a_owner[a] = s
-
-    def write_b(s):
-        ob = s % NOB
-        if b_owner[ob] is not None and b_owner[ob] not in mma_done:
-            raise Unsound("B operand %d overwritten by unit %d while unit %d's MMAs read it" % (ob, s, b_owner[ob]))
-        b_owner[ob] = s
+    def write(owner, s, what):
+        sl = s % NS
+        if owner[sl] is not None and owner[sl] not in mma_done:
+            raise Unsound("%s slot %d overwritten by unit %d while unit %d's MMAs read it" % (what, sl, s, owner[sl]))
+        owner[sl] = s
 
     pending = []   # asynchronous completions: callables
 
     def producer():
         for s in range(nu):
-            a, ob = s % NA, s % NOB
-            if s >= NA:
-                yield emptya[a], s // NA - 1
-            if s >= NOB and (bwait_all or kinds[s] == 1):
-                yield opfree[ob], (s - NOB) // NOB
-            write_a(s)
+            sl = s % NS
+            if s >= NS:
+                yield free[sl], s // NS - 1
+            write(a_owner, s, "A")
 
-            def land_a(s=s, a=a):
+            def land_a(s=s, sl=sl):
                 landed_a.add(s)
-                fulla[a].k += 1
+                fulla[sl].k += 1
             pending.append(land_a)
             if kinds[s] == 1:
-                write_b(s)   # TMA writes the B operand of an ra unit
+                write(b_owner, s, "B")   # TMA writes the B operand of an ra unit
 
-                def land_b(s=s, ob=ob):
+                def land_b(s=s, sl=sl):
                     landed_b.add(s)
-                    fullb[ob].k += 1
+                    fullb[sl].k += 1
                 pending.append(land_b)
-            else:
-                fullb[ob].k += 1   # the slot is the converters' to write
 
     def converter():
-        for s in range(nu):
-            ob = s % NOB
-            yield fullb[ob], s // NOB
-            if kinds[s] == 0:
-                write_b(s)   # widened codes into the B operand
-                landed_b.add(s)
-            conv[ob].k += 1
+        # the kernel's converters take the first nrow units as the row units
+        for s in range(nrow):
+            sl = s % NS
+            if s >= NS and conv_wait:
+                yield free[sl], s // NS - 1
+            write(b_owner, s, "B")   # widened codes into the B operand
+            landed_b.add(s)
+            conv[sl].k += 1
 
     def mma():
         for s in range(nu):
-            a, ob = s % NA, s % NOB
-            yield conv[ob], s // NOB
-            yield fulla[a], s // NA
+            sl = s % NS
+            if s < nrow:
+                yield conv[sl], s // NS
+            else:
+                yield fullb[sl], (s // NS if naive_ra_phase else ra_phase(s, nrow, NS))
+            yield fulla[sl], s // NS
             if s not in landed_a or s not in landed_b:
                 raise Unsound("the MMAs of unit %d read an operand still in flight" % s)
 
-            def commit(s=s, a=a, ob=ob):
+            def commit(s=s, sl=sl):
                 mma_done.add(s)
-                opfree[ob].k += 1
-                emptya[a].k += 1
+                free[sl].k += 1
             pending.append(commit)
 
     roles = [producer(), converter(), mma()]
@@ -149,37 +151,46 @@ def run(kinds, NA, NOB, bwait_all, seed):
             waits[j] = next(roles[j], None)
 
 
-def _mixes(rnd, n):
+def _mixes(rnd, n, ordered=True):
     for _ in range(n):
         nu = rnd.randint(1, 40)
         split = rnd.randint(0, nu)
-        # row units first, then ra units (the kernel's unit order), or a random mix
-        if rnd.random() < 0.5:
+        if ordered:   # row units first, then ra units (the kernel's unit order)
             yield [0] * split + [1] * (nu - split)
         else:
             yield [rnd.randint(0, 1) for _ in range(nu)]
 
 
-def test_update_protocol_is_sound():
-    c = _consts()
-    assert c["bwait_all"], "the producer's wait for the B slot before every unit is missing from update_tc.cuh"
-    rnd = random.Random(7)
-    for t, kinds in enumerate(_mixes(rnd, 300)):
-        run(kinds, c["TV_NA"], c["TV_NOB"], True, seed=t)
-
-
-def test_update_protocol_model_catches_a_missing_wait():
-    """Six A slots: sound with the B-slot wait before every unit, caught when
-    the producer waits for the B slot only before ra units."""
-    c = _consts()
-    rnd = random.Random(11)
-    mixes = list(_mixes(rnd, 300))
-    for t, kinds in enumerate(mixes):
-        run(kinds, 6, c["TV_NOB"], True, seed=t)
+def _caught(mixes, NS, **kw):
     caught = 0
     for t, kinds in enumerate(mixes):
         try:
-            run(kinds, 6, c["TV_NOB"], False, seed=t)
-        except Unsound:
+            run(kinds, NS, seed=t, **kw)
+        except (Unsound, AssertionError):
             caught += 1
-    assert caught > 0
+    return caught
+
+
+def test_update_protocol_is_sound():
+    c = _consts()
+    assert c["conv_wait"], "the converters' wait for the operand slot is missing from update_tc.cuh"
+    assert c["ra_phase"], "the MMA thread's fullb phase (ra_phase) is missing from update_tc.cuh"
+    rnd = random.Random(7)
+    for t, kinds in enumerate(_mixes(rnd, 400)):
+        run(kinds, c["TV_NS"], seed=t)
+
+
+def test_update_protocol_model_catches_planted_mistakes():
+    c = _consts()
+    NS = c["TV_NS"]
+    rnd = random.Random(11)
+    mixes = list(_mixes(rnd, 300))
+    assert _caught(mixes, NS) == 0
+    # converters that write B without waiting for the slot
+    assert _caught(mixes, NS, conv_wait=False) > 0
+    # a fullb phase that counts the slot's row units as ra uses
+    assert _caught(mixes, NS, naive_ra_phase=True) > 0
+    # ra units before row units: the kernel's converters and phases assume the opposite
+    rnd = random.Random(13)
+    shuffled = [k for k in _mixes(rnd, 300, ordered=False) if 0 in k and 1 in k and k.index(1) < len(k) - 1 - k[::-1].index(0)]
+    assert _caught(shuffled, NS) > 0
