@@ -180,10 +180,11 @@ def _make_job(spec, codes_dev, y, prec, chains, seed, numit=100000):
 def _rhs_bytes(n, N, chains, prec, tc=False):
     """Algorithmic bytes of one rhs launch: the subset's genotype columns and
     augmenting columns once, plus each chain's residual copies.  The
-    tensor-core rhs reads the upper triangle of U as three bf16 terms and the
-    residuals r and ra as their three-term bf16 splits."""
+    tensor-core rhs reads the genotype codes 2-bit packed (n N / 4 bytes), the
+    upper triangle of U as three bf16 terms and the residuals r and ra as their
+    three-term bf16 splits."""
     if tc:
-        return n * N + N * (N + 1) // 2 * 6 + chains * (n + N) * 6
+        return n * N // 4 + N * (N + 1) // 2 * 6 + chains * (n + N) * 6
     ex = {"fp8": 1, "fp32": 4, "fp64": 1}[prec]
     eu = {"fp8": 4, "fp32": 4, "fp64": 8}[prec]
     er = {"fp8": 4, "fp32": 4, "fp64": 8}[prec]
@@ -192,10 +193,10 @@ def _rhs_bytes(n, N, chains, prec, tc=False):
 
 def _update_bytes(n, N, chains):
     """Algorithmic bytes of one tensor-core update launch (every stage
-    active): the subset's genotype columns and the three bf16 terms of the
-    upper triangle of U once, the delta split once, and each chain's FP64
-    residual read and written with its bf16 split."""
-    return n * N + N * (N + 1) // 2 * 6 + 3 * chains * N * 2 + chains * n * (8 + 8 + 6)
+    active): the subset's genotype codes 2-bit packed (n N / 4 bytes) and the
+    three bf16 terms of the upper triangle of U once, the delta split once,
+    and each chain's FP64 residual read and written with its bf16 split."""
+    return n * N // 4 + N * (N + 1) // 2 * 6 + 3 * chains * N * 2 + chains * n * (8 + 8 + 6)
 
 
 def bench_ours(args, rank, ws):
@@ -584,6 +585,84 @@ def workload_c5(args):
     print(json.dumps(line), flush=True)
 
 
+def workload_c4(args):
+    """Config 4 on one GPU: 32 independent BayesB analyses, n ~ U[500, 20000], p ~ U[10000, 200000], LD
+    generator of config 2, h2 ~ U(0.1, 0.7), 0.5% of p causal, FP8, one chain each, subset sizes from the batch
+    autotuner, all analyses in one launch per kernel under one captured CUDA graph (SodaBatch).  Prints its own
+    JSON line: analysis iterations per second of the batch (CUDA-event timed, inputs resident), beside the same
+    analyses run one after another, each under its own graph, and the autotuner's modelled time."""
+    import torch
+    from sodabayes_gb300 import JobOptions, SodaBatch, SodaJob, autotune_batch, make_config, synth
+    J = 32
+    rng = np.random.default_rng(20260004)
+    n = rng.integers(500, 20001, size=J)
+    p = rng.integers(10000, 200001, size=J)
+    h2 = rng.uniform(0.1, 0.7, size=J)
+    t0 = time.perf_counter()
+    bs, steps, model_s = autotune_batch(n, p, 2000, max_blocksize=2000)
+    t_tune = time.perf_counter() - t0
+    jobs, t_gen, t_setup = [], 0.0, 0.0
+    for j in range(J):
+        spec = synth.SynthSpec(n=int(n[j]), p=int(p[j]), maf_lo=0.01, maf_hi=0.5, ld_block=50, rho=0.7,
+                               ncausal=max(1, int(round(0.005 * p[j]))), h2=float(h2[j]), seed=20264000 + j)
+        t = time.perf_counter()
+        codes, y, _ = synth.make_device(spec)
+        torch.cuda.synchronize()
+        t_gen += time.perf_counter() - t
+        vy = float(np.var(y))
+        o = JobOptions(method="BayesB", blocksize=int(bs[j]), numit=2000, burnin=0, seed=91 + j, precision="fp8",
+                       chains=1, kernels="cuda_cores", scale_va=0.5 * vy, df_va=4.0, scale_ve=0.5 * vy, df_ve=4.0)
+        t = time.perf_counter()
+        job = SodaJob(make_config(spec.n, spec.p, o))
+        job.load_genotypes(device_ptr=codes.data_ptr())
+        job.load_pheno(y)
+        job.build_z()
+        job.init_chains()
+        torch.cuda.synchronize()
+        t_setup += time.perf_counter() - t
+        del codes
+        jobs.append(job)
+    torch.cuda.empty_cache()
+    free, total = torch.cuda.mem_get_info()
+    K, W = args.steps, args.warmup
+    batch = SodaBatch(jobs)
+    batch.run(args.settle + W)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        batch.run(K)
+        torch.cuda.synchronize()
+    ms, nsteps = batch.timings()
+    batch.close()
+    # the same analyses one after another, each under its own graph
+    alone_ms = 0.0
+    for job in jobs:
+        job.run(W)
+        job.run(K)
+        alone_ms += job.timings()[2]
+    for job in jobs:
+        job.close()
+    modelled_iter_s = (model_s - sum(
+        int(p[j]) * (int(n[j]) * int(bs[j]) / 5e13 + int(bs[j]) ** 2 / (3 * 6e11)) for j in range(J))) / 2000
+    line = {"workload": "config 4: 32 independent SODA BayesB analyses in one launch per kernel, n~U[500,20000], "
+                        "p~U[10000,200000], LD generator of config 2 (50-SNP AR(1) blocks rho=0.7, maf~U(0.01,0.5)), "
+                        "h2~U(0.1,0.7), 0.5% of p causal, FP8, 1 chain each, subset sizes autotuned",
+            "metric": "SODA Gibbs analysis iterations/s (iterations x analyses)", "value": K * J / (ms / 1000.0),
+            "unit": "iters*analyses/s", "ms_per_step": ms / K, "steps": K, "warmup": W,
+            "settle_iterations": args.settle, "precision": "fp8", "kernels": "CUDA cores (one chain per analysis)",
+            "data": "synthetic (seeded generator of config 2 per analysis)",
+            "one_by_one": {"value": K * J / (alone_ms / 1000.0), "ms_per_step": alone_ms / K,
+                           "how": "the same 32 jobs, each run on its own stream and graph, one after another"},
+            "speedup_vs_one_by_one": alone_ms / ms,
+            "launches_per_iteration": 3 + 3 * nsteps + 6, "subset_steps": nsteps,
+            "autotune": {"blocksizes": [int(x) for x in bs], "steps": steps, "modelled_iteration_ms":
+                         round(1000 * modelled_iter_s, 3), "measured_iteration_ms": round(ms / K, 3),
+                         "tune_s": round(t_tune, 4)},
+            "n": [int(x) for x in n], "p": [int(x) for x in p], "genotype_bytes": int(np.sum(n * p)),
+            "device_gb_in_use": round((total - free) / 1e9, 1), "generate_s": round(t_gen, 1),
+            "z_build_and_init_s": round(t_setup, 1), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def profile_case(args):
     """Small case for kernel captures: same per-subset shape as the workload."""
     import torch
@@ -638,11 +717,26 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="n=20000, p=20000 case of the same subset shape, for ncu captures")
     ap.add_argument("--precision", default="fp8", choices=["fp64", "fp32", "fp8"], help="--profile-case only")
-    ap.add_argument("--workload", default="c3", choices=["c3", "c5"],
-                    help="c5: config 5 (BayesRc, n=50000, p=1000000, 16 chains) on its own JSON line")
+    ap.add_argument("--workload", default="c3", choices=["c3", "c4", "c5"],
+                    help="c4: config 4 (32 BayesB analyses in one launch per kernel); c5: config 5 (BayesRc, "
+                         "n=50000, p=1000000, 16 chains); each on its own JSON line")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one replica per GPU: relaunch this command under torch.distributed.run
+        import socket
+        with socket.socket() as so:
+            so.bind(("127.0.0.1", 0))
+            port = so.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(args.gpus),
+               "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+        os.execv(sys.executable, cmd)
     if args.profile_case:
         profile_case(args)
+        return
+    if args.workload == "c4":
+        if args.warmup < 3:
+            args.warmup = 3
+        workload_c4(args)
         return
     if args.workload == "c5":
         if args.warmup < 3:
@@ -676,8 +770,8 @@ def main():
         line = {"metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "u8 genotype codes (exact 0/1/2) x bf16 hi/mid/lo splits of the residuals, delta and "
-                         "U, FP32 accumulation, FP32 draws; FP64 residual masters",
+                "dtype": "2-bit packed genotype codes widened to exact bf16 0/1/2 on chip x bf16 hi/mid/lo splits "
+                         "of the residuals, delta and U; FP32 accumulation, FP32 draws, FP64 residual masters",
                 "data": "synthetic (seeded generator of config 3)",
                 "config": {**config, "chains": args.chains, "precision": "fp8", "settle_iterations": args.settle,
                            "parallelism": f"replicas x{ws}"},

@@ -311,6 +311,55 @@ int sodagpu_compute_dgv_noalloc(int32_t nind, int32_t nloci, const int8_t *codes
                                 const double *freq, double mu, const double *effects, double *pred,
                                 void *stream);
 
+/* ---- many analyses in one launch per kernel ------------------------------
+ * A batch runs the iterations of several independent jobs (analyses of their
+ * own n, p, phenotype, priors and seed) together: every kernel of an
+ * iteration is launched once over all jobs (each CTA finds its job in a
+ * table), and step t of the subset loop runs subset t of every job that has
+ * one.  No counterpart in the reference, which runs one analysis per .par job
+ * (SODABayes.f90:35-97) with soda_bayes (models.f90:9-605) each time; each
+ * job in a batch takes exactly the draws, and gives exactly the results, it
+ * would give on its own.  The jobs are ordinary contexts, created, loaded,
+ * Z-built and initialised one by one (sodagpu_init_chains), on one device,
+ * with one precision and chain count, and run on the CUDA-core kernels
+ * (SODAGPU_KERNELS_CUDA_CORES, or fewer than 4 chains); after a batch run
+ * their state and results are read with the per-job calls.  A job may belong
+ * to one batch at a time and must not be run on its own meanwhile. */
+#define SODAGPU_MAXJOBS 64
+/* flags of sodagpu_batch_create.  By default each job's rhs products get K
+ * splits in proportion to its share of the batch's genotype bytes, so that
+ * the batch's CTAs make about one wave; the partial sums of a split are then
+ * added in another grouping than in a job run on its own (results equal to
+ * rounding).  SOLO_SPLITS keeps every job's own splits: bit-identical
+ * results to the job run on its own. */
+#define SODAGPU_BATCH_SOLO_SPLITS 1
+typedef struct sodagpu_batch sodagpu_batch;
+int sodagpu_batch_create(sodagpu_batch **out, sodagpu_ctx *const *jobs, int32_t njobs, int32_t flags);
+/* `iters` iterations of every job (no trace rows are gathered). */
+int sodagpu_batch_run(sodagpu_batch *batch, int32_t iters);
+/* Device time of the last sodagpu_batch_run, in milliseconds (CUDA events on
+ * the batch's stream around the iteration launches), and the subset steps of
+ * one iteration (the largest subset count of the jobs). */
+int sodagpu_batch_timings(sodagpu_batch *batch, double *run_device_ms, int32_t *steps);
+void sodagpu_batch_destroy(sodagpu_batch *batch);
+
+/* Subset sizes for a batch of njobs analyses (n[j] individuals, p[j] SNPs)
+ * that will run `iters` iterations.  All jobs share one step count S (the
+ * subset loop runs in lock step), job j gets blocksize[j] = ceil(p[j] / S),
+ * capped at max_blocksize, and S is the candidate of least modelled time:
+ *   iters * (S * step_us + sum_j stream_bytes_j(S) / bw)  +  sum_j zbuild_j(S)
+ * where stream_bytes_j reads job j's codes and its factor's triangle twice
+ * per iteration (rhs and update; e_x and e_u bytes per element), and
+ * zbuild_j = p[j] * (n[j] * N_j / gram_ops + N_j^2 / (3 * fp64_flops)) is the
+ * Gram and Cholesky of its subsets (N_j = blocksize[j]).  model[] holds
+ * {step_us, bw (bytes/s), e_x, e_u, gram_ops (int8 multiply-adds/s),
+ * fp64_flops}; NULL takes values measured on GB300 for the FP8 mode
+ * {30, 4e12, 1, 4, 5e13, 6e11}.  *steps receives S and *model_s the
+ * modelled seconds of the choice. */
+int sodagpu_autotune_batch(int32_t njobs, const int32_t *n, const int32_t *p, int32_t iters,
+                           int32_t max_blocksize, const double *model, int32_t *blocksize, int32_t *steps,
+                           double *model_s);
+
 void sodagpu_destroy(sodagpu_ctx *ctx);
 const char *sodagpu_errstr(int code);
 const char *sodagpu_last_error(void);

@@ -374,6 +374,56 @@ class SodaJob:
         return {names[k]: (float(ms[k]), int(n[k])) for k in range(len(names))}
 
 
+class SodaBatch:
+    """Several SodaJob analyses run together: every kernel of an iteration is
+    launched once over all of them (sodagpu_batch_create).  Each job keeps
+    its own results, exactly those it would give on its own; read them with
+    the job's methods after run()."""
+
+    def __init__(self, jobs, solo_splits: bool = False):
+        self._lib = library()
+        self.jobs = list(jobs)
+        arr = (C.c_void_p * len(self.jobs))(*[j._ctx.value for j in self.jobs])
+        self._b = C.c_void_p()
+        flags = _abi.BATCH_SOLO_SPLITS if solo_splits else 0
+        _check(self._lib.sodagpu_batch_create(C.byref(self._b), arr, len(self.jobs), flags), "sodagpu_batch_create")
+
+    def run(self, iters: int) -> None:
+        _check(self._lib.sodagpu_batch_run(self._b, int(iters)), "sodagpu_batch_run")
+
+    def timings(self):
+        """(device milliseconds of the last run, subset steps per iteration)"""
+        ms, st = C.c_double(), C.c_int32()
+        _check(self._lib.sodagpu_batch_timings(self._b, C.byref(ms), C.byref(st)), "sodagpu_batch_timings")
+        return ms.value, st.value
+
+    def close(self) -> None:
+        if self._b:
+            self._lib.sodagpu_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def autotune_batch(n, p, iters: int, max_blocksize: int = 2000, model=None):
+    """Subset sizes for a batch (sodagpu_autotune_batch): returns (blocksizes,
+    steps, modelled seconds)."""
+    lib = library()
+    nn = np.ascontiguousarray(n, dtype=np.int32)
+    pp = np.ascontiguousarray(p, dtype=np.int32)
+    bs = np.zeros(nn.shape[0], dtype=np.int32)
+    steps, secs = C.c_int32(), C.c_double()
+    m = None if model is None else np.ascontiguousarray(model, dtype=np.float64)
+    _check(lib.sodagpu_autotune_batch(nn.shape[0], _ip(nn), _ip(pp), int(iters), int(max_blocksize),
+                                      None if m is None else _dp(m), _ip(bs), C.byref(steps), C.byref(secs)),
+           "sodagpu_autotune_batch")
+    return bs, steps.value, secs.value
+
+
 def predict(codes=None, freq=None, mu: float = 0.0, effects=None, bed: Optional[np.ndarray] = None,
             nind: Optional[int] = None) -> np.ndarray:
     """Prediction mode (utilities.f90:540-553, 616-622): mu + X*effects with

@@ -72,8 +72,16 @@ PROTOTYPES = {
     "sodagpu_timings": (C.c_int, [_P, _DP, _DP, _DP]),
     "sodagpu_profile_kernels": (C.c_int, [_P, C.c_int32, _DP, _IP]),
     "sodagpu_compute_dgv_noalloc": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int32, _P, C.c_double, _P, _P, _P]),
+    "sodagpu_batch_create": (C.c_int, [C.POINTER(_P), C.POINTER(_P), C.c_int32, C.c_int32]),
+    "sodagpu_batch_run": (C.c_int, [_P, C.c_int32]),
+    "sodagpu_batch_timings": (C.c_int, [_P, _DP, _IP]),
+    "sodagpu_batch_destroy": (None, [_P]),
+    "sodagpu_autotune_batch": (C.c_int, [C.c_int32, _IP, _IP, C.c_int32, C.c_int32, _DP, _IP, _IP, _DP]),
     "sodagpu_destroy": (None, [_P]),
 }
+
+MAXJOBS = 64
+BATCH_SOLO_SPLITS = 1
 
 
 def bind(lib: C.CDLL, prototypes: dict) -> C.CDLL:

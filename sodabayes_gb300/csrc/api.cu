@@ -1338,6 +1338,203 @@ int sodagpu_profile_kernels(sodagpu_ctx *c, int32_t iters, double *ms, int32_t *
     return rc;
 }
 
+}  // extern "C"
+
+struct sodagpu_batch {
+    std::vector<sodagpu_ctx *> jobs;
+    int dev = 0, sm_count = 0, steps = 0;
+    cudaStream_t st = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    Dev *ddev = nullptr;
+    double last_ms = 0.0;
+};
+
+extern "C" {
+
+void sodagpu_batch_destroy(sodagpu_batch *b)
+{
+    if (!b) return;
+    if (b->st) cudaStreamSynchronize(b->st);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->ddev) cudaFree(b->ddev);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+int sodagpu_batch_create(sodagpu_batch **out, sodagpu_ctx *const *jobs, int32_t njobs, int32_t flags)
+{
+    if (flags & ~SODAGPU_BATCH_SOLO_SPLITS) return fail(SODAGPU_E_ARG, "unknown flags 0x%x", flags);
+    if (!out || !jobs) return fail(SODAGPU_E_ARG, "null argument");
+    *out = nullptr;
+    if (njobs < 1 || njobs > SODAGPU_MAXJOBS) return fail(SODAGPU_E_ARG, "njobs %d outside 1..%d", njobs, SODAGPU_MAXJOBS);
+    for (int j = 0; j < njobs; ++j) {
+        const sodagpu_ctx *c = jobs[j];
+        if (!c) return fail(SODAGPU_E_ARG, "job %d is null", j);
+        for (int k = 0; k < j; ++k)
+            if (jobs[k] == c) return fail(SODAGPU_E_ARG, "job %d appears twice", j);
+        if (!c->have_chain) return fail(SODAGPU_E_STATE, "job %d: call sodagpu_init_chains first", j);
+        if (c->tc) return fail(SODAGPU_E_UNSUPPORTED, "job %d runs the tensor-core kernels; batches run the CUDA-core "
+                                                      "kernels (SODAGPU_KERNELS_CUDA_CORES or fewer than 4 chains)", j);
+        if (c->regular) return fail(SODAGPU_E_UNSUPPORTED, "job %d: the regular sampler is not batched", j);
+        if (c->tape) return fail(SODAGPU_E_UNSUPPORTED, "job %d has an injected-draw tape", j);
+        if (c->dev != jobs[0]->dev || c->C != jobs[0]->C || c->D.precision != jobs[0]->D.precision)
+            return fail(SODAGPU_E_ARG, "job %d: every job of a batch needs the same device, chain count and precision", j);
+    }
+    CUDA_TRY(cudaSetDevice(jobs[0]->dev));
+    for (int j = 0; j < njobs; ++j) CUDA_TRY(cudaStreamSynchronize(jobs[j]->st));
+    sodagpu_batch *b = new sodagpu_batch;
+    b->jobs.assign(jobs, jobs + njobs);
+    b->dev = jobs[0]->dev;
+    b->sm_count = jobs[0]->sm_count;
+    int max_bs = 0;
+    for (auto *c : b->jobs) {
+        max_bs = std::max(max_bs, c->bs);
+        b->steps = std::max(b->steps, c->nb);
+    }
+    const int prec = jobs[0]->D.precision, C = jobs[0]->C;
+    if (sweep_multi_prepare(prec, C, max_bs) != cudaSuccess) {
+        sodagpu_batch_destroy(b);
+        return fail(SODAGPU_E_UNSUPPORTED, "blocksize %d too large", max_bs);
+    }
+    // the rhs of every job gets a share of one wave of CTAs in proportion to its genotype bytes per step
+    std::vector<Dev> hdev(njobs);
+    std::vector<const int *> bsz(njobs);
+    std::vector<int> ks(njobs);
+    double wsum = 0.0;
+    for (auto *c : b->jobs) wsum += (double)c->n * c->bs;
+    for (int j = 0; j < njobs; ++j) {
+        sodagpu_ctx *c = b->jobs[j];
+        hdev[j] = c->D;
+        bsz[j] = c->blk_sizes.data();
+        // a job on its own takes one wave of CTAs for its rhs
+        const int share = (flags & SODAGPU_BATCH_SOLO_SPLITS)
+                              ? b->sm_count
+                              : std::max(1, (int)std::lround(b->sm_count * (double)c->n * c->bs / wsum));
+        ks[j] = sweep_multi_rhs_split(prec, c->bs, C, c->ldx, share);
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&b->ddev, sizeof(Dev) * njobs);
+    if (e == cudaSuccess) e = cudaMemcpy(b->ddev, hdev.data(), sizeof(Dev) * njobs, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        sodagpu_batch_destroy(b);
+        return fail(SODAGPU_E_CUDA, "batch set-up: %s", cudaGetErrorString(e));
+    }
+    BatchPlan P{njobs, hdev.data(), b->ddev, bsz.data(), ks.data()};
+    cudaGraph_t gr;
+    e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t e1 = sweep_enqueue_iteration_multi(P, b->sm_count, b->st);
+        cudaError_t e2 = cudaStreamEndCapture(b->st, &gr);
+        e = e1 != cudaSuccess ? e1 : e2;
+        if (e == cudaSuccess) {
+            e = cudaGraphInstantiate(&b->graph, gr, 0);
+            cudaGraphDestroy(gr);
+        }
+    }
+    if (e != cudaSuccess) {
+        sodagpu_batch_destroy(b);
+        return fail(SODAGPU_E_CUDA, "capturing the batched iteration: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return 0;
+}
+
+int sodagpu_batch_run(sodagpu_batch *b, int32_t iters)
+{
+    if (!b) return fail(SODAGPU_E_ARG, "null argument");
+    if (iters < 0) return fail(SODAGPU_E_ARG, "iters < 0");
+    if (iters == 0) return 0;
+    CUDA_TRY(cudaSetDevice(b->dev));
+    // each job's control block: no trace rows; the job's own stream drained first
+    for (auto *c : b->jobs) {
+        RunCtl h{};
+        CUDA_TRY(cudaMemcpyAsync(&h, c->ctl, sizeof h, cudaMemcpyDeviceToHost, c->st));
+        CUDA_TRY(cudaStreamSynchronize(c->st));
+        h.trace_iter = 0;
+        h.trace_cap = 0;
+        h.trace_count = 0;
+        h.trace = nullptr;
+        CUDA_TRY(cudaMemcpyAsync(c->ctl, &h, sizeof h, cudaMemcpyHostToDevice, c->st));
+        CUDA_TRY(cudaStreamSynchronize(c->st));
+    }
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaEventRecord(e0, b->st));
+    for (int t = 0; t < iters; ++t) CUDA_TRY(cudaGraphLaunch(b->graph, b->st));
+    CUDA_TRY(cudaEventRecord(e1, b->st));
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->last_ms = ms;
+    for (size_t j = 0; j < b->jobs.size(); ++j) {
+        RunCtl h{};
+        CUDA_TRY(cudaMemcpy(&h, b->jobs[j]->ctl, sizeof h, cudaMemcpyDeviceToHost));
+        if (h.err) return fail(SODAGPU_E_TIMEOUT, "job %zu: a bounded device loop gave up (code %d)", j, h.err);
+    }
+    return 0;
+}
+
+int sodagpu_batch_timings(sodagpu_batch *b, double *run_device_ms, int32_t *steps)
+{
+    if (!b) return fail(SODAGPU_E_ARG, "null argument");
+    if (run_device_ms) *run_device_ms = b->last_ms;
+    if (steps) *steps = b->steps;
+    return 0;
+}
+
+int sodagpu_autotune_batch(int32_t njobs, const int32_t *n, const int32_t *p, int32_t iters, int32_t max_blocksize,
+                           const double *model, int32_t *blocksize, int32_t *steps, double *model_s)
+{
+    if (!n || !p || !blocksize) return fail(SODAGPU_E_ARG, "null argument");
+    if (njobs < 1 || njobs > SODAGPU_MAXJOBS) return fail(SODAGPU_E_ARG, "njobs %d outside 1..%d", njobs, SODAGPU_MAXJOBS);
+    if (iters < 1 || max_blocksize < 2) return fail(SODAGPU_E_ARG, "iters < 1 or max_blocksize < 2");
+    static const double dflt[6] = {30.0, 4e12, 1.0, 4.0, 5e13, 6e11};
+    const double *m = model ? model : dflt;
+    for (int q = 0; q < 6; ++q)
+        if (!(m[q] > 0.0)) return fail(SODAGPU_E_ARG, "model[%d] must be positive", q);
+    int pmax = 0;
+    for (int j = 0; j < njobs; ++j) {
+        if (n[j] < 1 || p[j] < 1) return fail(SODAGPU_E_ARG, "job %d: n and p must be positive", j);
+        pmax = std::max(pmax, p[j]);
+    }
+    // S from the smallest that respects max_blocksize up to one SNP per subset; candidates grow by 1/16
+    int s_lo = 1;
+    for (int j = 0; j < njobs; ++j) s_lo = std::max(s_lo, (p[j] + max_blocksize - 1) / max_blocksize);
+    auto cost = [&](int S) {
+        double per_iter = S * m[0] * 1e-6, build = 0.0;
+        for (int j = 0; j < njobs; ++j) {
+            const double N = std::min<double>(max_blocksize, std::ceil((double)p[j] / S));
+            const double bytes = 2.0 * ((double)n[j] * p[j] * m[2] + (double)p[j] * (N + 1.0) / 2.0 * m[3]);
+            per_iter += bytes / m[1];
+            build += (double)p[j] * ((double)n[j] * N / m[4] + N * N / (3.0 * m[5]));
+        }
+        return iters * per_iter + build;
+    };
+    int best = s_lo;
+    double best_c = cost(s_lo);
+    for (int S = s_lo; S <= pmax;) {
+        const double cst = cost(S);
+        if (cst < best_c) {
+            best_c = cst;
+            best = S;
+        }
+        const int nx = S + std::max(1, S / 16);
+        if (nx > pmax && S < pmax) S = pmax;
+        else S = nx;
+    }
+    int smax = 0;
+    for (int j = 0; j < njobs; ++j) {
+        blocksize[j] = std::min(max_blocksize, (p[j] + best - 1) / best);
+        smax = std::max(smax, (p[j] + blocksize[j] - 1) / blocksize[j]);
+    }
+    if (steps) *steps = smax;
+    if (model_s) *model_s = best_c;
+    return 0;
+}
+
 void sodagpu_destroy(sodagpu_ctx *c)
 {
     if (!c) return;

@@ -87,7 +87,7 @@ __device__ __forceinline__ float code_to_f32(uint32_t w, int k)
 // three-way split of delta/sd per chain (dsplit; pairs up to `span`, past the
 // subset's end, write zeros) and per-CTA sums of x0_j delta_j (k0part).
 template <int MODE, int CT, bool TC>
-__global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int span)
+__device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int ksplit, int span)
 {
     __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring)
     __shared__ double s_k[256];
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     constexpr int SPC = 256 / CT;   // SNPs per CTA
     const int tid = threadIdx.x;
     const int jloc = tid % SPC, c = tid / SPC;
-    const int jl = blockIdx.x * SPC + jloc;
+    const int jl = vb.x * SPC + jloc;
     if (tid < SPC) s_nzf[tid] = 0;
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
@@ -257,19 +257,26 @@ __global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int s
     if (TC && tid < CT) {
         double tt = 0.0;
         for (int q = 0; q < SPC; ++q) tt += s_k[q * CT + tid];
-        D.k0part[(size_t)blockIdx.x * CT + tid] = tt;
+        D.k0part[(size_t)vb.x * CT + tid] = tt;
     }
     // delta32 chain-contiguous per SNP (the CTA's block of 256 values), and the flags of SNPs whose
     // delta is non-zero in some chain
     if (MODE != SODAGPU_FP64) {
-        const int j = blockIdx.x * SPC + tid / CT;
-        if (j < N) D.delta32[(size_t)blockIdx.x * 256 + tid] = s_d32[tid];
+        const int j = vb.x * SPC + tid / CT;
+        if (j < N) D.delta32[(size_t)vb.x * 256 + tid] = s_d32[tid];
     }
-    if (tid < SPC && blockIdx.x * SPC + tid < N) D.nzflag[blockIdx.x * SPC + tid] = s_nzf[tid];
+    if (tid < SPC && vb.x * SPC + tid < N) D.nzflag[vb.x * SPC + tid] = s_nzf[tid];
 }
 
+template <int MODE, int CT, bool TC>
+__global__ void __launch_bounds__(256, 1) k_draw(Dev D, int b, int ksplit, int span)
+{
+    draw_body<MODE, CT, TC>(D, vb_native(), b, ksplit, span);
+}
+
+
 template <int MODE, int CT>
-__global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
+__device__ __forceinline__ void rhs_body(const Dev &D, const VB &vb, int b, int ksplit)
 {
     using Cfg = RhsCfg<MODE>;
     constexpr int SPT = SptOf<CT>::v;
@@ -289,7 +296,7 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     tc::pdl_trigger();
     const int ls = D.blk_ls[b];
     const int N = D.blk_ls[b + 1] - ls;
-    const int mt = blockIdx.x / ksplit, ks = blockIdx.x % ksplit;
+    const int mt = vb.x / ksplit, ks = vb.x % ksplit;
     const int j0 = mt * MTS;
     if (j0 >= N) return;
     const int npad = (N + 7) & ~7;             // spacing of the subset's U columns
@@ -510,5 +517,12 @@ __global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
     publish(true);
 
 }
+
+template <int MODE, int CT>
+__global__ void __launch_bounds__(256, 1) k_rhs(Dev D, int b, int ksplit)
+{
+    rhs_body<MODE, CT>(D, vb_native(), b, ksplit);
+}
+
 
 }  // namespace soda

@@ -136,6 +136,51 @@ struct Dev {
     int tape_reps, tape_sites, tape_snp0;
 };
 
+// Block coordinates of a CTA in its own job's grid.  A plain launch takes the
+// hardware's; a batched launch (the grids of several jobs laid end to end
+// along x, JobGrid) maps blockIdx.x to (job, x, y, z) first.
+struct VB {
+    int x, y, z, nx, ny, nz;
+};
+
+__device__ __forceinline__ VB vb_native()
+{
+    return VB{(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x, (int)gridDim.y, (int)gridDim.z};
+}
+
+// One launch over several jobs: job j owns CTAs off[j] .. off[j+1]-1 of a
+// 1-D grid, its own grid being gx[j] x gy[j] x (the rest), and the kernel's
+// integer arguments for it are arg[j][0..2].  Passed by value (grid constant).
+constexpr int MAXJOBS = 64;
+struct JobGrid {
+    const Dev *dev;            // [njobs] the jobs' descriptors in device memory
+    int njobs;
+    int off[MAXJOBS + 1];
+    int gx[MAXJOBS], gy[MAXJOBS];
+    int arg[MAXJOBS][3];
+};
+
+// The job of this CTA (the last j with off[j] <= blockIdx.x, so jobs without
+// CTAs are passed over) and its block coordinates in that job's grid.
+__device__ __forceinline__ int jg_locate(const JobGrid &G, VB &vb)
+{
+    const int bid = (int)blockIdx.x;
+    int lo = 0, hi = G.njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (G.off[mid] <= bid) lo = mid;
+        else hi = mid - 1;
+    }
+    const int l = bid - G.off[lo], gx = G.gx[lo], gy = G.gy[lo];
+    vb.nx = gx;
+    vb.ny = gy;
+    vb.nz = (G.off[lo + 1] - G.off[lo]) / (gx * gy);
+    vb.x = l % gx;
+    vb.y = (l / gx) % gy;
+    vb.z = l / (gx * gy);
+    return lo;
+}
+
 constexpr int RHS_KSPLIT_MAX = 16;
 
 constexpr int NSTAT = 64;          // CTAs of the per-iteration SNP statistics

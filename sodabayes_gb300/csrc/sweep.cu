@@ -373,7 +373,7 @@ namespace soda {
 // ---------------------------------------------------------------------------
 // iteration start and the mu draw
 // ---------------------------------------------------------------------------
-__global__ void k_iter_begin(Dev D)
+__device__ __forceinline__ void iter_begin_body(const Dev &D, const VB &vb)
 {
     RunCtl *ctl = D.ctl;
     const int rep = ctl->rep + 1;
@@ -381,26 +381,38 @@ __global__ void k_iter_begin(Dev D)
     if (rep % D.thin == 0) ctl->trace_iter += 1;
 }
 
-__global__ void __launch_bounds__(ROW_THREADS) k_mu_partial(Dev D)
+__global__ void  k_iter_begin(Dev D)
+{
+    iter_begin_body(D, vb_native());
+}
+
+
+__device__ __forceinline__ void mu_partial_body(const Dev &D, const VB &vb)
 {
     __shared__ double sh[33];
-    const int c = blockIdx.y, rep = cur_rep(D);
+    const int c = vb.y, rep = cur_rep(D);
     const double mu_old = D.scal[c].mu[(rep - 1) & 1];
     double v = 0.0;
 #pragma unroll
     for (int q = 0; q < ROWS_PER_THREAD; ++q) {
-        const int i = blockIdx.x * ROW_TILE + q * ROW_THREADS + threadIdx.x;
+        const int i = vb.x * ROW_TILE + q * ROW_THREADS + threadIdx.x;
         if (i < D.n) v += D.r[(size_t)c * D.ldr + i] + mu_old;
     }
     const double t = block_sum(v, sh);
-    if (threadIdx.x == 0) D.rpart[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+    if (threadIdx.x == 0) D.rpart[(size_t)c * D.nr_ctas + vb.x] = t;
 }
 
-__global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
+__global__ void __launch_bounds__(ROW_THREADS) k_mu_partial(Dev D)
+{
+    mu_partial_body(D, vb_native());
+}
+
+
+__device__ __forceinline__ void mu_apply_body(const Dev &D, const VB &vb)
 {
     __shared__ double sh[33];
     __shared__ double s_mu;
-    const int c = blockIdx.y, rep = cur_rep(D);
+    const int c = vb.y, rep = cur_rep(D);
     ChainScal *S = &D.scal[c];
     const double mu_old = S->mu[(rep - 1) & 1];
     if (threadIdx.x == 0) {
@@ -411,14 +423,14 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
         const double nn = (double)D.n;
         const double mu = d_rnorm(tot / nn, sqrt(S->vare / nn), R);
         s_mu = mu;
-        if (blockIdx.x == 0) S->mu[rep & 1] = mu;
+        if (vb.x == 0) S->mu[rep & 1] = mu;
     }
     __syncthreads();
     const double mu = s_mu;
     double vs = 0.0;
 #pragma unroll
     for (int q = 0; q < ROWS_PER_THREAD; ++q) {
-        const int i = blockIdx.x * ROW_TILE + q * ROW_THREADS + threadIdx.x;
+        const int i = vb.x * ROW_TILE + q * ROW_THREADS + threadIdx.x;
         if (i < D.n) {
             const double v = (D.r[(size_t)c * D.ldr + i] + mu_old) - mu;
             store_r(D, c, i, v);
@@ -427,9 +439,15 @@ __global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
     }
     if (D.precision == SODAGPU_FP8) {
         const double t = block_sum(vs, sh);
-        if (threadIdx.x == 0) D.rsum[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+        if (threadIdx.x == 0) D.rsum[(size_t)c * D.nr_ctas + vb.x] = t;
     }
 }
+
+__global__ void __launch_bounds__(ROW_THREADS) k_mu_apply(Dev D)
+{
+    mu_apply_body(D, vb_native());
+}
+
 
 }  // namespace soda
 
@@ -572,12 +590,12 @@ __device__ __forceinline__ double single_site_draw(const Dev &D, ChainScal *S, i
     return upd;
 }
 
-__global__ void __launch_bounds__(SS_THREADS) k_skipped(Dev D)
+__device__ __forceinline__ void skipped_body(const Dev &D, const VB &vb)
 {
     extern __shared__ double s_r[];
     __shared__ double s_part[SS_THREADS / 32];
     __shared__ double s_upd;
-    const int c = blockIdx.x, rep = cur_rep(D);
+    const int c = vb.x, rep = cur_rep(D);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     ChainScal *S = &D.scal[c];
     double *rg = D.r + (size_t)c * D.ldr;
@@ -622,22 +640,28 @@ __global__ void __launch_bounds__(SS_THREADS) k_skipped(Dev D)
     }
 }
 
+__global__ void __launch_bounds__(SS_THREADS) k_skipped(Dev D)
+{
+    skipped_body(D, vb_native());
+}
+
+
 // ---------------------------------------------------------------------------
 // per-iteration statistics: class counts and sum g^2 per (group, class),
 // sum r^2 (models.f90:194, 321-325, 496-503, 515)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_stats(Dev D)
+__device__ __forceinline__ void stats_body(const Dev &D, const VB &vb)
 {
     __shared__ double sh[33];
-    const int c = blockIdx.y;
-    if (blockIdx.x < NSTAT) {
+    const int c = vb.y;
+    if (vb.x < NSTAT) {
         const int ngm = D.ngroup * D.nmix;
         const size_t base = (size_t)c * D.p;
         for (int e = 0; e < ngm; ++e) {
             const int eg = e % D.ngroup, em = e / D.ngroup;
             double v = 0.0;
             int cnt = 0;
-            for (int j = blockIdx.x * 256 + threadIdx.x; j < D.p; j += NSTAT * 256) {
+            for (int j = vb.x * 256 + threadIdx.x; j < D.p; j += NSTAT * 256) {
                 const int cl = D.cls[base + j];
                 if (D.grp[j] - 1 == eg && cl - 1 == em) {
                     const double gj = D.g[base + j];
@@ -648,13 +672,13 @@ __global__ void __launch_bounds__(256) k_stats(Dev D)
             const double tv = block_sum(v, sh);
             const double tc = block_sum((double)cnt, sh);
             if (threadIdx.x == 0) {
-                const size_t o = ((size_t)c * NSTAT + blockIdx.x) * ngm + e;
+                const size_t o = ((size_t)c * NSTAT + vb.x) * ngm + e;
                 D.statpart[o] = tv;
                 D.cntpart[o] = (int32_t)tc;
             }
         }
     } else {
-        const int rb = blockIdx.x - NSTAT;
+        const int rb = vb.x - NSTAT;
         double v2 = 0.0;
         const int i = rb * ROW_TILE + threadIdx.x;
         if (threadIdx.x < ROW_TILE && i < D.n) {
@@ -666,10 +690,16 @@ __global__ void __launch_bounds__(256) k_stats(Dev D)
     }
 }
 
-__global__ void __launch_bounds__(128) k_hyper(Dev D)
+__global__ void __launch_bounds__(256) k_stats(Dev D)
+{
+    stats_body(D, vb_native());
+}
+
+
+__device__ __forceinline__ void hyper_body(const Dev &D, const VB &vb)
 {
     __shared__ double s_vara;
-    const int c = blockIdx.x, rep = cur_rep(D);
+    const int c = vb.x, rep = cur_rep(D);
     ChainScal *S = &D.scal[c];
     const int ng = D.ngroup, nm = D.nmix, ngm = ng * nm, m = D.method;
     for (int e = threadIdx.x; e < ngm; e += blockDim.x) {
@@ -773,12 +803,18 @@ __global__ void __launch_bounds__(128) k_hyper(Dev D)
     }
 }
 
-// ra redraw (models.f90:523-525) and the per-SNP accumulators (528, 535-538, 544)
-__global__ void __launch_bounds__(256) k_post(Dev D)
+__global__ void __launch_bounds__(128) k_hyper(Dev D)
 {
-    const int c = blockIdx.y, rep = cur_rep(D);
+    hyper_body(D, vb_native());
+}
+
+
+// ra redraw (models.f90:523-525) and the per-SNP accumulators (528, 535-538, 544)
+__device__ __forceinline__ void post_body(const Dev &D, const VB &vb)
+{
+    const int c = vb.y, rep = cur_rep(D);
     const ChainScal *S = &D.scal[c];
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int t0 = vb.x * blockDim.x + threadIdx.x, stride = vb.nx * blockDim.x;
     const double sd = sqrt(S->vare);
     for (int i = t0; i < D.naind; i += stride) {
         CRng R;
@@ -796,13 +832,19 @@ __global__ void __launch_bounds__(256) k_post(Dev D)
     }
 }
 
+__global__ void __launch_bounds__(256) k_post(Dev D)
+{
+    post_body(D, vb_native());
+}
+
+
 // compute_residuals (utilities.f90:609-614), every `recal` iterations
-__global__ void __launch_bounds__(256) k_recal_partial(Dev D, int force)
+__device__ __forceinline__ void recal_partial_body(const Dev &D, const VB &vb, int force)
 {
     const int rep = cur_rep(D);
     if (!force && (D.recal <= 0 || rep % D.recal != 0)) return;
-    const int c = blockIdx.z, split = blockIdx.y;
-    const int i = blockIdx.x * 256 + threadIdx.x;
+    const int c = vb.z, split = vb.y;
+    const int i = vb.x * 256 + threadIdx.x;
     if (i >= D.n) return;
     const int per = (D.p + RECAL_SPLIT - 1) / RECAL_SPLIT;
     const int k0 = split * per, k1 = min(D.p, k0 + per);
@@ -816,18 +858,30 @@ __global__ void __launch_bounds__(256) k_recal_partial(Dev D, int force)
     D.recal_part[((size_t)c * RECAL_SPLIT + split) * D.ldr + i] = acc;
 }
 
-__global__ void __launch_bounds__(256) k_recal_apply(Dev D, int force, int mu_slot)
+__global__ void __launch_bounds__(256) k_recal_partial(Dev D, int force)
+{
+    recal_partial_body(D, vb_native(), force);
+}
+
+
+__device__ __forceinline__ void recal_apply_body(const Dev &D, const VB &vb, int force, int mu_slot)
 {
     const int rep = cur_rep(D);
     if (!force && (D.recal <= 0 || rep % D.recal != 0)) return;
-    const int c = blockIdx.y;
-    const int i = blockIdx.x * 256 + threadIdx.x;
+    const int c = vb.y;
+    const int i = vb.x * 256 + threadIdx.x;
     if (i >= D.n) return;
     double d = 0.0;
     for (int s = 0; s < RECAL_SPLIT; ++s) d = d + D.recal_part[((size_t)c * RECAL_SPLIT + s) * D.ldr + i];
     const int slot = mu_slot >= 0 ? mu_slot : (rep & 1);
     store_r(D, c, i, D.y[i] - d - D.scal[c].mu[slot]);
 }
+
+__global__ void __launch_bounds__(256) k_recal_apply(Dev D, int force, int mu_slot)
+{
+    recal_apply_body(D, vb_native(), force, mu_slot);
+}
+
 
 // ---------------------------------------------------------------------------
 // chain initialisation (models.f90:56-128)
@@ -1311,9 +1365,14 @@ void sweep_tc_tables(const int *blk_sizes, int nb, int bs, int ldx, int sm_count
     }
 }
 
-// Raises the dynamic shared-memory limits of the rhs and update kernels.
+// Raises the dynamic shared-memory limits of the rhs and update kernels (the
+// update's for the largest subset size asked for so far in this process:
+// the limit is per kernel, and every job's launches must stay within it).
 cudaError_t sweep_prepare(int bs)
 {
+    static int s_max_bs = 0;
+    if (bs < s_max_bs) bs = s_max_bs;
+    s_max_bs = bs;
     {
         cudaError_t e = carve_all();
         if (e == cudaSuccess) e = set_tc_smem<4>();
@@ -1448,6 +1507,287 @@ cudaError_t sweep_enqueue_recal(const Dev &D, double mu_slot_unused, cudaStream_
     (void)mu_slot_unused;
     k_recal_partial<<<dim3((D.n + 255) / 256, RECAL_SPLIT, D.chains), 256, 0, st>>>(D, 1);
     k_recal_apply<<<dim3((D.n + 255) / 256, D.chains), 256, 0, st>>>(D, 1, -1);
+    return cudaGetLastError();
+}
+
+}  // namespace soda
+
+// ---------------------------------------------------------------------------
+// Several jobs in one launch per kernel (the CUDA-core kernels; every job of a
+// batch has the same precision and chain count).  Each wrapper finds its job
+// and block coordinates (jg_locate) and runs the same body as the plain
+// kernel, so a job's results do not depend on the batch it runs in.
+// ---------------------------------------------------------------------------
+namespace soda {
+
+__global__ void k_iter_begin_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    iter_begin_body(G.dev[j], vb);
+}
+
+__global__ void __launch_bounds__(ROW_THREADS) k_mu_partial_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    mu_partial_body(G.dev[j], vb);
+}
+
+__global__ void __launch_bounds__(ROW_THREADS) k_mu_apply_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    mu_apply_body(G.dev[j], vb);
+}
+
+__global__ void __launch_bounds__(SS_THREADS) k_skipped_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    skipped_body(G.dev[j], vb);
+}
+
+__global__ void __launch_bounds__(256) k_stats_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    stats_body(G.dev[j], vb);
+}
+
+__global__ void __launch_bounds__(128) k_hyper_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    hyper_body(G.dev[j], vb);
+}
+
+__global__ void __launch_bounds__(256) k_post_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    post_body(G.dev[j], vb);
+}
+
+__global__ void __launch_bounds__(256) k_recal_partial_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    recal_partial_body(G.dev[j], vb, 0);
+}
+
+__global__ void __launch_bounds__(256) k_recal_apply_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    recal_apply_body(G.dev[j], vb, 0, -1);
+}
+
+template <int MODE, int CT>
+__global__ void __launch_bounds__(256, 1) k_rhs_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    rhs_body<MODE, CT>(G.dev[j], vb, G.arg[j][0], G.arg[j][1]);
+}
+
+template <int MODE, int CT>
+__global__ void __launch_bounds__(256, 1) k_draw_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    draw_body<MODE, CT, false>(G.dev[j], vb, G.arg[j][0], G.arg[j][1], G.arg[j][2]);
+}
+
+template <int MODE, int CT>
+__global__ void __launch_bounds__(32 * UpdWarps<MODE, CT>::v) k_update_m(const __grid_constant__ JobGrid G)
+{
+    VB vb;
+    const int j = jg_locate(G, vb);
+    update_body<MODE, CT>(G.dev[j], vb, G.arg[j][0]);
+}
+
+namespace {
+
+// Builds the JobGrid of one launch from each job's grid (x, y, z; all zero
+// for a job that sits the launch out) and arguments.
+struct GridBuilder {
+    JobGrid g;
+    explicit GridBuilder(const Dev *ddev, int njobs)
+    {
+        memset(&g, 0, sizeof g);
+        g.dev = ddev;
+        g.njobs = njobs;
+    }
+    void set(int j, int gx, int gy, int gz, int a0 = 0, int a1 = 0, int a2 = 0)
+    {
+        const int n = gx > 0 && gy > 0 && gz > 0 ? gx * gy * gz : 0;
+        g.gx[j] = gx > 0 ? gx : 1;
+        g.gy[j] = gy > 0 ? gy : 1;
+        g.off[j + 1] = g.off[j] + n;
+        g.arg[j][0] = a0;
+        g.arg[j][1] = a1;
+        g.arg[j][2] = a2;
+    }
+    int total() const { return g.off[g.njobs]; }
+};
+
+template <int MODE, int CT>
+static cudaError_t multi_step(const BatchPlan &P, int t, cudaStream_t st)
+{
+    const int nj = P.njobs;
+    constexpr int MTS = 8 * SptOf<CT>::v;
+    GridBuilder rhs(P.ddev, nj), draw(P.ddev, nj), upd(P.ddev, nj);
+    size_t usmem = 0;
+    for (int j = 0; j < nj; ++j) {
+        const Dev &D = P.hdev[j];
+        if (t >= D.nb) {
+            rhs.set(j, 0, 0, 0);
+            draw.set(j, 0, 0, 0);
+            upd.set(j, 0, 0, 0);
+            continue;
+        }
+        const int N = P.blk_sizes[j][t];
+        const int mtiles = (N + MTS - 1) / MTS;
+        const int ks = P.ksplit[j];
+        rhs.set(j, mtiles * ks, 1, 1, t, ks);
+        draw.set(j, (N * CT + 255) / 256, 1, 1, t, ks, N);
+        upd.set(j, D.nr_ctas + (D.bs + UT - 1) / UT, 1, 1, t);
+        usmem = std::max(usmem, update_smem_bytes_ct<MODE, CT>(D.bs));
+    }
+    if (rhs.total() == 0) return cudaSuccess;
+    cudaError_t e = launch_pdl(k_rhs_m<MODE, CT>, dim3(rhs.total()), dim3(256), rhs_smem_bytes<MODE, CT>(), st, rhs.g);
+    if (e == cudaSuccess) e = launch_pdl(k_draw_m<MODE, CT>, dim3(draw.total()), dim3(256), 0, st, draw.g);
+    if (e == cudaSuccess)
+        e = launch_pdl(k_update_m<MODE, CT>, dim3(upd.total()), dim3(32 * UpdWarps<MODE, CT>::v), usmem, st, upd.g);
+    return e;
+}
+
+template <int MODE>
+static cudaError_t multi_step_mode(const BatchPlan &P, int t, cudaStream_t st)
+{
+    switch (P.hdev[0].chains) {
+    case 1: return multi_step<MODE, 1>(P, t, st);
+    case 2: return multi_step<MODE, 2>(P, t, st);
+    case 4: return multi_step<MODE, 4>(P, t, st);
+    case 8: return multi_step<MODE, 8>(P, t, st);
+    case 16: return multi_step<MODE, 16>(P, t, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int MODE, int CT>
+static cudaError_t multi_attrs(size_t usmem)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_rhs_m<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)rhs_smem_bytes<MODE, CT>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_update_m<MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usmem);
+    if (e == cudaSuccess) e = max_carveout(k_rhs_m<MODE, CT>);
+    if (e == cudaSuccess) e = max_carveout(k_draw_m<MODE, CT>);
+    if (e == cudaSuccess) e = max_carveout(k_update_m<MODE, CT>);
+    return e;
+}
+
+template <int MODE>
+static cudaError_t multi_attrs_mode(int chains, int max_bs)
+{
+    switch (chains) {
+    case 1: return multi_attrs<MODE, 1>(update_smem_bytes_ct<MODE, 1>(max_bs));
+    case 2: return multi_attrs<MODE, 2>(update_smem_bytes_ct<MODE, 2>(max_bs));
+    case 4: return multi_attrs<MODE, 4>(update_smem_bytes_ct<MODE, 4>(max_bs));
+    case 8: return multi_attrs<MODE, 8>(update_smem_bytes_ct<MODE, 8>(max_bs));
+    case 16: return multi_attrs<MODE, 16>(update_smem_bytes_ct<MODE, 16>(max_bs));
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+cudaError_t sweep_multi_prepare(int precision, int chains, int max_bs)
+{
+    cudaError_t e = sweep_prepare(max_bs);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_skipped_m, cudaFuncAttributeMaxDynamicSharedMemorySize, SS_SMEM_MAX);
+    if (e != cudaSuccess) return e;
+    if (precision == SODAGPU_FP64) return multi_attrs_mode<SODAGPU_FP64>(chains, max_bs);
+    if (precision == SODAGPU_FP32) return multi_attrs_mode<SODAGPU_FP32>(chains, max_bs);
+    return multi_attrs_mode<SODAGPU_FP8>(chains, max_bs);
+}
+
+template <int MODE, int CT>
+static int multi_split(int N, int ldx, int cta_share)
+{
+    constexpr int MTS = 8 * SptOf<CT>::v;
+    const int mtiles = (N + MTS - 1) / MTS;
+    const int nst = (ldx + RhsCfg<MODE>::KST - 1) / RhsCfg<MODE>::KST;
+    int ks = cta_share / std::max(1, mtiles);
+    ks = std::max(1, std::min(ks, RHS_KSPLIT_MAX));
+    return std::min(ks, std::max(1, nst));
+}
+
+template <int MODE>
+static int multi_split_mode(int N, int chains, int ldx, int cta_share)
+{
+    switch (chains) {
+    case 1: return multi_split<MODE, 1>(N, ldx, cta_share);
+    case 2: return multi_split<MODE, 2>(N, ldx, cta_share);
+    case 4: return multi_split<MODE, 4>(N, ldx, cta_share);
+    case 8: return multi_split<MODE, 8>(N, ldx, cta_share);
+    default: return multi_split<MODE, 16>(N, ldx, cta_share);
+    }
+}
+
+int sweep_multi_rhs_split(int precision, int N, int chains, int ldx, int cta_share)
+{
+    if (precision == SODAGPU_FP64) return multi_split_mode<SODAGPU_FP64>(N, chains, ldx, cta_share);
+    if (precision == SODAGPU_FP32) return multi_split_mode<SODAGPU_FP32>(N, chains, ldx, cta_share);
+    return multi_split_mode<SODAGPU_FP8>(N, chains, ldx, cta_share);
+}
+
+cudaError_t sweep_enqueue_iteration_multi(const BatchPlan &P, int sm_count, cudaStream_t st)
+{
+    const int nj = P.njobs;
+    if (nj < 1 || nj > MAXJOBS) return cudaErrorInvalidValue;
+    const int prec = P.hdev[0].precision;
+    GridBuilder one(P.ddev, nj), rows(P.ddev, nj);
+    int maxnb = 0;
+    for (int j = 0; j < nj; ++j) {
+        const Dev &D = P.hdev[j];
+        one.set(j, 1, 1, 1);
+        rows.set(j, D.nr_ctas, D.chains, 1);
+        maxnb = std::max(maxnb, D.nb);
+    }
+    k_iter_begin_m<<<one.total(), 1, 0, st>>>(one.g);
+    k_mu_partial_m<<<rows.total(), ROW_THREADS, 0, st>>>(rows.g);
+    k_mu_apply_m<<<rows.total(), ROW_THREADS, 0, st>>>(rows.g);
+    for (int t = 0; t < maxnb; ++t) {
+        cudaError_t e = prec == SODAGPU_FP64   ? multi_step_mode<SODAGPU_FP64>(P, t, st)
+                        : prec == SODAGPU_FP32 ? multi_step_mode<SODAGPU_FP32>(P, t, st)
+                                               : multi_step_mode<SODAGPU_FP8>(P, t, st);
+        if (e != cudaSuccess) return e;
+    }
+    GridBuilder skp(P.ddev, nj), stats(P.ddev, nj), hyp(P.ddev, nj), post(P.ddev, nj), rp(P.ddev, nj),
+        ra(P.ddev, nj);
+    size_t ssm = 0;
+    for (int j = 0; j < nj; ++j) {
+        const Dev &D = P.hdev[j];
+        const int C = D.chains;
+        skp.set(j, D.nskipped > 0 ? C : 0, 1, 1);
+        if (D.nskipped > 0 && (size_t)D.n * sizeof(double) <= (size_t)SS_SMEM_MAX)
+            ssm = std::max(ssm, (size_t)D.n * sizeof(double));
+        stats.set(j, NSTAT + D.nr_ctas, C, 1);
+        hyp.set(j, C, 1, 1);
+        const int pgrid = (D.p + 255) / 256 < 4 * sm_count ? (D.p + 255) / 256 : 4 * sm_count;
+        post.set(j, pgrid > 0 ? pgrid : 1, C, 1);
+        rp.set(j, (D.n + 255) / 256, RECAL_SPLIT, C);
+        ra.set(j, (D.n + 255) / 256, C, 1);
+    }
+    if (skp.total() > 0) k_skipped_m<<<skp.total(), SS_THREADS, ssm, st>>>(skp.g);
+    k_stats_m<<<stats.total(), 256, 0, st>>>(stats.g);
+    k_hyper_m<<<hyp.total(), 128, 0, st>>>(hyp.g);
+    k_post_m<<<post.total(), 256, 0, st>>>(post.g);
+    k_recal_partial_m<<<rp.total(), 256, 0, st>>>(rp.g);
+    k_recal_apply_m<<<ra.total(), 256, 0, st>>>(ra.g);
     return cudaGetLastError();
 }
 

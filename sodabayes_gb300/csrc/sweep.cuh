@@ -81,4 +81,21 @@ cudaError_t sweep_set_state(const Dev &D, int c, const double *g, const int32_t 
                             int included, cudaStream_t st);
 cudaError_t sweep_enqueue_recal(const Dev &D, double unused, cudaStream_t st);
 
+// Several jobs per launch (CUDA-core kernels; the jobs share precision and
+// chain count).  hdev / ddev: the jobs' descriptors on the host and in device
+// memory; blk_sizes[j]: job j's subset sizes; ksplit[j]: the K splits of its
+// rhs tiles.  Step t of an iteration runs subset t of every job that has one.
+struct BatchPlan {
+    int njobs;
+    const Dev *hdev;
+    const Dev *ddev;
+    const int *const *blk_sizes;
+    const int *ksplit;
+};
+cudaError_t sweep_multi_prepare(int precision, int chains, int max_bs);
+// K splits of the rhs of a subset of N SNPs so that its CTAs number about
+// cta_share (at least one per 128-SNP tile, at most the stages of ldx).
+int sweep_multi_rhs_split(int precision, int N, int chains, int ldx, int cta_share);
+cudaError_t sweep_enqueue_iteration_multi(const BatchPlan &P, int sm_count, cudaStream_t st);
+
 }  // namespace soda

@@ -31,7 +31,7 @@ static inline size_t update_smem_bytes_ct(int bs)
 }
 
 template <int MODE, int CT>
-__global__ void __launch_bounds__(32 * UpdWarps<MODE, CT>::v) k_update(Dev D, int b)
+__device__ __forceinline__ void update_body(const Dev &D, const VB &vb, int b)
 {
     typedef typename std::conditional<MODE == SODAGPU_FP64, double, float>::type acc_t;
     constexpr int NW = UpdWarps<MODE, CT>::v;
@@ -74,8 +74,8 @@ __global__ void __launch_bounds__(32 * UpdWarps<MODE, CT>::v) k_update(Dev D, in
     const int nlist = s_n;
     if (nlist == 0) return;   // nothing changed: r, r32 and rsum stay valid
     const int ntile_r = D.nr_ctas;
-    const bool rows = (int)blockIdx.x < ntile_r;
-    const int t0 = (rows ? blockIdx.x : blockIdx.x - ntile_r) * UT;
+    const bool rows = (int)vb.x < ntile_r;
+    const int t0 = (rows ? vb.x : vb.x - ntile_r) * UT;
     const int nrow = rows ? D.n : D.bs;
     const int i0 = t0 + lane * 4;
 
@@ -180,9 +180,16 @@ __global__ void __launch_bounds__(32 * UpdWarps<MODE, CT>::v) k_update(Dev D, in
         if (MODE == SODAGPU_FP8 && rows) {
             // refresh this tile's partial sum of r (the centring of the next subset)
             const double t = block_sum(v, sh);
-            if (tid == 0) D.rsum[(size_t)c * D.nr_ctas + blockIdx.x] = t;
+            if (tid == 0) D.rsum[(size_t)c * D.nr_ctas + vb.x] = t;
         }
     }
 }
+
+template <int MODE, int CT>
+__global__ void __launch_bounds__(32 * UpdWarps<MODE, CT>::v) k_update(Dev D, int b)
+{
+    update_body<MODE, CT>(D, vb_native(), b);
+}
+
 
 }  // namespace soda
