@@ -354,8 +354,10 @@ void sodagpu_batch_destroy(sodagpu_batch *batch);
  * Gram and Cholesky of its subsets (N_j = blocksize[j]).  model[] holds
  * {step_us, bw (bytes/s), e_x, e_u, gram_ops (int8 multiply-adds/s),
  * fp64_flops}; NULL takes values measured on GB300 for the FP8 mode
- * {30, 4e12, 1, 4, 5e13, 6e11}.  *steps receives S and *model_s the
- * modelled seconds of the choice. */
+ * {30, 2.6e12, 1, 4, 5e13, 6e11} (the bandwidth as measured on a batch of
+ * 32 BayesB analyses, n up to 20,000 and p up to 200,000: 90 GB per
+ * iteration in 35.6 ms).  *steps receives S and *model_s the modelled
+ * seconds of the choice. */
 int sodagpu_autotune_batch(int32_t njobs, const int32_t *n, const int32_t *p, int32_t iters,
                            int32_t max_blocksize, const double *model, int32_t *blocksize, int32_t *steps,
                            double *model_s);

@@ -1491,7 +1491,7 @@ int sodagpu_autotune_batch(int32_t njobs, const int32_t *n, const int32_t *p, in
     if (!n || !p || !blocksize) return fail(SODAGPU_E_ARG, "null argument");
     if (njobs < 1 || njobs > SODAGPU_MAXJOBS) return fail(SODAGPU_E_ARG, "njobs %d outside 1..%d", njobs, SODAGPU_MAXJOBS);
     if (iters < 1 || max_blocksize < 2) return fail(SODAGPU_E_ARG, "iters < 1 or max_blocksize < 2");
-    static const double dflt[6] = {30.0, 4e12, 1.0, 4.0, 5e13, 6e11};
+    static const double dflt[6] = {30.0, 2.6e12, 1.0, 4.0, 5e13, 6e11};
     const double *m = model ? model : dflt;
     for (int q = 0; q < 6; ++q)
         if (!(m[q] > 0.0)) return fail(SODAGPU_E_ARG, "model[%d] must be positive", q);

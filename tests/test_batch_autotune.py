@@ -11,7 +11,7 @@ import pytest
 
 from sodabayes_gb300 import SodaGpuError, autotune_batch
 
-MODEL = (30.0, 4e12, 1.0, 4.0, 5e13, 6e11)
+MODEL = (30.0, 2.6e12, 1.0, 4.0, 5e13, 6e11)
 
 
 def _cost(n, p, iters, cap, S, m=MODEL):
