@@ -535,19 +535,41 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             }
         } else if (warp == TV_WARP_MMA) {
             if (lane == 0) {
+                // The loop keeps the tensor pipe fed only if it does little between MMA issues (the
+                // pipe queues about one unit ahead): the descriptors are built once per slot and
+                // advanced by constants, and a row unit is decoded from registers.  Descriptor
+                // start addresses are 16-byte units in bits 0-13; every address here is below 256 KB,
+                // so the additions never carry out of that field.
                 const uint32_t idesc = tc::idesc_bf16_bmn(TV_M, TV_N);
                 const int nrow = max(0, min(u_end, P.R) - u_begin);
+                const int pnq = P.nq, pR = P.R;
+                const uint64_t ad0 = tc::desc_sw128(tc::smem_u32(raw0), 1024);
+                const uint64_t brow0 = tc::desc_sw128_mn(tc::smem_u32(bop0), 1024, 4096);   // codes operand
+                const uint64_t bra0 = tc::desc_sw128_mn(tc::smem_u32(bop0), 8192, 1024);    // U operand
                 int hint = 0, seg = -1, pkind = -1, ptile = -1;
+                int rtile = u_begin / pnq, rq = u_begin - rtile * pnq;   // the next row unit
                 bool ok = true;
                 for (int s = 0; s < nu && ok; ++s) {
                     const int sl = s % TV_NS;
-                    const Unit x = decode_unit(P, u_begin + s, hint);
-                    const bool first = x.kind != pkind || x.tile != ptile;
+                    int kind, tile;
+                    if (u_begin + s < pR) {
+                        kind = 0;
+                        tile = rtile;
+                        if (++rq == pnq) {
+                            rq = 0;
+                            ++rtile;
+                        }
+                    } else {
+                        const Unit x = decode_unit(P, u_begin + s, hint);
+                        kind = 1;
+                        tile = x.tile;
+                    }
+                    const bool first = kind != pkind || tile != ptile;
                     if (first) {
                         if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
                         ++seg;
-                        pkind = x.kind;
-                        ptile = x.tile;
+                        pkind = kind;
+                        ptile = tile;
                         // this accumulator was last used by segment seg - 2
                         if (seg >= 2) ok = tc::mbar_wait(&s_dfree[seg & 1], ((seg - 2) >> 1) & 1);
                         if (!ok) s_err = 17;
@@ -564,17 +586,16 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     }
                     if (!ok) break;
                     tc::fence_after_sync();
-                    const uint32_t a0 = tc::smem_u32(raw0 + (size_t)sl * T::ASTRIDE);
-                    const uint32_t b0 = tc::smem_u32(bop0 + (size_t)sl * T::BOP);
+                    const uint64_t ad = ad0 + (uint64_t)((sl * T::ASTRIDE) >> 4);
+                    const uint64_t bd = (kind == 0 ? brow0 : bra0) + (uint64_t)((sl * T::BOP) >> 4);
                     const uint32_t dt = tm + 256 * (seg & 1);
+                    // codes operand: K groups of four atoms (4096 bytes), atoms 1024 apart; U operand:
+                    // atoms of eight K groups (8192 bytes), K groups 1024 apart
+                    const uint32_t bstep = kind == 0 ? (8192 >> 4) : (2048 >> 4);
 #pragma unroll
-                    for (int kk = 0; kk < TV_K / 16; ++kk) {
-                        // codes operand: K groups of four atoms (4096 bytes), atoms 1024 apart;
-                        // U operand: atoms of eight K groups (8192 bytes), K groups 1024 apart
-                        const uint64_t bd = x.kind == 0 ? tc::desc_sw128_mn(b0 + kk * 8192, 1024, 4096)
-                                                        : tc::desc_sw128_mn(b0 + kk * 2048, 8192, 1024);
-                        tc::mma_bf16(dt, tc::desc_sw128(a0 + kk * 32, 1024), bd, idesc, (first && kk == 0) ? 0u : 1u);
-                    }
+                    for (int kk = 0; kk < TV_K / 16; ++kk)
+                        tc::mma_bf16(dt, ad + (uint64_t)(kk * (32 >> 4)), bd + (uint64_t)(kk * bstep), idesc,
+                                     (first && kk == 0) ? 0u : 1u);
                     tc::mma_commit(&s_free[sl]);
                 }
                 if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
