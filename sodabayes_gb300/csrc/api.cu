@@ -165,7 +165,8 @@ struct sodagpu_ctx {
     int32_t *rtab = nullptr;
     std::vector<int32_t> h_qoff;         // first code block of each subset (tiled codes)
     int32_t *qoff = nullptr;
-    uint8_t *Gt = nullptr;               // packed codes: [blocks][TC_PACKED_BLOCK]
+    uint8_t *Gt = nullptr;               // packed codes: [blocks][TC_PACKED_BLOCK], position-major (rhs)
+    uint8_t *Gu = nullptr;               // the same blocks individual-major (residual update)
     long long ncblk = 0;
     sodagpu_trace_row *trace = nullptr;
     int trace_cap = 0;
@@ -827,6 +828,7 @@ int build_dev(sodagpu_ctx *c)
     D.vpart = c->vpart;
     D.ugrid = c->ugrid;
     D.gpk = c->Gt;
+    D.gpu = c->Gu;
     D.nvt = sweep_tc_update_tiles(c->n);
     D.rtab = c->rtab;
     D.qoff = c->qoff;
@@ -921,6 +923,7 @@ int sodagpu_init_chains(sodagpu_ctx *c)
             TRY(c->alloc(&c->qoff, c->h_qoff.size(), false));
             CUDA_TRY(cudaMemcpyAsync(c->qoff, c->h_qoff.data(), c->h_qoff.size() * 4, cudaMemcpyHostToDevice, c->st));
             TRY(c->alloc(&c->Gt, (size_t)c->ncblk * TC_PACKED_BLOCK, false));
+            TRY(c->alloc(&c->Gu, (size_t)c->ncblk * TC_PACKED_BLOCK, false));
         }
     }
     build_dev(c);
@@ -943,7 +946,7 @@ int sodagpu_init_chains(sodagpu_ctx *c)
         if (r != CUDA_SUCCESS) return fail(SODAGPU_E_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
         if (!c->usp_ready) {
             CUDA_TRY(sweep_tc_prepare(c->G, c->D, c->st));
-            CUDA_TRY(sweep_tc_tile_codes(c->G, c->D, c->Gt, c->ncblk, c->sm_count, c->st));
+            CUDA_TRY(sweep_tc_tile_codes(c->G, c->D, c->Gt, c->Gu, c->ncblk, c->sm_count, c->st));
             c->usp_ready = true;
         }
     }

@@ -116,7 +116,8 @@ struct Dev {
     double *k0part;            // [draw CTAs][C] per-CTA sums of x0_j delta_j
     float *vpart;              // [tiles + update CTAs][C][256] update partial sums, one slot per segment
     unsigned long long *ugrid; // grid-barrier counter of the update (each launch adds its CTA count)
-    const uint8_t *gpk;        // 2-bit packed code blocks (see TC_PACKED_BLOCK)
+    const uint8_t *gpk;        // 2-bit packed code blocks, position-major (the rhs; see TC_PACKED_BLOCK)
+    const uint8_t *gpu;        // the same codes individual-major (the residual update)
     int nvt;                   // row tiles of 256 individuals of the update
     const int32_t *qoff;       // [nb+1] first 128-position code block of each subset (tiled codes)
     const int32_t *rtab;       // [nb][tstride] first rhs CTA of each 128-SNP tile, then the total

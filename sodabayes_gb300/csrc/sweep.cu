@@ -1306,13 +1306,47 @@ __global__ void __launch_bounds__(256) k_tile_codes(const int8_t *G, Dev D, uint
     }
 }
 
-cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, uint8_t *Gt, long long nblocks, int sm_count,
-                                cudaStream_t st)
+// The individual-major copy: one thread per (block, stage, individual) writes
+// that individual's 16 bytes, reading its 64 codes of the stage one position
+// (column of G) at a time; a warp's 32 individuals read 32 consecutive bytes
+// of each column.
+__global__ void __launch_bounds__(256) k_tile_codes_ind(const int8_t *G, Dev D, uint8_t *Gu, long long nblocks)
+{
+    constexpr int WORDS = TC_PACKED_BLOCK / 16;   // 2 stages x 256 individuals
+    const long long total = nblocks * WORDS;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long blk = idx / WORDS;
+        const int wi = (int)(idx - blk * WORDS), st = wi / TV_N, il = wi - st * TV_N;
+        const int q2 = (int)(blk / D.nvt), t = (int)(blk - (long long)q2 * D.nvt);
+        int lo = 0, hi = D.nb - 1;   // the subset: last b with qoff[b] <= q2
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (D.qoff[mid] <= q2) lo = mid;
+            else hi = mid - 1;
+        }
+        const int ls = D.blk_ls[lo], N = D.blk_ls[lo + 1] - ls, r0 = (q2 - D.qoff[lo]) * TC_TM + st * TV_K;
+        const int i = t * TV_N + il;
+        uint32_t out[4] = {0u, 0u, 0u, 0u};
+        if (i < D.n) {
+            for (int k = 0; k < TV_K && r0 + k < N; ++k) {
+                const uint32_t c = (uint32_t)G[(size_t)(ls + r0 + k) * D.ldx + i] & 3u;
+                out[k >> 4] |= c << (8 * (k & 3) + 2 * ((k >> 2) & 3));
+            }
+        }
+        *reinterpret_cast<uint4 *>(Gu + blk * TC_PACKED_BLOCK + (size_t)wi * 16) =
+            make_uint4(out[0], out[1], out[2], out[3]);
+    }
+}
+
+cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, uint8_t *Gt, uint8_t *Gu, long long nblocks,
+                                int sm_count, cudaStream_t st)
 {
     if (!Gt || !D.qoff || nblocks <= 0) return cudaErrorInvalidValue;
     const long long words = nblocks * (TC_PACKED_BLOCK / 16);
     const long long grid = std::min<long long>((words + 255) / 256, 16LL * sm_count);
     k_tile_codes<<<(unsigned)grid, 256, 0, st>>>(G, D, Gt, nblocks);
+    if (Gu) k_tile_codes_ind<<<(unsigned)grid, 256, 0, st>>>(G, D, Gu, nblocks);
     return cudaGetLastError();
 }
 

@@ -40,10 +40,15 @@ cudaError_t sweep_tc_prepare(int8_t *G, const Dev &D, cudaStream_t st);
 // sweep_tc_code_blocks fills qoff[0..nb] and returns the block rows;
 // sweep_tc_tile_codes writes all nblocks = rows * D.nvt blocks from G (after
 // sweep_tc_prepare, on the same stream).
+// The update reads a second copy, individual-major: block (q2, t) holds
+// [2 stages of 64 positions][256 individuals][16 bytes], and in word w of an
+// individual's 16 bytes the code of position 16 w + 4 b + j of the stage sits
+// at bits 8 j + 2 b (one 16-byte load per individual and update unit).
+// sweep_tc_tile_codes writes both copies (Gu may be null).
 constexpr int TC_PACKED_BLOCK = 4 * 128 * 16;   // bytes of one packed code block
 int sweep_tc_code_blocks(const int *blk_sizes, int nb, int32_t *qoff);
-cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, uint8_t *Gt, long long nblocks, int sm_count,
-                                cudaStream_t st);
+cudaError_t sweep_tc_tile_codes(const int8_t *G, const Dev &D, uint8_t *Gt, uint8_t *Gu, long long nblocks,
+                                int sm_count, cudaStream_t st);
 // Optional per-launch event recording (eager profiling, never inside a graph):
 // before/after every launch an event pair is recorded and its kernel class
 // stored.  Classes: 0 rhs, 1 residual update, 2 mu, 3 everything else, 4 draws.

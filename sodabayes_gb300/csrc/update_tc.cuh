@@ -5,21 +5,24 @@
 //   r  += X_b delta = sum_j x0_j delta_j + G_b (delta / sd)
 //   ra += U_b delta = (U_b sd) (delta / sd)
 //
-// Both products run on tcgen05 as transposed products D = S B' with
-//   S (operand A, K-major, TMA) = the bf16 hi/mid/lo split of delta/sd written
-//     by the draws (delta itself for columns with sd = 0, whose codes are
-//     zero): rows term * chains + c (3 * chains of the M = 64 rows are
-//     used), K = subset positions, 64 per stage;
-//   B (N = 256) = for r, the genotype codes of 256 individuals: the
-//     converter warps load them 2-bit packed (4 KB per unit) straight from
-//     global memory into registers, several units ahead, and widen them to a
-//     bf16 MN-major operand (individuals contiguous); for ra, one bf16 term of
-//     sd * U (256 rows of U), loaded by TMA straight into an MN-major operand
-//     (the factor is stored column by column);
-//   D = 64 x 256 FP32 in tensor memory (rows 16q .. in lanes 32q ..),
-//     double-buffered.
-// A tcgen05.mma costs about the same for any N up to 256, so the codes sit on
-// the N = 256 side: one instruction consumes 4 KB of codes.
+// Both products run on tcgen05 as D (M = 128 individuals or rows of U, N =
+// the 3 * chains rows of the delta split) = A B':
+//   A for r = the genotype codes of 128 individuals x 16 subset positions per
+//     MMA, in tensor memory: the converter warps load them 2-bit packed
+//     (individual-major, 16 bytes per individual and 64-position stage)
+//     straight from global memory into registers, several units ahead, widen
+//     them to bf16 and store them with tcgen05.st (lane = individual), so the
+//     codes never pass through shared memory;
+//   A for ra = one bf16 term of sd * U (128 rows of U), loaded by TMA into an
+//     MN-major shared-memory operand (the factor is stored column by column);
+//   B (K-major, TMA) = the bf16 hi/mid/lo split of delta/sd written by the
+//     draws (delta itself for columns with sd = 0, whose codes are zero):
+//     rows term * chains + c, K = subset positions, 64 per stage;
+//   D = 128 x 3C FP32 in tensor memory (lane = individual, column = term and
+//     chain), two per unit (256 individuals), double-buffered by segment.
+// Measured on GB300: an N = 48 MMA costs 44 cycles against 128 for an N = 256
+// one, and a 32 KB widened operand costs about as many cycles to store in
+// shared memory as the MMAs that read it; in tensor memory both costs drop.
 //
 // Work units: (row tile of 256 individuals, stage of 64 positions) and, for
 // ra, (tile of 256 rows of U, stage, U term); an upper-triangular factor meets
@@ -43,11 +46,11 @@
 // then take part in the reductions.  A CTA's row units come before its ra
 // units.  Unit s uses slot s % TV_NS of both operands, and one commit of its
 // MMAs frees both:
-//   producer: wait free (MMAs of s - TV_NS); load A (+ tx) on fulla; for an
-//     ra unit also load B (+ tx) on fullb;
-//   converters (row units only): wait free; write B from the codes; arrive
-//     on conv;
-//   MMA: wait conv (row unit) or fullb (ra unit), and fulla; 4 MMAs; commit
+//   producer: wait free (MMAs of s - TV_NS); load the delta tile (+ tx) on
+//     fulla; for an ra unit also load the U tile (+ tx) on fullb;
+//   converters (row units only): wait free; write the codes into the slot's
+//     tensor-memory operand; arrive on conv;
+//   MMA: wait conv (row unit) or fullb (ra unit), and fulla; 8 MMAs; commit
 //     to free.
 // Every wait is at most one phase behind its barrier, so the parity waits are
 // exact (checked by a CPU model of this protocol in the tests).
@@ -55,10 +58,9 @@
 
 namespace soda {
 
-constexpr int TV_N = 256;          // individuals per row tile / rows of U per ra tile (MMA N)
+constexpr int TV_N = 256;          // individuals per row tile / rows of U per ra tile (two MMA M halves)
 constexpr int TV_K = 64;           // subset positions per stage
-constexpr int TV_M = 64;           // MMA M (the 3 * chains <= 48 rows of the delta split)
-constexpr int TV_NS = 4;           // operand slots: delta-split tile (A) and B operand
+constexpr int TV_NS = 4;           // operand slots: delta-split tile, and the codes or the U tile
 constexpr int TV_PF = 4;           // packed code words each converter thread holds in flight
 constexpr int TV_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
 constexpr int TV_MAXRA = 64;       // ra tiles per subset
@@ -71,21 +73,20 @@ constexpr int TV_WARP_TMA = 8, TV_WARP_MMA = 9, TV_WARP_EPI = 10;
 
 template <int CT>
 struct UpdTc {
-    static constexpr int NB = RhsTc<CT>::NB;
-    static constexpr int ROWS = 3 * CT;                // accumulator rows in use
+    static constexpr int NB = RhsTc<CT>::NB;           // MMA N: 3 * chains rounded up to 16
+    static constexpr int ROWS = 3 * CT;                // delta-split rows in use
     static constexpr int RAW_A = NB * TV_K * 2;        // delta split tile: NB rows x 64 bf16, 128-byte swizzle
-    // an M = 64 MMA reads 64 rows (8 KB) from A's start: each A slot owns 8 KB, so that no byte
-    // the MMA reads is the target of a TMA load in flight (rows past NB are never written)
-    static constexpr int ASTRIDE = TV_M * 128;
+    static constexpr int ASTRIDE = RAW_A;              // the MMAs read exactly the NB rows the TMA writes
     static constexpr int AREG = TV_NS * ASTRIDE;
-    static constexpr int BOP = TV_K * TV_N * 2;        // B operand: 64 x 256 bf16
+    static constexpr int BOP = TV_K * TV_N * 2;        // U tile of an ra unit: 256 rows x 64 bf16
     static constexpr int BOP0 = AREG;
-    // epilogue staging: the accumulator rows in use, all 256 columns (row stride 257 floats)
-    static constexpr int STG0 = BOP0 + TV_NS * BOP;
-    static constexpr int STG = ((ROWS * (TV_N + 1) * 4 + 1023) / 1024) * 1024;
-    static constexpr size_t SMEM = 1024 + (size_t)STG0 + (size_t)STG;
+    static constexpr size_t SMEM = 1024 + (size_t)AREG + (size_t)TV_NS * BOP;
+    // tensor memory: accumulators (segment parity p, half h) at columns NB (2p + h), the codes
+    // operands (slot sl, half h) at 256 + 64 sl + 32 h (32 columns: 64 positions, two bf16 each)
+    static constexpr int TM_ACC = NB;
+    static constexpr int TM_OPS = 256;
     static_assert(RAW_A % 1024 == 0 && AREG % 1024 == 0 && BOP % 1024 == 0, "buffer alignment");
-    static_assert(NB <= TV_M, "delta split rows exceed the MMA's M");
+    static_assert(4 * NB <= TM_OPS && TM_OPS + 64 * TV_NS <= 512, "tensor memory");
     static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 
@@ -362,15 +363,13 @@ __device__ __forceinline__ bool update_grid_sync(unsigned long long *ctr, unsign
     return s_ok != 0;
 }
 
-// Packed code word of a converter thread for row unit u: positions of stage q
-// of row tile `tile`; the thread takes position k = tid % 64 and individuals
-// 64 j .. 64 j + 63, j = tid / 64, of the tile (16 bytes: 64 codes of 2 bits).
-__device__ __forceinline__ uint4 update_code_word(const Dev &D, const UnitPlan &P, int cblk, int u, int tid)
+// Packed code word of a converter thread for row unit (tile, q): individual i
+// (0..255) of row tile `tile`, the 64 positions of stage q (16 bytes: 64 codes
+// of 2 bits; the individual-major copy, D.gpu).
+__device__ __forceinline__ uint4 update_code_word(const Dev &D, int nvt, int cblk, int tile, int q, int i)
 {
-    const int tile = u / P.nq, q = u - tile * P.nq;
-    const int k = tid & 63, j = tid >> 6;
-    const size_t blk = (size_t)(cblk + (q >> 1)) * P.nvt + tile;
-    const uint4 *w = reinterpret_cast<const uint4 *>(D.gpk + blk * TC_PACKED_BLOCK) + j * TC_TM + 64 * (q & 1) + k;
+    const size_t blk = (size_t)(cblk + (q >> 1)) * nvt + tile;
+    const uint4 *w = reinterpret_cast<const uint4 *>(D.gpu + blk * TC_PACKED_BLOCK) + (q & 1) * TV_N + i;
     uint4 v;
     asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
@@ -378,15 +377,17 @@ __device__ __forceinline__ uint4 update_code_word(const Dev &D, const UnitPlan &
     return v;
 }
 
-// Widens one 32-bit word of 16 packed codes (individuals 4b + j at bits
-// 8j + 2b) into the bf16 of two 16-byte operand chunks (individuals 0-7, 8-15).
-__device__ __forceinline__ void unpack16(uint32_t w, uint4 &lo, uint4 &hi)
+// Widens 64 packed codes (positions 16 w + 4 b + j at bits 8 j + 2 b of word
+// w) into the 32 tensor-memory columns of an A operand row: column c holds
+// the bf16 of positions 2c (low half) and 2c + 1.
+__device__ __forceinline__ void unpack64(const uint4 &v, uint32_t (&o)[32])
 {
-    uint32_t o[8];
+    const uint32_t ww[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int b = 0; b < 4; ++b) tc::codes_to_bf16x4((w >> (2 * b)) & 0x03030303u, o[2 * b], o[2 * b + 1]);
-    lo = make_uint4(o[0], o[1], o[2], o[3]);
-    hi = make_uint4(o[4], o[5], o[6], o[7]);
+    for (int w = 0; w < 4; ++w)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            tc::codes_to_bf16x4((ww[w] >> (2 * b)) & 0x03030303u, o[8 * w + 2 * b], o[8 * w + 2 * b + 1]);
 }
 
 template <int CT>
@@ -471,7 +472,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             }
             tc::mbar_fence_init();
         }
-        if (warp == TV_WARP_MMA) tc::tmem_alloc(&s_tmem, 512);   // two accumulators of 256 columns
+        if (warp == TV_WARP_MMA) tc::tmem_alloc(&s_tmem, 512);   // accumulators and codes operands
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
@@ -540,12 +541,12 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 // advanced by constants, and a row unit is decoded from registers.  Descriptor
                 // start addresses are 16-byte units in bits 0-13; every address here is below 256 KB,
                 // so the additions never carry out of that field.
-                const uint32_t idesc = tc::idesc_bf16_bmn(TV_M, TV_N);
+                const uint32_t id_row = tc::idesc_bf16(128, T::NB);               // A in tensor memory
+                const uint32_t id_ra = tc::idesc_bf16(128, T::NB) | (1u << 15);   // A MN-major in smem
                 const int nrow = max(0, min(u_end, P.R) - u_begin);
                 const int pnq = P.nq, pR = P.R;
-                const uint64_t ad0 = tc::desc_sw128(tc::smem_u32(raw0), 1024);
-                const uint64_t brow0 = tc::desc_sw128_mn(tc::smem_u32(bop0), 1024, 4096);   // codes operand
-                const uint64_t bra0 = tc::desc_sw128_mn(tc::smem_u32(bop0), 8192, 1024);    // U operand
+                const uint64_t bd0 = tc::desc_sw128(tc::smem_u32(raw0), 1024);          // delta split (B)
+                const uint64_t ud0 = tc::desc_sw128_mn(tc::smem_u32(bop0), 8192, 1024);  // U tile (A)
                 int hint = 0, seg = -1, pkind = -1, ptile = -1;
                 int rtile = u_begin / pnq, rq = u_begin - rtile * pnq;   // the next row unit
                 bool ok = true;
@@ -570,12 +571,12 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         ++seg;
                         pkind = kind;
                         ptile = tile;
-                        // this accumulator was last used by segment seg - 2
+                        // these accumulators were last used by segment seg - 2
                         if (seg >= 2) ok = tc::mbar_wait(&s_dfree[seg & 1], ((seg - 2) >> 1) & 1);
                         if (!ok) s_err = 17;
                     }
                     if (ok) {
-                        // B: widened codes of a row unit, or the U tile of an ra unit
+                        // A: widened codes of a row unit, or the U tile of an ra unit
                         ok = s < nrow ? tc::mbar_wait(&s_conv[sl], (s / TV_NS) & 1)
                                       : tc::mbar_wait(&s_fullb[sl], ra_phase(s, nrow) & 1);
                         if (!ok) s_err = 12;
@@ -586,16 +587,27 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     }
                     if (!ok) break;
                     tc::fence_after_sync();
-                    const uint64_t ad = ad0 + (uint64_t)((sl * T::ASTRIDE) >> 4);
-                    const uint64_t bd = (kind == 0 ? brow0 : bra0) + (uint64_t)((sl * T::BOP) >> 4);
-                    const uint32_t dt = tm + 256 * (seg & 1);
-                    // codes operand: K groups of four atoms (4096 bytes), atoms 1024 apart; U operand:
-                    // atoms of eight K groups (8192 bytes), K groups 1024 apart
-                    const uint32_t bstep = kind == 0 ? (8192 >> 4) : (2048 >> 4);
+                    const uint64_t bd = bd0 + (uint64_t)((sl * T::ASTRIDE) >> 4);
+                    const uint32_t acc = tm + T::TM_ACC * 2 * (seg & 1);
 #pragma unroll
-                    for (int kk = 0; kk < TV_K / 16; ++kk)
-                        tc::mma_bf16(dt, ad + (uint64_t)(kk * (32 >> 4)), bd + (uint64_t)(kk * bstep), idesc,
-                                     (first && kk == 0) ? 0u : 1u);
+                    for (int h = 0; h < 2; ++h) {
+                        const uint32_t dt = acc + T::TM_ACC * h;
+                        if (kind == 0) {
+                            // codes of individuals 128 h ..: 8 columns (16 positions) per MMA
+                            const uint32_t ta = tm + T::TM_OPS + 64 * sl + 32 * h;
+#pragma unroll
+                            for (int kk = 0; kk < TV_K / 16; ++kk)
+                                tc::mma_bf16_ta(dt, ta + 8 * kk, bd + (uint64_t)(kk * (32 >> 4)), id_row,
+                                                (first && kk == 0) ? 0u : 1u);
+                        } else {
+                            // rows 128 h .. of the U tile: two 64-row atoms (8 KB each), K groups 1 KB apart
+                            const uint64_t ad = ud0 + (uint64_t)((sl * T::BOP + h * 16384) >> 4);
+#pragma unroll
+                            for (int kk = 0; kk < TV_K / 16; ++kk)
+                                tc::mma_bf16(dt, ad + (uint64_t)(kk * (2048 >> 4)), bd + (uint64_t)(kk * (32 >> 4)),
+                                             id_ra, (first && kk == 0) ? 0u : 1u);
+                        }
+                    }
                     tc::mma_commit(&s_free[sl]);
                 }
                 if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
@@ -604,15 +616,24 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             // converters.  Row units come first in the unit order, so this CTA's row units are
             // u_begin .. min(u_end, R) - 1; the thread keeps the packed words of the next TV_PF of
             // them in registers (the codes are not written by any kernel of the sweep, so the first
-            // ones are loaded while the draws still run).  Thread tid writes position k = tid % 64
-            // (K group k / 8, row k % 8) of atom j = tid / 64 (individuals 64 j ..): eight 16-byte
-            // chunks, chunk cc at (cc ^ row) in the 128-byte swizzled row.
+            // ones are loaded while the draws still run).  Warp w writes tensor-memory lanes
+            // 32 (w % 4) .. of half h = w / 4: the thread's individual is 128 h + 32 (w % 4) + lane.
             const int nrow = max(0, min(u_end, P.R) - u_begin);
+            const int pnq = P.nq, pnvt = P.nvt;
+            const int ind = 128 * (warp >> 2) + 32 * (warp & 3) + lane;
+            int ftile = u_begin / pnq, fq = u_begin - ftile * pnq;   // the next unit to load
+            auto next_word = [&]() -> uint4 {
+                const uint4 v = update_code_word(D, pnvt, cblk, ftile, fq, ind);
+                if (++fq == pnq) {
+                    fq = 0;
+                    ++ftile;
+                }
+                return v;
+            };
             uint4 pf[TV_PF];
 #pragma unroll
-            for (int i = 0; i < TV_PF; ++i)
-                pf[i] = i < nrow ? update_code_word(D, P, cblk, u_begin + i, tid) : make_uint4(0u, 0u, 0u, 0u);
-            const int k = tid & 63, j = tid >> 6, row = k & 7;
+            for (int i = 0; i < TV_PF; ++i) pf[i] = i < nrow ? next_word() : make_uint4(0u, 0u, 0u, 0u);
+            const uint32_t tl = tm + ((uint32_t)(32 * (warp & 3)) << 16) + T::TM_OPS + 32 * (warp >> 2);
             // unit s uses pf[s % TV_PF] and reloads it for unit s + TV_PF: the loop is unrolled by
             // TV_PF so that every slot stays in its own registers (a shift of the slots would wait
             // for each load one unit after issuing it)
@@ -623,7 +644,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     const int s = s0 + i;
                     if (s >= nrow || stop) break;
                     const int ob = s % TV_NS;
-                    // the B operand was last read by the MMAs of unit s - TV_NS
+                    // the operand was last read by the MMAs of unit s - TV_NS
                     bool ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);
                     ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
                     if (!ok) {
@@ -631,33 +652,32 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         stop = true;
                         break;
                     }
-                    {
-                        const uint4 w = pf[i];
-                        pf[i] = s + TV_PF < nrow ? update_code_word(D, P, cblk, u_begin + s + TV_PF, tid)
-                                                 : make_uint4(0u, 0u, 0u, 0u);
-                        unsigned char *orow = bop0 + (size_t)ob * T::BOP + (k >> 3) * 4096 + j * 1024 + row * 128;
-                        const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+                    tc::fence_after_sync();
+                    const uint4 w = pf[i];
+                    pf[i] = s + TV_PF < nrow ? next_word() : make_uint4(0u, 0u, 0u, 0u);
+                    uint32_t o[32];
+                    unpack64(w, o);
+                    uint32_t lo[16], hi[16];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            uint4 c0, c1;
-                            unpack16(ww[q], c0, c1);
-                            *reinterpret_cast<uint4 *>(orow + (((2 * q) ^ row) << 4)) = c0;
-                            *reinterpret_cast<uint4 *>(orow + (((2 * q + 1) ^ row) << 4)) = c1;
-                        }
-                        tc::fence_async_smem();
+                    for (int e = 0; e < 16; ++e) {
+                        lo[e] = o[e];
+                        hi[e] = o[16 + e];
                     }
+                    tc::tmem_st16(tl + 64 * ob, lo);
+                    tc::tmem_st16(tl + 64 * ob + 16, hi);
+                    tc::tmem_wait_st();
+                    tc::fence_before_sync();
                     __syncwarp();
                     if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
                 }
             }
         } else {
-            // epilogue: per finished segment, warp w reads tensor-memory lanes 32(w%4) .. for all 256
-            // columns (an M = 64 accumulator keeps rows 16q .. 16q+15 in lanes 32q .. 32q+15) and
-            // stores hi + mid + lo per chain to the segment's slot of vpart
+            // epilogue: per finished segment, warp w reads tensor-memory lanes 32 (w % 4) .. (individuals
+            // or rows of U 128 h + 32 (w % 4) + lane) of both halves h, and stores hi + mid + lo per chain
+            // to the segment's slot of vpart
             tc::pdl_wait();   // the draws' centring sums; r of the previous update
             const int t = tid - 32 * TV_WARP_EPI;
-            const int qd = warp & 3, row = lane < 16 ? 16 * qd + lane : T::ROWS;
-            float *stg = reinterpret_cast<float *>(raw0 + T::STG0);
+            const int qd = warp & 3;
             update_k0<CT>(D, b, t, s_k0p, s_k0);
             int hint = 0, seg = -1, pkind = -1, ptile = -1;
             for (int s = 0; s <= nu; ++s) {
@@ -672,42 +692,32 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     if (!ok) s_err = 15;
                     tc::fence_after_sync();
                     const int tg = pkind == 0 ? ptile : P.nvt + ptile;
-                    // all 256 columns of the rows in use to the staging buffer (32 at a time), then
-                    // hi + mid + lo per chain to the slot in one coalesced pass
-                    float *dst = D.vpart + (size_t)(tg + blockIdx.x) * CT * TV_N;
-                    const uint32_t ta = tm + 256 * (seg & 1) + ((uint32_t)(32 * qd) << 16);
-                    if (ok && 16 * qd < T::ROWS) {
-#pragma unroll 1
-                        for (int jj = 0; jj < TV_N / 32; ++jj) {
-                            float v0[8], v1[8], v2[8], v3[8];
-                            tc::tmem_ld8(ta + 32 * jj, v0);
-                            tc::tmem_ld8(ta + 32 * jj + 8, v1);
-                            tc::tmem_ld8(ta + 32 * jj + 16, v2);
-                            tc::tmem_ld8(ta + 32 * jj + 24, v3);
-                            tc::tmem_wait_ld();
-                            if (row < T::ROWS) {
-                                float *sr = stg + row * (TV_N + 1) + 32 * jj;
+                    float *dst = D.vpart + (size_t)(tg + blockIdx.x) * CT * TV_N + 32 * qd + lane;
+                    const uint32_t ta = tm + ((uint32_t)(32 * qd) << 16) + T::TM_ACC * 2 * (seg & 1);
 #pragma unroll
-                                for (int e = 0; e < 8; ++e) {
-                                    sr[e] = v0[e];
-                                    sr[8 + e] = v1[e];
-                                    sr[16 + e] = v2[e];
-                                    sr[24 + e] = v3[e];
-                                }
+                    for (int h = 0; h < 2; ++h) {
+                        float v[T::NB];
+                        if (ok) {
+#pragma unroll
+                            for (int g = 0; g < T::NB / 8; ++g) {
+                                float u8[8];
+                                tc::tmem_ld8(ta + T::TM_ACC * h + 8 * g, u8);
+#pragma unroll
+                                for (int e = 0; e < 8; ++e) v[8 * g + e] = u8[e];
                             }
+                            tc::tmem_wait_ld();
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < T::NB; ++e) v[e] = 0.0f;
                         }
+#pragma unroll
+                        for (int c = 0; c < CT; ++c) dst[c * TV_N + 128 * h] = (v[c] + v[CT + c]) + v[2 * CT + c];
                     }
                     tc::fence_before_sync();
-                    asm volatile("bar.sync 1, 128;" ::: "memory");
-                    // the accumulator is free once every lane has read it
-                    if (t == 0) tc::mbar_arrive(&s_dfree[seg & 1]);
-                    for (int idx = t; idx < CT * TV_N; idx += 128) {
-                        const int cc = idx >> 8, col = idx & (TV_N - 1);
-                        dst[cc * TV_N + col] = (stg[cc * (TV_N + 1) + col] + stg[(CT + cc) * (TV_N + 1) + col]) +
-                                               stg[(2 * CT + cc) * (TV_N + 1) + col];
-                    }
                     __threadfence();   // the slot is read after the grid barrier
                     asm volatile("bar.sync 1, 128;" ::: "memory");
+                    // the accumulators are free once every lane has read them
+                    if (t == 0) tc::mbar_arrive(&s_dfree[seg & 1]);
                 }
                 if (s == nu) break;
                 ++seg;
