@@ -189,40 +189,49 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else if (warp == TC_WARP_MMA) {
         tc::pdl_wait();
         tc::pdl_trigger();
-        if (lane == 0 && ns > 0) {
+        // the whole warp runs the loop on warp-uniform values; one elected lane issues (its
+        // operands stay in uniform registers)
+        const bool leader = tc::elect_one();
+        if (ns > 0) {
             const uint32_t idesc = tc::idesc_bf16(TC_TM, NB);
             for (int s = 0; s < ns; ++s) {
                 const int buf = s % NS;
                 const uint32_t rb = tc::smem_u32(raw0 + (size_t)buf * T::RAW);
                 if (s < nck) {
                     const int ob = s % TC_NOB;
-                    if (!tc::mbar_wait(&s_conv[ob], (s / TC_NOB) & 1) || !tc::mbar_wait(&s_full[buf], (s / NS) & 1)) {
+                    bool ok = tc::mbar_wait(&s_conv[ob], (s / TC_NOB) & 1) && tc::mbar_wait(&s_full[buf], (s / NS) & 1);
+                    if (!__all_sync(0xffffffffu, ok)) {
                         s_err = 1;
                         break;
                     }
                     tc::fence_after_sync();
                     const uint32_t ta = tm + 64 + 64 * ob;
+                    if (leader) {
 #pragma unroll
-                    for (int kk = 0; kk < TC_KC / 16; ++kk) {
-                        const uint32_t kb = (kk >> 2) * (NB * 128) + (kk & 3) * 32;
-                        tc::mma_bf16_ta(tm, ta + 8 * kk, tc::desc_sw128(rb + T::RAW_A + kb, 1024), idesc,
-                                        (s | kk) != 0 ? 1u : 0u);
+                        for (int kk = 0; kk < TC_KC / 16; ++kk) {
+                            const uint32_t kb = (kk >> 2) * (NB * 128) + (kk & 3) * 32;
+                            tc::mma_bf16_ta(tm, ta + 8 * kk, tc::desc_sw128(rb + T::RAW_A + kb, 1024), idesc,
+                                            (s | kk) != 0 ? 1u : 0u);
+                        }
+                        tc::mma_commit(&s_opfree[ob]);
                     }
-                    tc::mma_commit(&s_opfree[ob]);
                 } else {
-                    if (!tc::mbar_wait(&s_full[buf], (s / NS) & 1)) {
+                    if (!__all_sync(0xffffffffu, tc::mbar_wait(&s_full[buf], (s / NS) & 1))) {
                         s_err = 1;
                         break;
                     }
                     tc::fence_after_sync();
+                    if (leader) {
 #pragma unroll
-                    for (int kk = 0; kk < TC_KU / 16; ++kk)
-                        tc::mma_bf16(tm, tc::desc_sw128(rb + kk * 32, 1024), tc::desc_sw128(rb + T::RAW_A + kk * 32, 1024),
-                                     idesc, (s | kk) != 0 ? 1u : 0u);
+                        for (int kk = 0; kk < TC_KU / 16; ++kk)
+                            tc::mma_bf16(tm, tc::desc_sw128(rb + kk * 32, 1024), tc::desc_sw128(rb + T::RAW_A + kk * 32, 1024),
+                                         idesc, (s | kk) != 0 ? 1u : 0u);
+                    }
                 }
-                tc::mma_commit(&s_empty[buf]);
+                if (leader) tc::mma_commit(&s_empty[buf]);
+                __syncwarp();
             }
-            tc::mma_commit(&s_done);
+            if (leader) tc::mma_commit(&s_done);
         }
     } else {
         // converters: thread (SNP m of the tile, individuals 32 s4 .. 32 s4 + 31 of each stage) loads

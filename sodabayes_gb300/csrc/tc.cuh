@@ -173,6 +173,21 @@ __device__ __forceinline__ void fence_after_sync()
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// True in one lane of the (fully active) warp.  Issue loops run on the whole
+// warp with warp-uniform values and issue from the elected lane: the operands
+// of its tensor-core instructions then stay in uniform registers instead of
+// being moved there one instruction at a time.
+__device__ __forceinline__ bool elect_one()
+{
+    uint32_t pred = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "elect.sync _|p, 0xffffffff;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(pred));
+    return pred != 0;
+}
+
 // Warp-wide: allocate ncols tensor-memory columns (power of two, >= 32); the
 // address is written to *slot.
 __device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols)

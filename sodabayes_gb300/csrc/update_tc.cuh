@@ -535,60 +535,65 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 }
             }
         } else if (warp == TV_WARP_MMA) {
-            if (lane == 0) {
-                // The loop keeps the tensor pipe fed only if it does little between MMA issues (the
-                // pipe queues about one unit ahead): the descriptors are built once per slot and
-                // advanced by constants, and a row unit is decoded from registers.  Descriptor
-                // start addresses are 16-byte units in bits 0-13; every address here is below 256 KB,
-                // so the additions never carry out of that field.
-                const uint32_t id_row = tc::idesc_bf16(128, T::NB);               // A in tensor memory
-                const uint32_t id_ra = tc::idesc_bf16(128, T::NB) | (1u << 15);   // A MN-major in smem
-                const int nrow = max(0, min(u_end, P.R) - u_begin);
-                const int pnq = P.nq, pR = P.R;
-                const uint64_t bd0 = tc::desc_sw128(tc::smem_u32(raw0), 1024);          // delta split (B)
-                const uint64_t ud0 = tc::desc_sw128_mn(tc::smem_u32(bop0), 8192, 1024);  // U tile (A)
-                int hint = 0, seg = -1, pkind = -1, ptile = -1;
-                int rtile = u_begin / pnq, rq = u_begin - rtile * pnq;   // the next row unit
-                bool ok = true;
-                for (int s = 0; s < nu && ok; ++s) {
-                    const int sl = s % TV_NS;
-                    int kind, tile;
-                    if (u_begin + s < pR) {
-                        kind = 0;
-                        tile = rtile;
-                        if (++rq == pnq) {
-                            rq = 0;
-                            ++rtile;
-                        }
-                    } else {
-                        const Unit x = decode_unit(P, u_begin + s, hint);
-                        kind = 1;
-                        tile = x.tile;
+            // The loop keeps the tensor pipe fed only if it does little between MMA issues (the pipe
+            // queues about one unit ahead): the whole warp runs it on warp-uniform values and one
+            // elected lane issues, the descriptors are built once per slot and advanced by constants,
+            // and a row unit is decoded from registers.  Descriptor start addresses are 16-byte units
+            // in bits 0-13; every address here is below 256 KB, so the additions never carry out of
+            // that field.
+            const bool leader = tc::elect_one();
+            const uint32_t id_row = tc::idesc_bf16(128, T::NB);               // A in tensor memory
+            const uint32_t id_ra = tc::idesc_bf16(128, T::NB) | (1u << 15);   // A MN-major in smem
+            const int nrow = max(0, min(u_end, P.R) - u_begin);
+            const int pnq = P.nq, pR = P.R;
+            const uint64_t bd0 = tc::desc_sw128(tc::smem_u32(raw0), 1024);          // delta split (B)
+            const uint64_t ud0 = tc::desc_sw128_mn(tc::smem_u32(bop0), 8192, 1024);  // U tile (A)
+            int hint = 0, seg = -1, pkind = -1, ptile = -1;
+            int rtile = u_begin / pnq, rq = u_begin - rtile * pnq;   // the next row unit
+            bool ok = true;
+            for (int s = 0; s < nu && ok; ++s) {
+                const int sl = s % TV_NS;
+                int kind, tile;
+                if (u_begin + s < pR) {
+                    kind = 0;
+                    tile = rtile;
+                    if (++rq == pnq) {
+                        rq = 0;
+                        ++rtile;
                     }
-                    const bool first = kind != pkind || tile != ptile;
-                    if (first) {
-                        if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
-                        ++seg;
-                        pkind = kind;
-                        ptile = tile;
-                        // these accumulators were last used by segment seg - 2
-                        if (seg >= 2) ok = tc::mbar_wait(&s_dfree[seg & 1], ((seg - 2) >> 1) & 1);
-                        if (!ok) s_err = 17;
-                    }
-                    if (ok) {
-                        // A: widened codes of a row unit, or the U tile of an ra unit
-                        ok = s < nrow ? tc::mbar_wait(&s_conv[sl], (s / TV_NS) & 1)
-                                      : tc::mbar_wait(&s_fullb[sl], ra_phase(s, nrow) & 1);
-                        if (!ok) s_err = 12;
-                    }
-                    if (ok) {
-                        ok = tc::mbar_wait(&s_fulla[sl], (s / TV_NS) & 1);
-                        if (!ok) s_err = 18;
-                    }
-                    if (!ok) break;
-                    tc::fence_after_sync();
-                    const uint64_t bd = bd0 + (uint64_t)((sl * T::ASTRIDE) >> 4);
-                    const uint32_t acc = tm + T::TM_ACC * 2 * (seg & 1);
+                } else {
+                    const Unit x = decode_unit(P, u_begin + s, hint);
+                    kind = 1;
+                    tile = x.tile;
+                }
+                const bool first = kind != pkind || tile != ptile;
+                if (first) {
+                    if (seg >= 0 && leader) tc::mma_commit(&s_segdone[seg & 1]);
+                    ++seg;
+                    pkind = kind;
+                    ptile = tile;
+                    // these accumulators were last used by segment seg - 2
+                    if (seg >= 2) ok = tc::mbar_wait(&s_dfree[seg & 1], ((seg - 2) >> 1) & 1);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (!ok) s_err = 17;
+                }
+                if (ok) {
+                    // A: widened codes of a row unit, or the U tile of an ra unit
+                    ok = s < nrow ? tc::mbar_wait(&s_conv[sl], (s / TV_NS) & 1)
+                                  : tc::mbar_wait(&s_fullb[sl], ra_phase(s, nrow) & 1);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (!ok) s_err = 12;
+                }
+                if (ok) {
+                    ok = tc::mbar_wait(&s_fulla[sl], (s / TV_NS) & 1);
+                    ok = __all_sync(0xffffffffu, ok);
+                    if (!ok) s_err = 18;
+                }
+                if (!ok) break;
+                tc::fence_after_sync();
+                const uint64_t bd = bd0 + (uint64_t)((sl * T::ASTRIDE) >> 4);
+                const uint32_t acc = tm + T::TM_ACC * 2 * (seg & 1);
+                if (leader) {
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
                         const uint32_t dt = acc + T::TM_ACC * h;
@@ -610,8 +615,9 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     }
                     tc::mma_commit(&s_free[sl]);
                 }
-                if (seg >= 0) tc::mma_commit(&s_segdone[seg & 1]);
+                __syncwarp();
             }
+            if (seg >= 0 && leader) tc::mma_commit(&s_segdone[seg & 1]);
         } else if (warp < TV_WARP_TMA) {
             // converters.  Row units come first in the unit order, so this CTA's row units are
             // u_begin .. min(u_end, R) - 1; the thread keeps the packed words of the next TV_PF of
