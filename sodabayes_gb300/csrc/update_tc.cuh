@@ -66,6 +66,9 @@ constexpr int TV_MAXQ = 256;       // stages per subset (subsets up to 16384 SNP
 constexpr int TV_MAXRA = 64;       // ra tiles per subset
 constexpr int TV_THREADS = 448;    // 8 converter warps, TMA, MMA, 4 epilogue warps
 constexpr int TV_NW = TV_THREADS / 32;
+constexpr int TV_NPW = 10;         // warps that take part in the reductions (all but the epilogue warps)
+constexpr int TV_WROW = 5, TV_WRA = 6;   // weights of a row unit and an ra unit in the split (ra
+                                         // units stream their U tile from DRAM: ~1.2x the time)
 constexpr int TV_MAXG = 512;       // CTAs (one per SM)
 constexpr int TV_CONV = 256;
 constexpr int TV_CONV_WARPS = TV_CONV / 32;   // each converter warp arrives once per unit
@@ -158,10 +161,16 @@ __device__ __forceinline__ Unit decode_unit_bs(const UnitPlan &P, int u)
     return x;
 }
 
-// First unit of CTA q when the W units are split over G CTAs in equal shares.
+// First unit of CTA q when the W units (R row units, then ra units) are split
+// over G CTAs in equal shares of weight (TV_WROW per row unit, TV_WRA per ra
+// unit): the first unit whose cumulative weight reaches q / G of the total.
 __device__ __forceinline__ int split_bound(const UnitPlan &P, int q, int G)
 {
-    return (int)(((long long)q * P.W) / G);
+    const long long wr = (long long)TV_WROW * P.R;
+    const long long tw = wr + (long long)TV_WRA * (P.W - P.R);
+    const long long target = (q * tw) / G;
+    if (target <= wr) return (int)((target + TV_WROW - 1) / TV_WROW);
+    return P.R + (int)((target - wr + TV_WRA - 1) / TV_WRA);
 }
 
 // CTA holding unit u: the last q with bnd[q] <= u.
@@ -458,6 +467,18 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     tc::pdl_trigger();
     const int u_begin = s_bnd[blockIdx.x], u_end = s_bnd[blockIdx.x + 1];
     const int nu = u_end - u_begin;
+    // this warp's first two reduction pairs (pr0 and pr0 + stride), prepared as soon as its role
+    // ends (the epilogue warps, the last to finish, take none)
+    const int npair = 2 * (P.nvt + P.nra) * CT;
+    const int pr0 = blockIdx.x * TV_NPW + warp, stride = G * TV_NPW;
+    PairJob ja, jb;
+    auto prepare = [&]() {
+        if (warp < TV_NPW) {
+            tc::pdl_wait();   // r and ra of the previous update
+            pair_prepare<CT>(D, P, s_bnd, G, pr0, npair, N, ja);
+            pair_prepare<CT>(D, P, s_bnd, G, pr0 + stride, npair, N, jb);
+        }
+    };
     if (nu > 0) {
         if (tid == 0) {
             for (int i = 0; i < TV_NS; ++i) {
@@ -731,24 +752,21 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 ptile = x.tile;
             }
         }
+        prepare();
         __syncthreads();
         if (warp == TV_WARP_MMA) {
             tc::fence_after_sync();
             tc::tmem_dealloc(tm, 512);
         }
-    } else if (warp >= TV_WARP_EPI) {
-        tc::pdl_wait();
-        update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);   // the centring term
+    } else {
+        if (warp >= TV_WARP_EPI) {
+            tc::pdl_wait();
+            update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);   // the centring term
+        }
+        prepare();
     }
     __syncthreads();   // s_k0 is complete
     if (tid < CT) s_k0f[tid] = (float)s_k0[tid];   // read after the grid barrier's __syncthreads
-    // this warp's first two pairs (pr0 and pr0 + stride) prepared while the other CTAs finish
-    tc::pdl_wait();   // r and ra of the previous update (every warp reads them below)
-    const int npair = 2 * (P.nvt + P.nra) * CT;
-    const int pr0 = blockIdx.x * TV_NW + warp, stride = G * TV_NW;
-    PairJob ja, jb;
-    pair_prepare<CT>(D, P, s_bnd, G, pr0, npair, N, ja);
-    pair_prepare<CT>(D, P, s_bnd, G, pr0 + stride, npair, N, jb);
     // every segment is in vpart once all CTAs are here; then the reductions, an equal share of the
     // (half tile, chain) pairs per CTA, one pair per warp at a time
     if (!update_grid_sync(D.ugrid, (unsigned)G)) s_err = 16;
@@ -756,6 +774,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
         if (tid == 0) flag_err(D, s_err);
         return;
     }
+    if (warp >= TV_NPW) return;
     for (int pr = pr0; pr < npair; pr += 2 * stride) {
         if (pr != pr0) {
             pair_prepare<CT>(D, P, s_bnd, G, pr, npair, N, ja);
