@@ -44,12 +44,12 @@ namespace soda {
 constexpr int TC_TM = 128;       // SNPs per M tile
 constexpr int TC_KC = 128;       // individuals per genotype stage
 constexpr int TC_KU = 64;        // U rows per augmenting stage
-constexpr int TC_THREADS = 576;  // 16 converter warps, the TMA warp, the MMA warp
-constexpr int TC_CONV = 512;     // converter threads
+constexpr int TC_THREADS = 320;  // 8 converter warps, the TMA warp, the MMA warp
+constexpr int TC_CONV = 256;     // converter threads
 constexpr int TC_CONV_WARPS = TC_CONV / 32;   // each converter warp arrives once per stage
 constexpr int TC_NOB = 4;        // bf16 codes operands in tensor memory (converters run up to 4 stages ahead)
 constexpr int TC_PF = 4;         // packed code words each converter thread holds in flight
-constexpr int TC_WARP_TMA = 16, TC_WARP_MMA = 17;
+constexpr int TC_WARP_TMA = 8, TC_WARP_MMA = 9;
 
 template <int CT>
 struct RhsTc {
@@ -234,27 +234,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (leader) tc::mma_commit(&s_done);
         }
     } else {
-        // converters: thread (SNP m of the tile, individuals 32 s4 .. 32 s4 + 31 of each stage) loads
-        // 8 bytes of packed codes per genotype stage, TC_PF stages ahead, and widens them into one of
-        // four bf16 operands in tensor memory; they take no part in the raw buffers' hand-offs
-        const int m = 32 * (warp & 3) + lane, s4 = warp >> 2;
+        // converters: thread (SNP m of the tile, individuals 64 g .. 64 g + 63 of each stage) loads
+        // 16 bytes of packed codes per genotype stage, TC_PF stages ahead, and widens them into one
+        // of four bf16 operands in tensor memory (32 columns); they take no part in the raw buffers'
+        // hand-offs.  Few, wide converter threads: each stage costs a warp one tensor-memory store,
+        // its wait and an arrival, whatever the number of codes it carries.
+        const int m = 32 * (warp & 3) + lane, g = warp >> 2;
         // a packed block is [4 groups of 64 individuals][128 positions][16 bytes]; stage t covers
-        // individuals 128 (t % 2) .. of tile t / 2, so this thread's 8 bytes are half s4 % 2 of the
-        // 16-byte word (group 2 (t % 2) + s4 / 2, position m)
-        const uint64_t *cw = reinterpret_cast<const uint64_t *>(D.gpk) + 2 * ((s4 >> 1) * TC_TM + m) + (s4 & 1);
+        // individuals 128 (t % 2) .. of tile t / 2, so this thread's word is that of group
+        // 2 (t % 2) + g, position m
+        const uint4 *cw = reinterpret_cast<const uint4 *>(D.gpk) + g * TC_TM + m;
         const size_t blk0 = (size_t)(D.qoff[b] + mt) * D.nvt;
-        auto code_word = [&](int s) -> uint64_t {
+        auto code_word = [&](int s) -> uint4 {
             const int t = t0 + s;
-            const uint64_t *p = cw + (blk0 + (t >> 1)) * (TC_PACKED_BLOCK / 8) + (t & 1) * (4 * TC_TM);
-            uint64_t v;
-            asm volatile("ld.global.nc.L1::no_allocate.u64 %0, [%1];" : "=l"(v) : "l"(p));
+            const uint4 *p = cw + (blk0 + (t >> 1)) * (TC_PACKED_BLOCK / 16) + (t & 1) * (2 * TC_TM);
+            uint4 v;
+            asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                         : "l"(p));
             return v;
         };
-        uint64_t pf[TC_PF];
+        uint4 pf[TC_PF];
 #pragma unroll
-        for (int i = 0; i < TC_PF; ++i) pf[i] = i < nck ? code_word(i) : 0ull;
+        for (int i = 0; i < TC_PF; ++i) pf[i] = i < nck ? code_word(i) : make_uint4(0u, 0u, 0u, 0u);
         tc::pdl_wait();
         tc::pdl_trigger();
+        const uint32_t tl = tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 32 * g;
         // stage s uses pf[s % TC_PF] and reloads it for stage s + TC_PF: the loop is unrolled by
         // TC_PF so that every slot stays in its own registers (a shift of the slots would wait for
         // each load one stage after issuing it)
@@ -273,18 +278,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     stop = true;
                     break;
                 }
-                const uint64_t w = pf[i];
-                pf[i] = s + TC_PF < nck ? code_word(s + TC_PF) : 0ull;
-                // word ww of the 8 bytes: individuals 16 ww + 4 q + e at bits 8 e + 2 q
-                uint32_t v[16];
+                tc::fence_after_sync();
+                const uint4 w = pf[i];
+                pf[i] = s + TC_PF < nck ? code_word(s + TC_PF) : make_uint4(0u, 0u, 0u, 0u);
+                uint32_t o[32];
+                tc::codes64_to_bf16(w, o);   // individuals of the stage, two per column
+                uint32_t lo[16], hi[16];
 #pragma unroll
-                for (int ww = 0; ww < 2; ++ww) {
-                    const uint32_t x = (uint32_t)(w >> (32 * ww));
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        tc::codes_to_bf16x4((x >> (2 * q)) & 0x03030303u, v[8 * ww + 2 * q], v[8 * ww + 2 * q + 1]);
+                for (int e = 0; e < 16; ++e) {
+                    lo[e] = o[e];
+                    hi[e] = o[16 + e];
                 }
-                tc::tmem_st16(tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 64 * ob + 16 * s4, v);
+                tc::tmem_st16(tl + 64 * ob, lo);
+                tc::tmem_st16(tl + 64 * ob + 16, hi);
                 tc::tmem_wait_st();
                 tc::fence_before_sync();
                 __syncwarp();

@@ -308,6 +308,19 @@ __device__ __forceinline__ void codes_to_bf16x4(uint32_t w, uint32_t &w01, uint3
     w23 = bf16x2_sub128(__byte_perm(w, 0x43u, 0x4342u));
 }
 
+// Widens 64 packed codes (element 16 w + 4 b + j at bits 8 j + 2 b of word w)
+// into 32 words of a tensor-memory A operand row: word c holds the bf16 of
+// elements 2c (low half) and 2c + 1.
+__device__ __forceinline__ void codes64_to_bf16(const uint4 &v, uint32_t (&o)[32])
+{
+    const uint32_t ww[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int w = 0; w < 4; ++w)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            codes_to_bf16x4((ww[w] >> (2 * b)) & 0x03030303u, o[8 * w + 2 * b], o[8 * w + 2 * b + 1]);
+}
+
 // (bf16(b) << 16) | bf16(a), round to nearest even
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 {

@@ -386,19 +386,6 @@ __device__ __forceinline__ uint4 update_code_word(const Dev &D, int nvt, int cbl
     return v;
 }
 
-// Widens 64 packed codes (positions 16 w + 4 b + j at bits 8 j + 2 b of word
-// w) into the 32 tensor-memory columns of an A operand row: column c holds
-// the bf16 of positions 2c (low half) and 2c + 1.
-__device__ __forceinline__ void unpack64(const uint4 &v, uint32_t (&o)[32])
-{
-    const uint32_t ww[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int w = 0; w < 4; ++w)
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-            tc::codes_to_bf16x4((ww[w] >> (2 * b)) & 0x03030303u, o[8 * w + 2 * b], o[8 * w + 2 * b + 1]);
-}
-
 template <int CT>
 __global__ void __launch_bounds__(TV_THREADS, 1)
     k_update_tc(const __grid_constant__ CUtensorMap tm_d, const __grid_constant__ CUtensorMap tm_u, Dev D, int b)
@@ -683,7 +670,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     const uint4 w = pf[i];
                     pf[i] = s + TV_PF < nrow ? next_word() : make_uint4(0u, 0u, 0u, 0u);
                     uint32_t o[32];
-                    unpack64(w, o);
+                    tc::codes64_to_bf16(w, o);   // positions of the stage, two per column
                     uint32_t lo[16], hi[16];
 #pragma unroll
                     for (int e = 0; e < 16; ++e) {
