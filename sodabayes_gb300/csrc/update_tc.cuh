@@ -60,7 +60,7 @@ namespace soda {
 
 constexpr int TV_N = 256;          // individuals per row tile / rows of U per ra tile (two MMA M halves)
 constexpr int TV_K = 64;           // subset positions per stage
-constexpr int TV_NS = 4;           // operand slots: delta-split tile, and the codes or the U tile
+constexpr int TV_NS = 5;           // operand slots: delta-split tile, and the codes or the U tile
 constexpr int TV_PF = 4;           // packed code words each converter thread holds in flight
 constexpr int TV_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
 constexpr int TV_MAXRA = 64;       // ra tiles per subset
@@ -85,9 +85,9 @@ struct UpdTc {
     static constexpr int BOP0 = AREG;
     static constexpr size_t SMEM = 1024 + (size_t)AREG + (size_t)TV_NS * BOP;
     // tensor memory: accumulators (segment parity p, half h) at columns NB (2p + h), the codes
-    // operands (slot sl, half h) at 256 + 64 sl + 32 h (32 columns: 64 positions, two bf16 each)
+    // operands (slot sl, half h) at 192 + 64 sl + 32 h (32 columns: 64 positions, two bf16 each)
     static constexpr int TM_ACC = NB;
-    static constexpr int TM_OPS = 256;
+    static constexpr int TM_OPS = 192;
     static_assert(RAW_A % 1024 == 0 && AREG % 1024 == 0 && BOP % 1024 == 0, "buffer alignment");
     static_assert(4 * NB <= TM_OPS && TM_OPS + 64 * TV_NS <= 512, "tensor memory");
     static_assert(SMEM <= 227 * 1024, "shared memory");
@@ -493,11 +493,11 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 tc::tma_prefetch_desc(&tm_d);
                 tc::tma_prefetch_desc(&tm_u);
             }
-            tc::pdl_wait();   // the A tiles are the draws' delta split
             bool ok = true;
             int issued = 0;
-            for (int s0 = 0; s0 < nu && ok; s0 += 32) {
-                int kind = 0, ax = 0, cy = 0, cz = 0;
+            int kind = 0, ax = 0, cy = 0, cz = 0;
+            auto decode = [&](int s0) {
+                kind = ax = cy = cz = 0;
                 if (s0 + lane < nu) {
                     const Unit x = decode_unit_bs(P, u_begin + s0 + lane);
                     kind = x.kind;
@@ -505,6 +505,25 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     cy = x.tile * TV_N;                 // ra: four boxes of 64 rows of U x 64 positions
                     cz = x.term * D.p + ls + ax;        //     from row 256 tile, term's plane
                 }
+            };
+            auto load_u = [&](int sl, int y, int z) {
+                unsigned char *bo = bop0 + (size_t)sl * T::BOP;   // MN atoms 8 KB apart
+                tc::mbar_expect_tx(&s_fullb[sl], T::BOP);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) tc::tma_load_2d(bo + h * 8192, &tm_u, y + 64 * h, z, &s_fullb[sl]);
+            };
+            // the U tiles of the first slots' ra units do not depend on the draws: they stream from
+            // DRAM while the draws run
+            decode(0);
+            const int npre = min(nu, TV_NS);
+            for (int i = 0; i < npre; ++i) {
+                const int kd = __shfl_sync(0xffffffffu, kind, i);
+                const int y = __shfl_sync(0xffffffffu, cy, i), z = __shfl_sync(0xffffffffu, cz, i);
+                if (lane == 0 && kd == 1) load_u(i, y, z);
+            }
+            tc::pdl_wait();   // the delta tiles are the draws' split
+            for (int s0 = 0; s0 < nu && ok; s0 += 32) {
+                if (s0 > 0) decode(s0);
                 const int m = min(32, nu - s0);
                 for (int i = 0; i < m; ++i) {
                     const int s = s0 + i;
@@ -519,13 +538,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                         } else {
                             tc::mbar_expect_tx(&s_fulla[sl], T::RAW_A);
                             tc::tma_load_2d(raw0 + (size_t)sl * T::ASTRIDE, &tm_d, k0, 0, &s_fulla[sl]);
-                            if (kd == 1) {
-                                unsigned char *bo = bop0 + (size_t)sl * T::BOP;   // MN atoms 8 KB apart
-                                tc::mbar_expect_tx(&s_fullb[sl], T::BOP);
-#pragma unroll
-                                for (int h = 0; h < 4; ++h)
-                                    tc::tma_load_2d(bo + h * 8192, &tm_u, y + 64 * h, z, &s_fullb[sl]);
-                            }
+                            if (kd == 1 && s >= TV_NS) load_u(sl, y, z);
                             issued = s + 1;
                         }
                     }
@@ -534,11 +547,13 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 }
             }
             // no copy may still be in flight into this CTA's shared memory when it exits: wait (bounded)
-            // for the last loads issued into every slot (already complete unless a wait above gave up)
-            if (lane == 0 && issued > 0) {
+            // for the last loads issued into every slot (already complete unless a wait above gave up),
+            // the U tiles issued before the dependency wait included
+            if (lane == 0) {
                 const int nrow = max(0, min(u_end, P.R) - u_begin);
-                for (int s = max(0, issued - TV_NS); s < issued; ++s) {
-                    if (!tc::mbar_wait(&s_fulla[s % TV_NS], (s / TV_NS) & 1)) s_err = 21;
+                const int last = max(issued, npre);
+                for (int s = max(0, last - TV_NS); s < last; ++s) {
+                    if (s < issued && !tc::mbar_wait(&s_fulla[s % TV_NS], (s / TV_NS) & 1)) s_err = 21;
                     if (s >= nrow && !tc::mbar_wait(&s_fullb[s % TV_NS], ra_phase(s, nrow) & 1)) s_err = 21;
                 }
             }
