@@ -130,6 +130,12 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
                 vs = (float)D.vara_s[(size_t)c * D.p + snp];
         }
     }
+    // the SNP's draw site and its first Philox block, ahead of the dependency wait
+    CRng R;
+    if (snp >= 0 && !D.rhs_out) {
+        crng_site(R, D, c, cur_rep(D), snp, P_SNP);
+        crng_warm(R);
+    }
     if (TC && act) {   // the tensor-core rhs gives each 128-SNP tile its own number of splits
         const int32_t *rt = D.rtab + (size_t)b * D.tstride + jl / 128;
         ksplit = rt[1] - rt[0];
@@ -216,8 +222,6 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
         if (TC) xr = xr * (inv != 0.0 ? inv : 1.0) + x0 * s_rs[c];   // columns with sd = 0 carry U unscaled
         else if (MODE == SODAGPU_FP8) xr = xr * inv + x0 * s_rs[c];
         const ChainScal *S = &D.scal[c];
-        CRng R;
-        crng_site(R, D, c, cur_rep(D), snp, P_SNP);
         int err = 0;
         if (MODE == SODAGPU_FP64) {
             delta = draw_snp(D, S, c, cur_rep(D), snp, xr + ur, zz, zz / S->vare, R, &err);

@@ -31,8 +31,8 @@ constexpr int CRNG_TAPE_OVERRUN = 19;
 
 struct CRng {
     uint32_t k0, k1, c0, c1, c2, c3;
-    uint32_t o2, o3;
-    int have;
+    uint32_t o0, o1, o2, o3;
+    int have;   // cached outputs of the last block: 2 both halves, 1 the second, 0 none
     // injected draws: the uniforms of this draw site come from a tape record
     // of SODAGPU_TAPE_W values instead of Philox; tover is set on overrun
     const double *tape;
@@ -86,8 +86,28 @@ __device__ __forceinline__ double crng_tape_next(CRng &s)
     return v;
 }
 
+// Computes the first Philox block of a draw site ahead of its first use (the
+// counters do not depend on the data, so a kernel can do this before waiting
+// for the kernel that produces them): crng_u64 then returns the same values.
+__host__ __device__ __forceinline__ void crng_warm(CRng &s)
+{
+    if (s.have != 0 || s.tape) return;
+    uint32_t a = s.c0, b = s.c1, c = s.c2, d = s.c3;
+    philox4x32_10(a, b, c, d, s.k0, s.k1);
+    s.c3++;
+    s.o0 = a;
+    s.o1 = b;
+    s.o2 = c;
+    s.o3 = d;
+    s.have = 2;
+}
+
 __host__ __device__ __forceinline__ uint64_t crng_u64(CRng &s)
 {
+    if (s.have == 2) {
+        s.have = 1;
+        return ((uint64_t)s.o1 << 32) | s.o0;
+    }
     if (s.have == 0) {
         uint32_t a = s.c0, b = s.c1, c = s.c2, d = s.c3;
         philox4x32_10(a, b, c, d, s.k0, s.k1);
