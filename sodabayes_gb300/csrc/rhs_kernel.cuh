@@ -91,6 +91,7 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
 {
     __shared__ double s_rs[CT];   // sum(r) per chain (FP8 centring)
     __shared__ double s_k[256];
+    __shared__ float s_kf[256];   // tensor-core path: x0_j delta_j in FP32
     __shared__ DrawPre s_pre[CT];   // chain constants in FP32 (the FP64 pipe is narrow)
     __shared__ float s_zzv[CT];
     __shared__ float s_d32[256];
@@ -168,11 +169,15 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
         s_rs[tid] = tt;
     }
     __syncthreads();
+    // tensor-core path: the rhs is assembled in FP32 (its split sums are FP32; the FP64 pipe of
+    // GB300 is narrow and also runs every double <-> float conversion)
+    const float x0f = (float)x0, rsf = TC ? (float)s_rs[c] : 0.0f;
     tc::pdl_trigger();
     tc::pdl_wait();
     // the rhs partial sums of all splits, added in split order (the tensor-core rhs
     // gives one FP32 sum per split: codes' r + (sd u)' ra)
     double xr = 0.0, ur = 0.0;
+    float xf = 0.0f;
     if (TC) {
         const float *px32 = reinterpret_cast<const float *>(D.rpx);
         float px[RHS_KSPLIT_MAX];
@@ -184,7 +189,8 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
         float xs = 0.0f;
 #pragma unroll
         for (int sp = 0; sp < RHS_KSPLIT_MAX; ++sp) xs += px[sp];
-        xr = xs;
+        // columns with sd = 0 (zero codes) carry U unscaled
+        xf = __fmaf_rn(x0f, rsf, __fmul_rn(xs, inv32 != 0.0f ? inv32 : 1.0f));
     } else {
         double px[RHS_KSPLIT_MAX], pu[RHS_KSPLIT_MAX];
 #pragma unroll
@@ -209,9 +215,9 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
             double v = 0.0;
             if (snp >= 0) {
                 double x = xr;
-                if (TC) x = x * (inv != 0.0 ? inv : 1.0) + x0 * s_rs[c];
-                else if (MODE == SODAGPU_FP8) x = x * inv + x0 * s_rs[c];
-                v = MODE == SODAGPU_FP64 ? x + ur : (double)(float)(x + ur);   // what the draw consumes
+                if (MODE == SODAGPU_FP8 && !TC) x = x * inv + x0 * s_rs[c];
+                // what the draw consumes
+                v = TC ? (double)xf : MODE == SODAGPU_FP64 ? x + ur : (double)(float)(x + ur);
             }
             D.rhs_out[(size_t)c * D.bs + jl] = v;
         }
@@ -219,8 +225,7 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
     }
     double delta = 0.0;
     if (snp >= 0) {
-        if (TC) xr = xr * (inv != 0.0 ? inv : 1.0) + x0 * s_rs[c];   // columns with sd = 0 carry U unscaled
-        else if (MODE == SODAGPU_FP8) xr = xr * inv + x0 * s_rs[c];
+        if (MODE == SODAGPU_FP8 && !TC) xr = xr * inv + x0 * s_rs[c];
         const ChainScal *S = &D.scal[c];
         int err = 0;
         if (MODE == SODAGPU_FP64) {
@@ -233,7 +238,8 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
                 for (int q = 0; q < DRAW_PRE; ++q)
                     pre.logp[q] = q < D.nmix ? (float)S->log_p[sg + q * D.ngroup] : 0.0f;
             }
-            delta = draw_snp_f(D, S, c, snp, (float)(xr + ur), (float)zz, s_zzv[c], R, &err, gold, cl, sg, pre);
+            const float rhs = TC ? xf : (float)(xr + ur);
+            delta = draw_snp_f(D, S, c, snp, rhs, (float)zz, s_zzv[c], R, &err, gold, cl, sg, pre);
         }
         if (err) flag_err(D, 1);
     }
@@ -253,15 +259,15 @@ __device__ __forceinline__ void draw_body(const Dev &D, const VB &vb, int b, int
             D.dsplit[(size_t)(CT + c) * D.ldd + jl] = (uint16_t)mid;
             D.dsplit[(size_t)(2 * CT + c) * D.ldd + jl] = (uint16_t)lo;
         }
-        // this CTA's sum of x0_j delta_j per chain, SNPs in order
-        __syncthreads();
-        s_k[jloc * CT + c] = x0 * delta;
+        // this CTA's sum of x0_j delta_j per chain, SNPs in order (FP32: the update adds the
+        // centring term to FP32 segment sums)
+        s_kf[jloc * CT + c] = __fmul_rn(x0f, delta32);
     }
     __syncthreads();
     if (TC && tid < CT) {
-        double tt = 0.0;
-        for (int q = 0; q < SPC; ++q) tt += s_k[q * CT + tid];
-        D.k0part[(size_t)vb.x * CT + tid] = tt;
+        float tt = 0.0f;
+        for (int q = 0; q < SPC; ++q) tt += s_kf[q * CT + tid];
+        D.k0part[(size_t)vb.x * CT + tid] = (double)tt;
     }
     // delta32 chain-contiguous per SNP (the CTA's block of 256 values), and the flags of SNPs whose
     // delta is non-zero in some chain
