@@ -16,19 +16,20 @@
 // draw kernel.  A CTA owns one M tile and a contiguous range of its stages
 // (genotype stages first) and runs a warp-specialised pipeline synchronised
 // by mbarriers:
-//   warp 16 (one thread) TMA: each stage's B tile (the residual split) and,
+//   warp 8 (one thread) TMA: each stage's B tile (the residual split) and,
 //           for U stages, its A tile (128 x 64 bf16), 128-byte swizzled, into
 //           a raw buffer (NS buffers in flight);
-//   warps 0-15 load the genotype codes of a stage 2-bit packed from global
-//           memory (8 bytes = 32 codes per thread, several stages ahead; the
+//   warps 0-7 load the genotype codes of a stage 2-bit packed from global
+//           memory (16 bytes = 64 codes per thread, several stages ahead; the
 //           codes are written once, before the sweep, so the first loads are
 //           issued before the dependency wait) and widen them into one of four
 //           bf16 operands in tensor memory (lane = SNP, tcgen05.st); they take
 //           no part in the raw buffers' hand-offs;
-//   warp 17 (one thread) issues the stage's MMAs (A from tensor memory or,
-//           for U stages, from the raw buffer; B always from the raw buffer)
-//           once the operands are in place, and commits their completion,
-//           which frees the buffers.
+//   warp 9 runs the issue loop on warp-uniform values and one elected lane
+//           issues the stage's MMAs (A from tensor memory or, for U stages,
+//           from the raw buffer; B always from the raw buffer) once the
+//           operands are in place, and commits their completion, which frees
+//           the buffers.
 // With programmatic dependent launch the prologue (barriers, tensor memory,
 // the first U tiles, which are constant, and the first code words) overlaps
 // the previous kernel; the residual splits are read after it completes.  Each

@@ -29,25 +29,27 @@
 // an ra tile only from its first row on.  The plan depends on the subset's
 // shape alone, so it is made, and the first code words are loaded, before
 // the draws of this subset complete.  The units are laid out row tiles first
-// and split evenly over the CTAs (stream-K, one CTA per SM); a CTA's
-// consecutive units of one tile form a segment, whose accumulator rows go to
-// vpart as FP32 partial sums (hi + mid + lo per chain).  After a grid-wide
-// barrier (one CTA per SM, all resident; the wait is bounded) every CTA takes
+// and split over the CTAs (stream-K, one CTA per SM) in equal shares of
+// weight, an ra unit weighing 6/5 of a row unit; a CTA's consecutive units of
+// one tile form a segment, whose accumulator rows go to vpart as FP32 partial
+// sums (hi + mid + lo per chain).  After a grid-wide barrier (one CTA per SM,
+// all resident; the wait is bounded) the non-epilogue warps of every CTA take
 // an equal share of the (128-element half tile, chain) pairs, whose old
-// residuals it loaded before the barrier: it adds the pair's segments in
+// residuals each loaded as soon as its own role ended: it adds the pair's segments in
 // segment order (deterministic) and the centring term sum_j x0_j delta_j, and
 // writes the FP64 residuals.  Spreading this over every SM matters: GB300
 // runs FP64 at a small fraction of its FP32 rate, and a tile's residuals take
 // about as long on one SM's FP64 pipe as a third of the unit loop.
 //
 // Warp roles (mbarrier hand-offs, every wait bounded): warp 8 issues the TMA
-// loads, warps 0-7 widen the codes, warp 9 issues the MMAs, warps 10-13
-// reduce the centring term and move finished accumulators to vpart; all warps
-// then take part in the reductions.  A CTA's row units come before its ra
-// units.  Unit s uses slot s % TV_NS of both operands, and one commit of its
-// MMAs frees both:
+// loads, warps 0-7 widen the codes, warp 9 runs the MMA loop on warp-uniform
+// values with one elected lane issuing, warps 10-13 reduce the centring term
+// and move finished accumulators to vpart; warps 0-9 then take part in the
+// reductions.  A CTA's row units come before its ra units.  Unit s uses slot
+// s % TV_NS of both operands, and one commit of its MMAs frees both:
 //   producer: wait free (MMAs of s - TV_NS); load the delta tile (+ tx) on
-//     fulla; for an ra unit also load the U tile (+ tx) on fullb;
+//     fulla; for an ra unit also load the U tile (+ tx) on fullb (the U
+//     tiles of the first TV_NS units load before the dependency wait);
 //   converters (row units only): wait free; write the codes into the slot's
 //     tensor-memory operand; arrive on conv;
 //   MMA: wait conv (row unit) or fullb (ra unit), and fulla; 8 MMAs; commit
