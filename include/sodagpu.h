@@ -324,7 +324,10 @@ int sodagpu_compute_dgv_noalloc(int32_t nind, int32_t nloci, const int8_t *codes
  * with one precision and chain count, and run on the CUDA-core kernels
  * (SODAGPU_KERNELS_CUDA_CORES, or fewer than 4 chains); after a batch run
  * their state and results are read with the per-job calls.  A job may belong
- * to one batch at a time and must not be run on its own meanwhile. */
+ * to one batch at a time and must not be run on its own meanwhile.  The batch
+ * copies each job's device layout when it is created: destroy the batch
+ * before any of its jobs, and create it again after re-initialising a job
+ * (sodagpu_init_chains). */
 #define SODAGPU_MAXJOBS 64
 /* flags of sodagpu_batch_create.  By default each job's rhs products get K
  * splits in proportion to its share of the batch's genotype bytes, so that

@@ -560,6 +560,9 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                 }
             }
         } else if (warp == TV_WARP_MMA) {
+            // nothing to issue before the draws' delta tiles: block in the dependency wait rather than
+            // in mbarrier polls, which would take issue slots from the draw kernel on this SM
+            tc::pdl_wait();
             // The loop keeps the tensor pipe fed only if it does little between MMA issues (the pipe
             // queues about one unit ahead): the whole warp runs it on warp-uniform values and one
             // elected lane issues, the descriptors are built once per slot and advanced by constants,
@@ -675,6 +678,10 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     const int s = s0 + i;
                     if (s >= nrow || stop) break;
                     const int ob = s % TV_NS;
+                    // the first TV_NS units are widened while the draws still run; the next ones wait
+                    // for MMAs that need the draws' output, so block in the dependency wait first
+                    // (mbarrier polls would take issue slots from the draw kernel on this SM)
+                    if (s == TV_NS) tc::pdl_wait();
                     // the operand was last read by the MMAs of unit s - TV_NS
                     bool ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);
                     ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
