@@ -282,12 +282,17 @@ def bench_ours(args, rank, ws):
     job = SodaJob(make_config(spec.n, spec.p, _opts("fp8", C, 77 + rank, Ke)))
     job.load_genotypes(host_ptr=host_codes.data_ptr())
     job.load_pheno(y)
+    t_up = time.perf_counter()
     job.build_z()
     job.init_chains()
+    t_setup = time.perf_counter()
     job.run(Ke, trace=lambda r: rows.append(r.rep))
+    t_run = time.perf_counter()
     outs = [job.results(c) for c in range(C)]
     job.close()
     t_e2e = time.perf_counter() - t0
+    phases = {"create_and_upload_s": round(t_up - t0, 3), "z_build_and_init_s": round(t_setup - t_up, 3),
+              "iterations_s": round(t_run - t_setup, 3), "results_s": round(t0 + t_e2e - t_run, 3)}
     t_e2e = _max_over_ranks(t_e2e, ws)
     units_e2e = _sum_over_ranks(float(Ke * C), ws)
     h2d = spec.n * spec.p + 8 * spec.n
@@ -295,7 +300,7 @@ def bench_ours(args, rank, ws):
     res["e2e"] = {"value": units_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d / Ke),
                   "d2h_bytes_per_step": int(d2h / Ke), "iterations": Ke, "wall_s": round(t_e2e, 3),
                   "includes": "create, genotype+phenotype upload, Z build, init, iterations with .hyp trace, "
-                              "posterior means download"}
+                              "posterior means download", "phases": phases}
     del outs
     return res
 
