@@ -383,7 +383,7 @@ def _batch_means(x):
 
 
 def acceptance(spec, codes, y, C, burn, keep):
-    """Free-running config-3 chains (the benchmark spec acceptance): the FP8 sampler with C chains, the plain
+    """Free-running chains of the n=20000, p=500000 workload (acceptance): the FP8 sampler with C chains, the plain
     FP32 path (1 chain) and two FP64 runs (1 chain each, seeds A and B: the Monte-Carlo floor of two
     independent FP64 runs).  Posterior means of the SNP effects and GEBVs (compute_dgv,
     utilities.f90:616-622, of the posterior means, models.f90:576-598), pi = included / p, the model's
