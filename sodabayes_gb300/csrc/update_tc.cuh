@@ -63,10 +63,10 @@ namespace soda {
 constexpr int TV_N = 256;          // individuals per row tile / rows of U per ra tile (two MMA M halves)
 constexpr int TV_K = 64;           // subset positions per stage
 constexpr int TV_NS = 5;           // operand slots: delta-split tile, and the codes or the U tile
-constexpr int TV_PF = 4;           // packed code words each converter thread holds in flight
+constexpr int TV_NC = 6;           // shared-memory slots of packed codes (4 KB: one row unit each)
 constexpr int TV_MAXQ = 256;       // stages per subset (subsets up to 16384 SNPs)
 constexpr int TV_MAXRA = 64;       // ra tiles per subset
-constexpr int TV_THREADS = 448;    // 8 converter warps, TMA, MMA, 4 epilogue warps
+constexpr int TV_THREADS = 480;    // 8 converter warps, TMA, MMA, 4 epilogue warps, code loader
 constexpr int TV_NW = TV_THREADS / 32;
 constexpr int TV_NPW = 10;         // warps that take part in the reductions (all but the epilogue warps)
 constexpr int TV_WROW = 5, TV_WRA = 6;   // weights of a row unit and an ra unit in the split (ra
@@ -74,7 +74,7 @@ constexpr int TV_WROW = 5, TV_WRA = 6;   // weights of a row unit and an ra unit
 constexpr int TV_MAXG = 512;       // CTAs (one per SM)
 constexpr int TV_CONV = 256;
 constexpr int TV_CONV_WARPS = TV_CONV / 32;   // each converter warp arrives once per unit
-constexpr int TV_WARP_TMA = 8, TV_WARP_MMA = 9, TV_WARP_EPI = 10;
+constexpr int TV_WARP_TMA = 8, TV_WARP_MMA = 9, TV_WARP_EPI = 10, TV_WARP_CODES = 14;
 
 template <int CT>
 struct UpdTc {
@@ -85,7 +85,9 @@ struct UpdTc {
     static constexpr int AREG = TV_NS * ASTRIDE;
     static constexpr int BOP = TV_K * TV_N * 2;        // U tile of an ra unit: 256 rows x 64 bf16
     static constexpr int BOP0 = AREG;
-    static constexpr size_t SMEM = 1024 + (size_t)AREG + (size_t)TV_NS * BOP;
+    static constexpr int CODE = TV_N * 16;             // packed codes of one row unit (256 individuals)
+    static constexpr int CODE0 = BOP0 + TV_NS * BOP;
+    static constexpr size_t SMEM = 1024 + (size_t)CODE0 + (size_t)TV_NC * CODE;
     // tensor memory: accumulators (segment parity p, half h) at columns NB (2p + h), the codes
     // operands (slot sl, half h) at 192 + 64 sl + 32 h (32 columns: 64 positions, two bf16 each)
     static constexpr int TM_ACC = NB;
@@ -374,20 +376,6 @@ __device__ __forceinline__ bool update_grid_sync(unsigned long long *ctr, unsign
     return s_ok != 0;
 }
 
-// Packed code word of a converter thread for row unit (tile, q): individual i
-// (0..255) of row tile `tile`, the 64 positions of stage q (16 bytes: 64 codes
-// of 2 bits; the individual-major copy, D.gpu).
-__device__ __forceinline__ uint4 update_code_word(const Dev &D, int nvt, int cblk, int tile, int q, int i)
-{
-    const size_t blk = (size_t)(cblk + (q >> 1)) * nvt + tile;
-    const uint4 *w = reinterpret_cast<const uint4 *>(D.gpu + blk * TC_PACKED_BLOCK) + (q & 1) * TV_N + i;
-    uint4 v;
-    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(w));
-    return v;
-}
-
 template <int CT>
 __global__ void __launch_bounds__(TV_THREADS, 1)
     k_update_tc(const __grid_constant__ CUtensorMap tm_d, const __grid_constant__ CUtensorMap tm_u, Dev D, int b)
@@ -395,6 +383,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
     using T = UpdTc<CT>;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
     __shared__ uint64_t s_fulla[TV_NS], s_fullb[TV_NS], s_conv[TV_NS], s_free[TV_NS];
+    __shared__ uint64_t s_cfull[TV_NC], s_cfree[TV_NC];
     __shared__ uint64_t s_segdone[2], s_dfree[2];
     __shared__ uint32_t s_tmem;
     __shared__ int s_err;
@@ -479,6 +468,10 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             for (int i = 0; i < 2; ++i) {
                 tc::mbar_init(&s_segdone[i], 1);
                 tc::mbar_init(&s_dfree[i], 1);
+            }
+            for (int i = 0; i < TV_NC; ++i) {
+                tc::mbar_init(&s_cfull[i], 1);                // a row unit's packed codes landed
+                tc::mbar_init(&s_cfree[i], TV_CONV_WARPS);    // every converter warp has read them
             }
             tc::mbar_fence_init();
         }
@@ -648,66 +641,81 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             if (seg >= 0 && leader) tc::mma_commit(&s_segdone[seg & 1]);
         } else if (warp < TV_WARP_TMA) {
             // converters.  Row units come first in the unit order, so this CTA's row units are
-            // u_begin .. min(u_end, R) - 1; the thread keeps the packed words of the next TV_PF of
-            // them in registers (the codes are not written by any kernel of the sweep, so the first
-            // ones are loaded while the draws still run).  Warp w writes tensor-memory lanes
-            // 32 (w % 4) .. of half h = w / 4: the thread's individual is 128 h + 32 (w % 4) + lane.
+            // u_begin .. min(u_end, R) - 1; the code loader streams their packed codes into a ring
+            // of shared-memory slots, and each thread takes its 16 bytes from there.  Warp w writes
+            // tensor-memory lanes 32 (w % 4) .. of half h = w / 4: the thread's individual is
+            // 128 h + 32 (w % 4) + lane.
             const int nrow = max(0, min(u_end, P.R) - u_begin);
-            const int pnq = P.nq, pnvt = P.nvt;
             const int ind = 128 * (warp >> 2) + 32 * (warp & 3) + lane;
-            int ftile = u_begin / pnq, fq = u_begin - ftile * pnq;   // the next unit to load
-            auto next_word = [&]() -> uint4 {
-                const uint4 v = update_code_word(D, pnvt, cblk, ftile, fq, ind);
-                if (++fq == pnq) {
-                    fq = 0;
-                    ++ftile;
-                }
-                return v;
-            };
-            uint4 pf[TV_PF];
-#pragma unroll
-            for (int i = 0; i < TV_PF; ++i) pf[i] = i < nrow ? next_word() : make_uint4(0u, 0u, 0u, 0u);
+            const unsigned char *codes0 = raw0 + T::CODE0 + ind * 16;
             const uint32_t tl = tm + ((uint32_t)(32 * (warp & 3)) << 16) + T::TM_OPS + 32 * (warp >> 2);
-            // unit s uses pf[s % TV_PF] and reloads it for unit s + TV_PF: the loop is unrolled by
-            // TV_PF so that every slot stays in its own registers (a shift of the slots would wait
-            // for each load one unit after issuing it)
-            bool stop = false;
-            for (int s0 = 0; s0 < nrow && !stop; s0 += TV_PF) {
+            for (int s = 0; s < nrow; ++s) {
+                const int ob = s % TV_NS, cs = s % TV_NC;
+                bool ok = tc::mbar_wait(&s_cfull[cs], (s / TV_NC) & 1);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) {
+                    s_err = 13;
+                    break;
+                }
+                const uint4 w = *reinterpret_cast<const uint4 *>(codes0 + (size_t)cs * T::CODE);
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&s_cfree[cs]);   // the slot may be refilled
+                // the first TV_NS units are widened while the draws still run; the next ones wait
+                // for MMAs that need the draws' output, so block in the dependency wait first
+                // (mbarrier polls would take issue slots from the draw kernel on this SM)
+                if (s == TV_NS) tc::pdl_wait();
+                // the operand was last read by the MMAs of unit s - TV_NS
+                ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);
+                ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
+                if (!ok) {
+                    s_err = 13;
+                    break;
+                }
+                tc::fence_after_sync();
+                uint32_t o[32];
+                tc::codes64_to_bf16(w, o);   // positions of the stage, two per column
+                uint32_t lo[16], hi[16];
 #pragma unroll
-                for (int i = 0; i < TV_PF; ++i) {
-                    const int s = s0 + i;
-                    if (s >= nrow || stop) break;
-                    const int ob = s % TV_NS;
-                    // the first TV_NS units are widened while the draws still run; the next ones wait
-                    // for MMAs that need the draws' output, so block in the dependency wait first
-                    // (mbarrier polls would take issue slots from the draw kernel on this SM)
-                    if (s == TV_NS) tc::pdl_wait();
-                    // the operand was last read by the MMAs of unit s - TV_NS
-                    bool ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);
-                    ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
-                    if (!ok) {
-                        s_err = 13;
-                        stop = true;
+                for (int e = 0; e < 16; ++e) {
+                    lo[e] = o[e];
+                    hi[e] = o[16 + e];
+                }
+                tc::tmem_st16(tl + 64 * ob, lo);
+                tc::tmem_st16(tl + 64 * ob + 16, hi);
+                tc::tmem_wait_st();
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
+            }
+        } else if (warp == TV_WARP_CODES) {
+            // code loader: one bulk copy (4 KB, individual-major packed codes) per row unit into the
+            // ring, issued as slots free; the codes are not written by any kernel of the sweep, so
+            // the first copies run while the draws still do.  Bulk copies stream at DRAM rates that
+            // per-thread loads of the same bytes do not reach (each SM caps its outstanding loads).
+            if (lane == 0) {
+                const int nrow = max(0, min(u_end, P.R) - u_begin);
+                const int pnq = P.nq, pnvt = P.nvt;
+                int tile = u_begin / pnq, q = u_begin - tile * pnq;
+                int issued = 0;
+                for (int s = 0; s < nrow; ++s) {
+                    const int cs = s % TV_NC;
+                    if (s >= TV_NC && !tc::mbar_wait(&s_cfree[cs], ((s / TV_NC) - 1) & 1)) {
+                        s_err = 14;
                         break;
                     }
-                    tc::fence_after_sync();
-                    const uint4 w = pf[i];
-                    pf[i] = s + TV_PF < nrow ? next_word() : make_uint4(0u, 0u, 0u, 0u);
-                    uint32_t o[32];
-                    tc::codes64_to_bf16(w, o);   // positions of the stage, two per column
-                    uint32_t lo[16], hi[16];
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                        lo[e] = o[e];
-                        hi[e] = o[16 + e];
+                    const size_t blk = (size_t)(cblk + (q >> 1)) * pnvt + tile;
+                    tc::mbar_expect_tx(&s_cfull[cs], T::CODE);
+                    tc::bulk_load(raw0 + T::CODE0 + cs * T::CODE, D.gpu + blk * TC_PACKED_BLOCK + (q & 1) * T::CODE,
+                                  T::CODE, &s_cfull[cs]);
+                    issued = s + 1;
+                    if (++q == pnq) {
+                        q = 0;
+                        ++tile;
                     }
-                    tc::tmem_st16(tl + 64 * ob, lo);
-                    tc::tmem_st16(tl + 64 * ob + 16, hi);
-                    tc::tmem_wait_st();
-                    tc::fence_before_sync();
-                    __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
                 }
+                // no copy may still be in flight into this CTA's shared memory when it exits
+                for (int s = max(0, issued - TV_NC); s < issued; ++s)
+                    if (!tc::mbar_wait(&s_cfull[s % TV_NC], (s / TV_NC) & 1)) s_err = 21;
             }
         } else {
             // epilogue: per finished segment, warp w reads tensor-memory lanes 32 (w % 4) .. (individuals
@@ -770,7 +778,7 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
             tc::tmem_dealloc(tm, 512);
         }
     } else {
-        if (warp >= TV_WARP_EPI) {
+        if (warp >= TV_WARP_EPI && warp < TV_WARP_EPI + 4) {
             tc::pdl_wait();
             update_k0<CT>(D, b, tid - 32 * TV_WARP_EPI, s_k0p, s_k0);   // the centring term
         }

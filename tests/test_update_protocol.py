@@ -6,7 +6,10 @@ phase parity: a wait for phase i returns as soon as the barrier's completed
 phase count k has the other parity than i.  It is therefore sound only if it
 is never asked while k <= i - 1 (it would return at once, a phase early) and
 never when k >= i + 2 (a whole phase was missed).  A CTA's row units come
-before its ra units; unit s uses operand slot s % NS.  The producer waits for
+before its ra units; unit s uses operand slot s % NS.  A code loader streams
+each row unit's packed codes into code slot s % NC (bulk copy; cfull
+completes on arrival), waiting until every converter has read the slot's
+previous unit (cfree).  The producer waits for
 the slot (the MMAs of unit s - NS), loads A, and for an ra unit also loads B
 by TMA (fullb completes on arrival); the converters, for row units only, wait
 for the slot themselves, widen the codes into B and arrive on conv; the MMA
@@ -17,8 +20,8 @@ commit) under random interleavings, with the slot count read from the
 kernel's source, and checks that every wait that returns has exactly its
 phase completed and that no buffer is written while a reader of its previous
 contents is pending.  Planted mistakes it must catch: converters that do not
-wait for the slot, a fullb phase that forgets the row units, and ra units
-placed before row units."""
+wait for the slot, a code loader that does not wait for its slot, a fullb
+phase that forgets the row units, and ra units placed before row units."""
 import os
 import random
 import re
@@ -31,10 +34,17 @@ def _consts():
     txt = open(SRC).read()
     m = re.search(r"constexpr int TV_NS = (\d+);", txt)
     assert m, "TV_NS"
+    mc = re.search(r"constexpr int TV_NC = (\d+);", txt)
+    assert mc, "TV_NC"
     return {
         "TV_NS": int(m.group(1)),
+        "TV_NC": int(mc.group(1)),
+        # the code loader waits until every converter has read the slot's previous unit
+        "cfree_wait": "if (s >= TV_NC && !tc::mbar_wait(&s_cfree[cs], ((s / TV_NC) - 1) & 1)) {" in txt,
+        # the converters wait for their unit's codes
+        "cfull_wait": "bool ok = tc::mbar_wait(&s_cfull[cs], (s / TV_NC) & 1);" in txt,
         # the converters wait for the slot before writing B
-        "conv_wait": "bool ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);" in txt,
+        "conv_wait": "ok = s < TV_NS || tc::mbar_wait(&s_free[ob], ((s / TV_NS) - 1) & 1);" in txt,
         # the MMA thread's fullb phase discounts the slot's row units
         "ra_phase": "tc::mbar_wait(&s_fullb[sl], ra_phase(s, nrow) & 1)" in txt,
     }
@@ -64,7 +74,7 @@ def ra_phase(s, nrow, NS):
     return s // NS - ((nrow - 1 - sl) // NS + 1 if nrow > sl else 0)
 
 
-def run(kinds, NS, seed, conv_wait=True, naive_ra_phase=False):
+def run(kinds, NS, seed, conv_wait=True, naive_ra_phase=False, NC=6, cfree_wait=True):
     rnd = random.Random(seed)
     nu = len(kinds)
     nrow = 0
@@ -74,6 +84,10 @@ def run(kinds, NS, seed, conv_wait=True, naive_ra_phase=False):
     fullb = [Bar() for _ in range(NS)]
     conv = [Bar() for _ in range(NS)]
     free = [Bar() for _ in range(NS)]
+    cfull = [Bar() for _ in range(NC)]
+    cfree = [Bar() for _ in range(NC)]
+    c_owner = [None] * NC        # unit whose packed codes are in the code slot, until the converters read them
+    codes_read, landed_c = set(), set()
     a_owner = [None] * NS        # unit whose A tile is in the slot, until its MMAs complete
     b_owner = [None] * NS        # unit whose B operand is in the slot, until its MMAs complete
     mma_done = set()
@@ -106,10 +120,29 @@ def run(kinds, NS, seed, conv_wait=True, naive_ra_phase=False):
                     fullb[sl].k += 1
                 pending.append(land_b)
 
+    def loader():
+        for s in range(nrow):
+            cs = s % NC
+            if s >= NC and cfree_wait:
+                yield cfree[cs], s // NC - 1
+            if c_owner[cs] is not None and c_owner[cs] not in codes_read:
+                raise Unsound("code slot %d overwritten by unit %d before unit %d was read" % (cs, s, c_owner[cs]))
+            c_owner[cs] = s
+
+            def land_c(s=s, cs=cs):
+                landed_c.add(s)
+                cfull[cs].k += 1
+            pending.append(land_c)
+
     def converter():
         # the kernel's converters take the first nrow units as the row units
         for s in range(nrow):
-            sl = s % NS
+            sl, cs = s % NS, s % NC
+            yield cfull[cs], s // NC
+            if s not in landed_c:
+                raise Unsound("the converters read the codes of unit %d still in flight" % s)
+            codes_read.add(s)
+            cfree[cs].k += 1
             if s >= NS and conv_wait:
                 yield free[sl], s // NS - 1
             write(b_owner, s, "B")   # widened codes into the B operand
@@ -132,7 +165,7 @@ def run(kinds, NS, seed, conv_wait=True, naive_ra_phase=False):
                 free[sl].k += 1
             pending.append(commit)
 
-    roles = [producer(), converter(), mma()]
+    roles = [producer(), loader(), converter(), mma()]
     waits = [next(r, None) for r in roles]
     steps = 0
     while any(w is not None for w in waits) or pending:
@@ -165,7 +198,7 @@ def _caught(mixes, NS, **kw):
     caught = 0
     for t, kinds in enumerate(mixes):
         try:
-            run(kinds, NS, seed=t, **kw)
+            run(kinds, NS, seed=t, NC=_consts()["TV_NC"], **kw)
         except (Unsound, AssertionError):
             caught += 1
     return caught
@@ -175,9 +208,10 @@ def test_update_protocol_is_sound():
     c = _consts()
     assert c["conv_wait"], "the converters' wait for the operand slot is missing from update_tc.cuh"
     assert c["ra_phase"], "the MMA thread's fullb phase (ra_phase) is missing from update_tc.cuh"
+    assert c["cfree_wait"] and c["cfull_wait"], "the code ring's waits are missing from update_tc.cuh"
     rnd = random.Random(7)
     for t, kinds in enumerate(_mixes(rnd, 400)):
-        run(kinds, c["TV_NS"], seed=t)
+        run(kinds, c["TV_NS"], seed=t, NC=c["TV_NC"])
 
 
 def test_update_protocol_model_catches_planted_mistakes():
@@ -188,6 +222,8 @@ def test_update_protocol_model_catches_planted_mistakes():
     assert _caught(mixes, NS) == 0
     # converters that write B without waiting for the slot
     assert _caught(mixes, NS, conv_wait=False) > 0
+    # a code loader that refills a slot before the converters have read it
+    assert _caught([k for k in mixes if k.count(0) > 8], NS, cfree_wait=False) > 0
     # a fullb phase that counts the slot's row units as ra uses
     assert _caught(mixes, NS, naive_ra_phase=True) > 0
     # ra units before row units: the kernel's converters and phases assume the opposite
