@@ -19,12 +19,14 @@
 //   warp 8 (one thread) TMA: each stage's B tile (the residual split) and,
 //           for U stages, its A tile (128 x 64 bf16), 128-byte swizzled, into
 //           a raw buffer (NS buffers in flight);
-//   warps 0-7 load the genotype codes of a stage 2-bit packed from global
-//           memory (16 bytes = 64 codes per thread, several stages ahead; the
-//           codes are written once, before the sweep, so the first loads are
-//           issued before the dependency wait) and widen them into one of four
-//           bf16 operands in tensor memory (lane = SNP, tcgen05.st); they take
-//           no part in the raw buffers' hand-offs;
+//   warp 10 (one thread) streams each genotype stage's 2-bit packed codes
+//           (4 KB) into a ring of shared-memory slots by bulk copy, the first
+//           ones before the dependency wait (the codes are written once,
+//           before the sweep);
+//   warps 0-7 take their 16 bytes (64 codes) of a stage from that ring and
+//           widen them into one of four bf16 operands in tensor memory
+//           (lane = SNP, tcgen05.st); they take no part in the raw buffers'
+//           hand-offs;
 //   warp 9 runs the issue loop on warp-uniform values and one elected lane
 //           issues the stage's MMAs (A from tensor memory or, for U stages,
 //           from the raw buffer; B always from the raw buffer) once the
@@ -45,12 +47,12 @@ namespace soda {
 constexpr int TC_TM = 128;       // SNPs per M tile
 constexpr int TC_KC = 128;       // individuals per genotype stage
 constexpr int TC_KU = 64;        // U rows per augmenting stage
-constexpr int TC_THREADS = 320;  // 8 converter warps, the TMA warp, the MMA warp
+constexpr int TC_THREADS = 352;  // 8 converter warps, the TMA warp, the MMA warp, the code loader
 constexpr int TC_CONV = 256;     // converter threads
 constexpr int TC_CONV_WARPS = TC_CONV / 32;   // each converter warp arrives once per stage
 constexpr int TC_NOB = 4;        // bf16 codes operands in tensor memory (converters run up to 4 stages ahead)
-constexpr int TC_PF = 4;         // packed code words each converter thread holds in flight
-constexpr int TC_WARP_TMA = 8, TC_WARP_MMA = 9;
+constexpr int TC_NC = 6;         // shared-memory slots of packed codes (4 KB: one genotype stage each)
+constexpr int TC_WARP_TMA = 8, TC_WARP_MMA = 9, TC_WARP_CODES = 10;
 
 template <int CT>
 struct RhsTc {
@@ -60,9 +62,11 @@ struct RhsTc {
     static constexpr int RAW = RAW_A + RAW_B;
     static constexpr uint32_t TX_G = RAW_B;                // bytes a genotype stage loads
     static constexpr uint32_t TX_U = RAW_A + NB * TC_KU * 2;   // bytes an augmenting stage loads
-    static constexpr int NS_FIT = (220 * 1024 - 1024) / RAW;
+    static constexpr int CODE = 2 * 64 * 16 * 2;            // packed codes of a stage: 128 SNPs x 128 individuals
+    static constexpr int NS_FIT = (220 * 1024 - 1024 - TC_NC * CODE) / RAW;
     static constexpr int NS = NS_FIT > 8 ? 8 : NS_FIT;     // raw buffers in flight
-    static constexpr size_t SMEM = 1024 + (size_t)NS * RAW;
+    static constexpr int CODE0 = NS * RAW;
+    static constexpr size_t SMEM = 1024 + (size_t)CODE0 + (size_t)TC_NC * CODE;
     static_assert(RAW % 1024 == 0 && (NB * 128) % 1024 == 0, "buffers and K regions must keep 1024-byte alignment");
     static_assert(NS >= 4, "pipeline too shallow");
 };
@@ -98,6 +102,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     constexpr int NB = T::NB, NS = T::NS;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
     __shared__ uint64_t s_full[NS], s_empty[NS], s_conv[TC_NOB], s_opfree[TC_NOB], s_done;
+    __shared__ uint64_t s_cfull[TC_NC], s_cfree[TC_NC];
     __shared__ uint32_t s_tmem;
     __shared__ int s_err;
     unsigned char *raw0 = smem_dyn + ((1024u - (tc::smem_u32(smem_dyn) & 1023u)) & 1023u);
@@ -130,6 +135,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc::mbar_init(&s_opfree[i], 1);
         }
         tc::mbar_init(&s_done, 1);
+        for (int i = 0; i < TC_NC; ++i) {
+            tc::mbar_init(&s_cfull[i], 1);                // a stage's packed codes landed
+            tc::mbar_init(&s_cfree[i], TC_CONV_WARPS);    // every converter warp has read them
+        }
         tc::mbar_fence_init();
         s_err = 0;
     }
@@ -234,69 +243,82 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (leader) tc::mma_commit(&s_done);
         }
+    } else if (warp == TC_WARP_CODES) {
+        // code loader: one bulk copy (4 KB) of a genotype stage's packed codes per stage into the
+        // ring, issued as slots free.  A packed block is [4 groups of 64 individuals][128 positions]
+        // [16 bytes]; stage t covers individuals 128 (t % 2) .. of tile t / 2, groups 2 (t % 2) and
+        // 2 (t % 2) + 1: one contiguous 4 KB.  The codes are not written by any kernel of the sweep,
+        // so the first copies run before the dependency wait.  Bulk copies stream at DRAM rates that
+        // per-thread loads of the same bytes do not reach (each SM caps its outstanding loads).
+        if (lane == 0) {
+            const unsigned char *blk0 = D.gpk + (size_t)(D.qoff[b] + mt) * D.nvt * TC_PACKED_BLOCK;
+            int issued = 0;
+            for (int s = 0; s < nck; ++s) {
+                const int cs = s % TC_NC, t = t0 + s;
+                if (s == TC_NC) {
+                    // the draw kernel launches once every thread has passed its dependency wait
+                    tc::pdl_wait();
+                    tc::pdl_trigger();
+                }
+                if (s >= TC_NC && !tc::mbar_wait(&s_cfree[cs], ((s / TC_NC) - 1) & 1)) {
+                    s_err = 1;
+                    break;
+                }
+                tc::mbar_expect_tx(&s_cfull[cs], T::CODE);
+                tc::bulk_load(raw0 + T::CODE0 + cs * T::CODE, blk0 + (size_t)(t >> 1) * TC_PACKED_BLOCK + (t & 1) * T::CODE,
+                              T::CODE, &s_cfull[cs]);
+                issued = s + 1;
+            }
+            // no copy may still be in flight into this CTA's shared memory when it exits
+            for (int s = max(0, issued - TC_NC); s < issued; ++s)
+                if (!tc::mbar_wait(&s_cfull[s % TC_NC], (s / TC_NC) & 1)) s_err = 1;
+        }
+        tc::pdl_wait();
+        tc::pdl_trigger();
     } else {
-        // converters: thread (SNP m of the tile, individuals 64 g .. 64 g + 63 of each stage) loads
-        // 16 bytes of packed codes per genotype stage, TC_PF stages ahead, and widens them into one
+        // converters: thread (SNP m of the tile, individuals 64 g .. 64 g + 63 of each stage) takes
+        // 16 bytes of packed codes per genotype stage from the code ring and widens them into one
         // of four bf16 operands in tensor memory (32 columns); they take no part in the raw buffers'
         // hand-offs.  Few, wide converter threads: each stage costs a warp one tensor-memory store,
         // its wait and an arrival, whatever the number of codes it carries.
         const int m = 32 * (warp & 3) + lane, g = warp >> 2;
-        // a packed block is [4 groups of 64 individuals][128 positions][16 bytes]; stage t covers
-        // individuals 128 (t % 2) .. of tile t / 2, so this thread's word is that of group
-        // 2 (t % 2) + g, position m
-        const uint4 *cw = reinterpret_cast<const uint4 *>(D.gpk) + g * TC_TM + m;
-        const size_t blk0 = (size_t)(D.qoff[b] + mt) * D.nvt;
-        auto code_word = [&](int s) -> uint4 {
-            const int t = t0 + s;
-            const uint4 *p = cw + (blk0 + (t >> 1)) * (TC_PACKED_BLOCK / 16) + (t & 1) * (2 * TC_TM);
-            uint4 v;
-            asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-                         : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                         : "l"(p));
-            return v;
-        };
-        uint4 pf[TC_PF];
-#pragma unroll
-        for (int i = 0; i < TC_PF; ++i) pf[i] = i < nck ? code_word(i) : make_uint4(0u, 0u, 0u, 0u);
+        const unsigned char *codes0 = raw0 + T::CODE0 + (g * TC_TM + m) * 16;
         tc::pdl_wait();
         tc::pdl_trigger();
         const uint32_t tl = tm + ((uint32_t)(32 * (warp & 3)) << 16) + 64 + 32 * g;
-        // stage s uses pf[s % TC_PF] and reloads it for stage s + TC_PF: the loop is unrolled by
-        // TC_PF so that every slot stays in its own registers (a shift of the slots would wait for
-        // each load one stage after issuing it)
-        bool stop = false;
-        for (int s0 = 0; s0 < nck && !stop; s0 += TC_PF) {
-#pragma unroll
-            for (int i = 0; i < TC_PF; ++i) {
-                const int s = s0 + i;
-                if (s >= nck || stop) break;
-                const int ob = s % TC_NOB;
-                // the operand buffer was last read by the MMAs of stage s - TC_NOB
-                bool ok = s < TC_NOB || tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
-                ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
-                if (!ok) {
-                    s_err = 1;
-                    stop = true;
-                    break;
-                }
-                tc::fence_after_sync();
-                const uint4 w = pf[i];
-                pf[i] = s + TC_PF < nck ? code_word(s + TC_PF) : make_uint4(0u, 0u, 0u, 0u);
-                uint32_t o[32];
-                tc::codes64_to_bf16(w, o);   // individuals of the stage, two per column
-                uint32_t lo[16], hi[16];
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    lo[e] = o[e];
-                    hi[e] = o[16 + e];
-                }
-                tc::tmem_st16(tl + 64 * ob, lo);
-                tc::tmem_st16(tl + 64 * ob + 16, hi);
-                tc::tmem_wait_st();
-                tc::fence_before_sync();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
+        for (int s = 0; s < nck; ++s) {
+            const int ob = s % TC_NOB, cs = s % TC_NC;
+            bool ok = tc::mbar_wait(&s_cfull[cs], (s / TC_NC) & 1);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                s_err = 1;
+                break;
             }
+            const uint4 w = *reinterpret_cast<const uint4 *>(codes0 + (size_t)cs * T::CODE);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&s_cfree[cs]);   // the slot may be refilled
+            // the operand buffer was last read by the MMAs of stage s - TC_NOB
+            ok = s < TC_NOB || tc::mbar_wait(&s_opfree[ob], ((s - TC_NOB) / TC_NOB) & 1);
+            ok = __all_sync(0xffffffffu, ok);   // the warp arrives as one
+            if (!ok) {
+                s_err = 1;
+                break;
+            }
+            tc::fence_after_sync();
+            uint32_t o[32];
+            tc::codes64_to_bf16(w, o);   // individuals of the stage, two per column
+            uint32_t lo[16], hi[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                lo[e] = o[e];
+                hi[e] = o[16 + e];
+            }
+            tc::tmem_st16(tl + 64 * ob, lo);
+            tc::tmem_st16(tl + 64 * ob + 16, hi);
+            tc::tmem_wait_st();
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&s_conv[ob]);
         }
         if (ns > 0 && !tc::mbar_wait(&s_done, 0)) s_err = 1;
     }

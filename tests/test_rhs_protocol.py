@@ -3,9 +3,11 @@ sodabayes_gb300/csrc/rhs_tc.cuh), as a model run on the CPU, like
 test_update_protocol.py for the residual update.
 
 Roles: the TMA thread loads each stage's B tile, and a U stage's A tile,
-into raw buffer s % NS (one barrier phase per stage); the converter warps
-load a genotype stage's codes from global memory and widen them into
-tensor-memory operand s % NOB and take no part in the raw buffers; the MMA
+into raw buffer s % NS (one barrier phase per stage); a code loader streams
+each genotype stage's packed codes into code slot s % NC (bulk copy, cfull
+completes on arrival) once every converter has read the slot's previous stage
+(cfree); the converter warps take a stage's codes from its slot and widen
+them into tensor-memory operand s % NOB and take no part in the raw buffers; the MMA
 thread reads that operand and the stage's B tile (genotype stages: it waits
 for both) or both raw tiles (U stages, which follow the genotype stages).  A
 raw buffer is free once the MMAs of its stage are done (MMA commit); an
@@ -15,9 +17,10 @@ Checked for every number of stages and genotype/U split, for the kernel's
 NS (computed from its buffer sizes for 4, 8 and 16 chains) and NOB, under
 random interleavings: no parity wait returns a phase early, and no raw
 buffer or operand is overwritten while a reader of its previous contents is
-pending.  Two mistakes planted in the model must be caught: converters that
-do not wait for the MMAs of the operand's previous stage, and an MMA thread
-that takes a genotype stage without waiting for its B tile."""
+pending.  Three mistakes planted in the model must be caught: converters that
+do not wait for the MMAs of the operand's previous stage, a code loader that
+refills a slot before it is read, and an MMA thread that takes a genotype
+stage without waiting for its B tile."""
 import os
 import random
 import re
@@ -29,6 +32,7 @@ SRC = os.path.join(ROOT, "sodabayes_gb300", "csrc", "rhs_tc.cuh")
 def _consts():
     txt = open(SRC).read()
     nob = int(re.search(r"constexpr int TC_NOB = (\d+);", txt).group(1))
+    nc = int(re.search(r"constexpr int TC_NC = (\d+);", txt).group(1))
     tm = int(re.search(r"constexpr int TC_TM = (\d+);", txt).group(1))
     kc = int(re.search(r"constexpr int TC_KC = (\d+);", txt).group(1))
     ku = int(re.search(r"constexpr int TC_KU = (\d+);", txt).group(1))
@@ -36,8 +40,10 @@ def _consts():
     for ct in (4, 8, 16):
         nb = ((3 * ct + 15) // 16) * 16
         raw = tm * ku * 2 + nb * kc * 2
-        ns[ct] = min(8, (220 * 1024 - 1024) // raw)
-    return nob, ns
+        ns[ct] = min(8, (220 * 1024 - 1024 - nc * 4096) // raw)
+    assert "if (s >= TC_NC && !tc::mbar_wait(&s_cfree[cs], ((s / TC_NC) - 1) & 1)) {" in txt
+    assert "bool ok = tc::mbar_wait(&s_cfull[cs], (s / TC_NC) & 1);" in txt
+    return nob, ns, nc
 
 
 class Unsound(AssertionError):
@@ -57,7 +63,7 @@ class Bar:
         return ok
 
 
-def run(ns_total, nck, NS, NOB, seed, skip_opfree=False, skip_bwait=False):
+def run(ns_total, nck, NS, NOB, seed, skip_opfree=False, skip_bwait=False, NC=6, skip_cfree=False):
     rnd = random.Random(seed)
     full = [Bar() for _ in range(NS)]
     empty = [Bar() for _ in range(NS)]   # MMA commit
@@ -66,7 +72,25 @@ def run(ns_total, nck, NS, NOB, seed, skip_opfree=False, skip_bwait=False):
     raw_owner = [None] * NS
     op_owner = [None] * NOB
     mma_done, landed = set(), set()
+    cfull = [Bar() for _ in range(NC)]
+    cfree = [Bar() for _ in range(NC)]
+    c_owner = [None] * NC
+    codes_read, landed_c = set(), set()
     pending = []
+
+    def loader():
+        for s in range(nck):
+            cs = s % NC
+            if s >= NC and not skip_cfree:
+                yield cfree[cs], s // NC - 1
+            if c_owner[cs] is not None and c_owner[cs] not in codes_read:
+                raise Unsound("code slot %d overwritten by stage %d before stage %d was read" % (cs, s, c_owner[cs]))
+            c_owner[cs] = s
+
+            def land_c(s=s, cs=cs):
+                landed_c.add(s)
+                cfull[cs].k += 1
+            pending.append(land_c)
 
     def producer():
         for s in range(ns_total):
@@ -85,7 +109,12 @@ def run(ns_total, nck, NS, NOB, seed, skip_opfree=False, skip_bwait=False):
 
     def converter():
         for s in range(nck):
-            ob = s % NOB
+            ob, cs = s % NOB, s % NC
+            yield cfull[cs], s // NC
+            if s not in landed_c:
+                raise Unsound("the converters read the codes of stage %d still in flight" % s)
+            codes_read.add(s)
+            cfree[cs].k += 1
             if s >= NOB and not skip_opfree:
                 yield opfree[ob], (s - NOB) // NOB
             prev = op_owner[ob]
@@ -113,7 +142,7 @@ def run(ns_total, nck, NS, NOB, seed, skip_opfree=False, skip_bwait=False):
                 empty[buf].k += 1
             pending.append(commit)
 
-    roles = [producer(), converter(), mma()]
+    roles = [producer(), loader(), converter(), mma()]
     waits = [next(r, None) for r in roles]
     steps = 0
     while any(w is not None for w in waits) or pending:
@@ -133,7 +162,7 @@ def run(ns_total, nck, NS, NOB, seed, skip_opfree=False, skip_bwait=False):
 
 
 def test_rhs_protocol_is_sound():
-    nob, ns = _consts()
+    nob, ns, nc = _consts()
     rnd = random.Random(3)
     t = 0
     for ct, NS in ns.items():
@@ -141,20 +170,20 @@ def test_rhs_protocol_is_sound():
         for _ in range(150):
             total = rnd.randint(1, 48)
             nck = rnd.randint(0, total)
-            run(total, nck, NS, nob, seed=t)
+            run(total, nck, NS, nob, seed=t, NC=nc)
             t += 1
 
 
 def test_rhs_protocol_model_catches_a_missing_wait():
     """The mistake planted in the model: converters that do not wait for the
     MMAs of the operand's previous stage."""
-    nob, ns = _consts()
+    nob, ns, nc = _consts()
     rnd = random.Random(5)
     caught = 0
     for t in range(200):
         total = rnd.randint(nob + 1, 48)
         try:
-            run(total, total, ns[16], nob, seed=t, skip_opfree=True)
+            run(total, total, ns[16], nob, seed=t, skip_opfree=True, NC=nc)
         except Unsound:
             caught += 1
     assert caught > 0
@@ -164,13 +193,26 @@ def test_rhs_protocol_model_catches_an_mma_before_its_b_tile():
     """An MMA thread that takes a genotype stage once its codes are converted,
     without waiting for the stage's B tile (the converters no longer wait for
     the raw buffer), must be caught."""
-    nob, ns = _consts()
+    nob, ns, nc = _consts()
     rnd = random.Random(9)
     caught = 0
     for t in range(200):
         total = rnd.randint(1, 48)
         try:
-            run(total, total, ns[16], nob, seed=t, skip_bwait=True)
+            run(total, total, ns[16], nob, seed=t, skip_bwait=True, NC=nc)
+        except Unsound:
+            caught += 1
+    assert caught > 0
+
+
+def test_rhs_protocol_model_catches_a_code_slot_refilled_too_early():
+    nob, ns, nc = _consts()
+    rnd = random.Random(17)
+    caught = 0
+    for t in range(200):
+        total = rnd.randint(nc + 2, 48)
+        try:
+            run(total, total, ns[16], nob, seed=t, NC=nc, skip_cfree=True)
         except Unsound:
             caught += 1
     assert caught > 0
