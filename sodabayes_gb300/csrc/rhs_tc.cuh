@@ -295,6 +295,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 break;
             }
             const uint4 w = *reinterpret_cast<const uint4 *>(codes0 + (size_t)cs * T::CODE);
+            // the next bulk copy (async proxy) overwrites what these generic loads read: order
+            // them first, or the copy can land before the reads (results then vary run to run)
+            tc::fence_async_smem();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&s_cfree[cs]);   // the slot may be refilled
             // the operand buffer was last read by the MMAs of stage s - TC_NOB

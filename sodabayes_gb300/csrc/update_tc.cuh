@@ -658,6 +658,9 @@ __global__ void __launch_bounds__(TV_THREADS, 1)
                     break;
                 }
                 const uint4 w = *reinterpret_cast<const uint4 *>(codes0 + (size_t)cs * T::CODE);
+                // the next bulk copy (async proxy) overwrites what these generic loads read: order
+                // them first, or the copy can land before the reads (results then vary run to run)
+                tc::fence_async_smem();
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(&s_cfree[cs]);   // the slot may be refilled
                 // the first TV_NS units are widened while the draws still run; the next ones wait
